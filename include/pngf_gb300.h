@@ -1,0 +1,209 @@
+/* pngf_gb300 — GB300 (sm_103a) implementation of the PNGF direct-binary-search
+ * hot path: Woodbury tile-flip evaluation and the rank-k accept update over a
+ * precomputed numerical Green's function (NGF) matrix G.
+ *
+ * C ABI. Every call returns a status code (PNGF_OK = 0); pngf_last_error()
+ * gives a message for the last failure on a handle. A handle owns one CUDA
+ * stream and all device memory for every frequency; it is not thread-safe.
+ * Complex numbers are passed as interleaved (re, im) doubles.
+ *
+ * The reference is the header-only C++ class PNGF_Optimizer
+ * (pngf-opt/pngfopt.hpp:18-679) driven by pngf-opt/main.cpp. Each entry point
+ * names the reference member or code block it replaces.
+ *
+ * Algebra. With H = G - I, P the 0/1 design-edge indicator and C = I + P H
+ * (the reference's C = (I-P) + P G, pngfopt.hpp:196-233), the handle keeps,
+ * per frequency, the augmented matrix
+ *     M = [ T  y    ]     T = H C^-1 (N x N),    y = T PEinc,
+ *         [ R  Eobj ]     R = Gobj C^-1 (E x N), Eobj = R PEinc,
+ * instead of C^-1 (pngfopt.hpp:240-249). A flip of the edge set s with signs
+ * d (diag D) needs only gathers of M: its capacitance matrix is
+ * K = I + T[s,s] D (the reference's I + V C^-1 U, pngfopt.hpp:435-455), and
+ * newEobj = Eobj - R[:,s] D (Einc_s + K^-1 w), w = y_s - T[s,s] D Einc_s
+ * (pngfopt.hpp:458-537). Accepting the flip is one rank-k update
+ * M <- M - M[:,s] W with W = [D K^-1 T[s,:] , D (Einc_s + K^-1 w)]
+ * (replaces update_C_inv, pngfopt.hpp:256-367, and compute_R_matrix(0)).
+ */
+#ifndef PNGF_GB300_H
+#define PNGF_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define PNGF_OK 0
+#define PNGF_ERR_ARG 1         /* bad argument (null pointer, size, index) */
+#define PNGF_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define PNGF_ERR_NOMEM 3       /* device or host allocation failed */
+#define PNGF_ERR_IO 4          /* G file missing or short */
+#define PNGF_ERR_SINGULAR 5    /* capacitance matrix K has a zero pivot */
+#define PNGF_ERR_STATE 6       /* call out of order (e.g. accept before eval) */
+#define PNGF_ERR_TIMEOUT 7     /* a bounded device wait ran out */
+#define PNGF_ERR_UNSUPPORTED 8 /* configuration not supported by this build */
+#define PNGF_ERR_NO_DEVICE 9   /* no usable CUDA device / kernel image */
+
+/* ---- precision modes ---- */
+#define PNGF_PREC_FP64 0 /* M in complex128, all arithmetic FP64 */
+#define PNGF_PREC_C64 1  /* M in complex64, rank-k update on tensor cores;
+                            capacitance LU, objective and accept test in FP64 */
+
+#define PNGF_MAX_FREQ 16
+#define PNGF_MAX_EOBJ 4
+
+typedef struct pngf_handle pngf_handle;
+
+/* Problem description. Mirrors the arguments of PNGF_Optimizer::init
+ * (pngfopt.hpp:66-69) plus the constants pngf-opt/main.cpp fixes
+ * (frequencies main.cpp:116-117, k0 main.cpp:162-164). */
+typedef struct pngf_config {
+  int tiles_x, tiles_y;  /* map_xsz, map_ysz */
+  int cells_x, cells_y;  /* Yee cells per tile: tiles_yee_x, tiles_yee_y (3, 3) */
+  int num_eobj;          /* E: rows of Gobj (1 port voltage + 2 NF2FF rows = 3) */
+  int max_flips;         /* most tiles flipped by one candidate (4 for mirror mode) */
+  double dx, dy, dz;     /* Yee cell size, metres */
+  int num_freq;          /* frequencies handled by this handle */
+  double freq_hz[PNGF_MAX_FREQ];
+  int precision;         /* PNGF_PREC_FP64 or PNGF_PREC_C64 */
+  int defer_rank;        /* C64: flush the deferred low-rank correction at this rank (0 = every accept) */
+  int device;            /* CUDA device ordinal */
+} pngf_config;
+
+/* Fills a config with the reference's defaults (main.cpp:142-160):
+ * 3x3 cells per tile, E = 3, dx = dy = 0.01/60 m, dz = 0.01/180 m, FP64. */
+void pngf_config_default(pngf_config *cfg, int tiles_x, int tiles_y, int num_freq,
+                         const double *freq_hz);
+
+/* Number of design edges N for a tile map (pngfopt.hpp:86-94). */
+long pngf_num_edges(int tiles_x, int tiles_y, int cells_x, int cells_y);
+
+/* ---- G matrices (acmefdfd layout: (N+E-1)^2 complex128, column-major) ---- */
+
+/* Synthetic complex-symmetric stand-in for an acmefdfd G: dyadic free-space
+ * Green's function at k = 2 pi f sqrt(eps_r)/c between Yee edge centres,
+ * edge-projected, scaled by dx*dy*dz; diagonal (0.3+0.05i) x row's largest
+ * off-diagonal magnitude; seeded symmetric complex Gaussian relative
+ * perturbation 1e-3. Writes N x N column-major with leading dimension ld. */
+int pngf_synth_G(int tiles_x, int tiles_y, int cells_x, int cells_y, double dx, double dy,
+                 double dz, double freq_hz, double eps_r, unsigned long long seed, double *out,
+                 long ld);
+/* Writes / reads a G file (acmefdfd/main.cpp:533-538, pngfopt.hpp:163-180).
+ * gobj_rows: (num_eobj-1) rows of n complex entries, row-major; NULL = zero. */
+int pngf_write_G_file(const char *path, long n, int num_eobj, const double *G, long ldg,
+                      const double *gobj_rows);
+int pngf_read_G_file(const char *path, long n, int num_eobj, double *G, long ldg,
+                     double *gobj_rows);
+
+/* ---- handle lifecycle ---- */
+
+/* Allocates device state for every frequency. Replaces the constructor and
+ * the buffer sizing of PNGF_Optimizer::init (pngfopt.hpp:66-119). */
+int pngf_create(const pngf_config *cfg, pngf_handle **out);
+int pngf_destroy(pngf_handle *h);
+/* Runs all later work on this CUDA stream (cudaStream_t); NULL = the handle's own. */
+int pngf_set_stream(pngf_handle *h, void *cuda_stream);
+const char *pngf_last_error(const pngf_handle *h);
+/* N (edges) and the leading dimension of the device matrix M. */
+int pngf_dims(const pngf_handle *h, long *n_edges, long *ld_m);
+
+/* Loads frequency f's G from host memory (column-major, leading dimension
+ * ldg) and the E-1 objective rows (row-major, may be NULL = zero). Replaces
+ * the file read of PNGF_Optimizer::init (pngfopt.hpp:121-184). */
+int pngf_load_G(pngf_handle *h, int f, const double *G, long ldg, const double *gobj_rows);
+/* Same, from an acmefdfd G file. Missing or short file -> PNGF_ERR_IO. */
+int pngf_load_G_file(pngf_handle *h, int f, const char *path);
+
+/* Sets the design (PNGF_Optimizer::set_tile_map, pngfopt.hpp:669-674). */
+int pngf_set_tile_map(pngf_handle *h, const int *tile_map);
+int pngf_get_tile_map(const pngf_handle *h, int *tile_map);
+/* Source port of x-directed edges (set_source_port, pngfopt.hpp:559-618);
+ * an invalid y offset/size is PNGF_ERR_ARG (the reference exits). */
+int pngf_set_source_port(pngf_handle *h, int tile_x, int tile_y, int y_offset, int y_size);
+/* Builds M for the current design at every frequency. Replaces
+ * compute_C_matrix + LinAlg::invertMatrix + compute_PEinc +
+ * compute_R_matrix(1) (main.cpp:244-252; pngfopt.hpp:196-250, 542-552;
+ * linalg.hpp:34-85). */
+int pngf_prepare(pngf_handle *h);
+
+/* Current Eobj (E complex) and the port constants Vinc, LN1inc, LN2inc
+ * (3 complex) of frequency f: the members main.cpp reads (277-284). */
+int pngf_get_eobj(pngf_handle *h, int f, double *eobj, double *vinc_ln);
+/* Objective F = sum_f 200|S11|^2 + (15-D)^2 of the current design
+ * (main.cpp:271-302). */
+int pngf_objective(pngf_handle *h, double *F);
+
+/* ---- hot path ---- */
+
+/* Evaluates ncand candidates at every frequency. Candidate c flips tiles
+ * tiles[c*max_flips .. + nflip[c]-1]. Outputs (host memory, either may be
+ * NULL): new_eobj[(c*num_freq + f)*E] (complex) and F[c]. Also records the
+ * batch so that pngf_accept can apply one of its candidates.
+ * Replaces compute_updated_Eobj (pngfopt.hpp:379-539) and the objective loop
+ * (main.cpp:401-420). */
+int pngf_eval_candidates(pngf_handle *h, const int *tiles, const int *nflip, int ncand,
+                         double *new_eobj, double *F);
+/* Same with device pointers, asynchronous on the handle's stream. d_first,
+ * if not NULL, receives the index of the first candidate with F < F_best
+ * (-1 if none), the accept test of main.cpp:429. */
+int pngf_eval_candidates_device(pngf_handle *h, const int *d_tiles, const int *d_nflip,
+                                int ncand, double *d_new_eobj, double *d_F, double F_best,
+                                int *d_first);
+/* Accepts candidate `cand` of the last evaluated batch at every frequency:
+ * rank-k update of M, then P and the tile map are committed. Replaces
+ * update_C_inv + compute_PEinc + compute_R_matrix(0) (main.cpp:447-452). */
+int pngf_accept(pngf_handle *h, int cand);
+
+/* Largest relative deviation of the maintained M from one rebuilt from G in
+ * FP64 on `ncols` sampled columns (drift check for PNGF_PREC_C64). */
+int pngf_drift_check(pngf_handle *h, int ncols, double *max_rel);
+/* Rebuilds M from G for the current design (drift refresh). */
+int pngf_refresh(pngf_handle *h);
+
+/* ---- DBS driver (host, native): pngf-opt/main.cpp:181-459 ---- */
+
+#define PNGF_DBS_SYMMETRIC 0 /* 4-fold mirror quarter hat, main.cpp:181, 343-392 */
+#define PNGF_DBS_SINGLE 1    /* one tile per candidate over the whole map */
+#define PNGF_INIT_EMPTY 0    /* main.cpp:107 */
+#define PNGF_INIT_RANDOM 1   /* main.cpp:108, 187-208 */
+
+typedef struct pngf_dbs_params {
+  int mode;       /* PNGF_DBS_SYMMETRIC / PNGF_DBS_SINGLE */
+  int init;       /* PNGF_INIT_EMPTY / PNGF_INIT_RANDOM */
+  int seed;       /* MagicHat rng_seed (magichat.hpp:53-75); 0 is rejected */
+  int run_index;
+  long max_evals; /* stop after this many evaluations; 0 = run to convergence */
+  int batch;      /* speculative candidates per launch (0 = whole remaining hat) */
+} pngf_dbs_params;
+
+typedef struct pngf_dbs pngf_dbs;
+
+typedef struct pngf_dbs_stats {
+  long evals;          /* flip evaluations in reference order (main.cpp flip_count) */
+  long accepts;
+  long launched;       /* candidates evaluated on the GPU, speculative included */
+  int converged;       /* hat ran out with no improving flip */
+  double F_init, F_best;
+} pngf_dbs_stats;
+
+/* Draws the initial design (rand_binary per tile, main.cpp:187-208), forces
+ * the port tiles (main.cpp:215-219), sets the source port at the map centre
+ * (main.cpp:241) and prepares every frequency. G must be loaded. */
+int pngf_dbs_begin(pngf_handle *h, const pngf_dbs_params *p, pngf_dbs **out);
+/* One DBS decision: evaluate draws in hat order until the first improving
+ * flip (accepting it, main.cpp:429-456) or until the hat is empty. */
+int pngf_dbs_step(pngf_dbs *d, int *accepted);
+int pngf_dbs_stats_get(const pngf_dbs *d, pngf_dbs_stats *out);
+/* Log of every evaluation in reference order (Logger::record_flip,
+ * logger.hpp:64-73): tile index tx+ty*tiles_x, accept bit, F, F_best and per
+ * frequency (Re S11, Im S11, D). Arrays sized by the caller for `cap` rows;
+ * returns the number of rows in *rows. Any pointer may be NULL. */
+int pngf_dbs_log(const pngf_dbs *d, long cap, int *tile, int *accept, double *F, double *F_best,
+                 double *perf, long *rows);
+/* Writes the log in Logger::save's text format (logger.hpp:75-106). */
+int pngf_dbs_save_log(const pngf_dbs *d, const char *path);
+int pngf_dbs_end(pngf_dbs *d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

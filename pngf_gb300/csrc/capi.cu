@@ -1,0 +1,574 @@
+// C ABI of the PNGF hot path: handle lifecycle, G loading, design setup,
+// candidate evaluation and the accept step. See include/pngf_gb300.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "pngf_internal.h"
+
+namespace pngf {
+
+int set_error(Handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+int cuda_check(Handle *h, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return PNGF_OK;
+  return set_error(h, PNGF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define PNGF_CUDA(h, call)                                   \
+  do {                                                       \
+    const int _rc = cuda_check((h), (call), #call);          \
+    if (_rc != PNGF_OK) return _rc;                          \
+  } while (0)
+
+template <typename T> static int dalloc(Handle *h, T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) return PNGF_OK;
+  const cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), sizeof(T) * count);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(h, PNGF_ERR_NOMEM,
+                     std::string("cudaMalloc of ") + std::to_string(sizeof(T) * count) + " bytes: " +
+                         cudaGetErrorString(e));
+  }
+  return PNGF_OK;
+}
+
+template <typename T> static void dfree(T *&p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+static int edges_per_tile(const pngf_config &c) {
+  return c.cells_x * (c.cells_y + 1) + (c.cells_x + 1) * c.cells_y;
+}
+
+// compute_P_matrix (pngfopt.hpp:624-664): an edge is set when any owning tile is set.
+static void compute_P(const Handle *h, const std::vector<int> &map, std::vector<signed char> &P) {
+  const pngf_config &c = h->cfg;
+  P.assign(h->n, 0);
+  for (int t = 0; t < h->map_sz; ++t) {
+    if (!map[t]) continue;
+    const int ty = t / c.tiles_x, tx = t - ty * c.tiles_x;
+    const long bx = (long)tx * c.cells_x + (long)ty * c.cells_y * h->ex_xsz;
+    const long by = h->nx + (long)tx * c.cells_x + (long)ty * c.cells_y * h->ey_xsz;
+    for (int jj = 0; jj < c.cells_y + 1; ++jj)
+      for (int ii = 0; ii < c.cells_x; ++ii) P[bx + ii + (long)jj * h->ex_xsz] = 1;
+    for (int jj = 0; jj < c.cells_y; ++jj)
+      for (int ii = 0; ii < c.cells_x + 1; ++ii) P[by + ii + (long)jj * h->ey_xsz] = 1;
+  }
+}
+
+static int ensure_cand_cap(Handle *h, int ncand) {
+  if (ncand <= h->cand_cap) return PNGF_OK;
+  const int cap = std::max(ncand, 2 * h->cand_cap);
+  const int nf = h->cfg.num_freq;
+  dfree(h->d_tiles);
+  dfree(h->d_nflip);
+  dfree(h->d_es);
+  dfree(h->d_ed);
+  dfree(h->d_ek);
+  dfree(h->d_new_eobj);
+  dfree(h->d_Ff);
+  dfree(h->d_perf);
+  dfree(h->d_F);
+  dfree(h->d_status);
+  if (h->h_tiles) cudaFreeHost(h->h_tiles);
+  if (h->h_nflip) cudaFreeHost(h->h_nflip);
+  h->h_tiles = h->h_nflip = nullptr;
+  h->cand_cap = 0;
+  int rc;
+  if ((rc = dalloc(h, &h->d_tiles, (size_t)cap * h->cfg.max_flips)) ||
+      (rc = dalloc(h, &h->d_nflip, (size_t)cap)) || (rc = dalloc(h, &h->d_es, (size_t)cap * h->kmax)) ||
+      (rc = dalloc(h, &h->d_ed, (size_t)cap * h->kmax)) || (rc = dalloc(h, &h->d_ek, (size_t)cap)) ||
+      (rc = dalloc(h, &h->d_new_eobj, (size_t)cap * nf * h->E)) || (rc = dalloc(h, &h->d_Ff, (size_t)cap * nf)) ||
+      (rc = dalloc(h, &h->d_perf, (size_t)cap * nf * 3)) || (rc = dalloc(h, &h->d_F, (size_t)cap)) ||
+      (rc = dalloc(h, &h->d_status, (size_t)cap * nf)))
+    return rc;
+  PNGF_CUDA(h, cudaMallocHost(&h->h_tiles, sizeof(int) * (size_t)cap * h->cfg.max_flips));
+  PNGF_CUDA(h, cudaMallocHost(&h->h_nflip, sizeof(int) * (size_t)cap));
+  h->cand_cap = cap;
+  return PNGF_OK;
+}
+
+static int ensure_host_out(Handle *h, size_t doubles) {
+  if (doubles <= h->h_out_cap) return PNGF_OK;
+  if (h->h_out) cudaFreeHost(h->h_out);
+  h->h_out = nullptr;
+  h->h_out_cap = 0;
+  PNGF_CUDA(h, cudaMallocHost(&h->h_out, sizeof(double) * doubles));
+  h->h_out_cap = doubles;
+  return PNGF_OK;
+}
+
+static int check_tiles(Handle *h, const int *tiles, const int *nflip, int ncand) {
+  for (int c = 0; c < ncand; ++c) {
+    if (nflip[c] < 0 || nflip[c] > h->cfg.max_flips)
+      return set_error(h, PNGF_ERR_ARG, "candidate " + std::to_string(c) + ": flip count out of range");
+    for (int i = 0; i < nflip[c]; ++i) {
+      const int t = tiles[(size_t)c * h->cfg.max_flips + i];
+      if (t < 0 || t >= h->map_sz)
+        return set_error(h, PNGF_ERR_ARG, "candidate " + std::to_string(c) + ": tile index out of range");
+    }
+  }
+  return PNGF_OK;
+}
+
+// Evaluates a batch whose tile lists are already in h->d_tiles / h->d_nflip.
+static int eval_resident(Handle *h, int ncand, double F_best) {
+  PNGF_CUDA(h, launch_edge_lists(h, ncand, h->d_tiles, h->d_nflip));
+  PNGF_CUDA(h, launch_eval(h, ncand, F_best));
+  h->batch_n = ncand;
+  h->batch_valid = true;
+  return PNGF_OK;
+}
+
+int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best, EvalOut *out) {
+  if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "pngf_prepare has not been called for this design");
+  if (ncand <= 0) return set_error(h, PNGF_ERR_ARG, "ncand must be positive");
+  int rc;
+  if ((rc = check_tiles(h, tiles, nflip, ncand))) return rc;
+  if ((rc = ensure_cand_cap(h, ncand))) return rc;
+  const int mf = h->cfg.max_flips, nf = h->cfg.num_freq;
+  std::memcpy(h->h_tiles, tiles, sizeof(int) * (size_t)ncand * mf);
+  std::memcpy(h->h_nflip, nflip, sizeof(int) * (size_t)ncand);
+  PNGF_CUDA(h, cudaMemcpyAsync(h->d_tiles, h->h_tiles, sizeof(int) * (size_t)ncand * mf, cudaMemcpyHostToDevice,
+                               h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(h->d_nflip, h->h_nflip, sizeof(int) * (size_t)ncand, cudaMemcpyHostToDevice,
+                               h->stream));
+  if ((rc = eval_resident(h, ncand, F_best))) return rc;
+  h->batch_tiles.assign(tiles, tiles + (size_t)ncand * mf);
+  h->batch_nflip.assign(nflip, nflip + ncand);
+  if (!out) return PNGF_OK;
+  // One pinned block: F, perf, new_eobj (as doubles), then ints first, ek, status.
+  const size_t nF = ncand, nperf = (size_t)ncand * nf * 3, neo = (size_t)ncand * nf * h->E * 2;
+  const size_t nint = 1 + (size_t)ncand + (size_t)ncand * nf;
+  if ((rc = ensure_host_out(h, nF + nperf + neo + nint))) return rc;
+  double *hF = h->h_out, *hperf = hF + nF, *heo = hperf + nperf;
+  int *hint = reinterpret_cast<int *>(heo + neo);
+  PNGF_CUDA(h, cudaMemcpyAsync(hF, h->d_F, sizeof(double) * nF, cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(hperf, h->d_perf, sizeof(double) * nperf, cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(heo, h->d_new_eobj, sizeof(double) * neo, cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(hint, h->d_first, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(hint + 1, h->d_ek, sizeof(int) * ncand, cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(hint + 1 + ncand, h->d_status, sizeof(int) * ncand * nf, cudaMemcpyDeviceToHost,
+                               h->stream));
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  out->F.assign(hF, hF + nF);
+  out->perf.assign(hperf, hperf + nperf);
+  out->new_eobj.assign(heo, heo + neo);
+  out->first = hint[0];
+  out->k.assign(hint + 1, hint + 1 + ncand);
+  out->status.assign(hint + 1 + ncand, hint + 1 + ncand + (size_t)ncand * nf);
+  return PNGF_OK;
+}
+
+int accept_cand(Handle *h, int c, int k) {
+  if (!h->batch_valid) return set_error(h, PNGF_ERR_STATE, "no evaluated batch to accept from");
+  if (c < 0 || c >= h->batch_n) return set_error(h, PNGF_ERR_ARG, "candidate index outside the last batch");
+  if (k < 0 || k > h->kmax) return set_error(h, PNGF_ERR_ARG, "invalid flipped-edge count");
+  PNGF_CUDA(h, cudaMemsetAsync(h->d_acc_status, 0, sizeof(int), h->stream));
+  for (int f = 0; f < h->cfg.num_freq; ++f)
+    PNGF_CUDA(h, launch_accept_edges(h, f, h->d_es + (size_t)c * h->kmax, h->d_ed + (size_t)c * h->kmax, k));
+  PNGF_CUDA(h, launch_commit(h, c));
+  // host mirror of the design (update_C_inv commits the flip, pngfopt.hpp:360-366)
+  const int mf = h->cfg.max_flips;
+  for (int i = 0; i < h->batch_nflip[c]; ++i) h->tile_map[h->batch_tiles[(size_t)c * mf + i]] ^= 1;
+  compute_P(h, h->tile_map, h->P);
+  h->batch_valid = false;
+  return PNGF_OK;
+}
+
+}  // namespace pngf
+
+using namespace pngf;
+
+static Handle *H(pngf_handle *p) { return reinterpret_cast<Handle *>(p); }
+static const Handle *H(const pngf_handle *p) { return reinterpret_cast<const Handle *>(p); }
+
+extern "C" {
+
+void pngf_config_default(pngf_config *cfg, int tiles_x, int tiles_y, int num_freq, const double *freq_hz) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->tiles_x = tiles_x;
+  cfg->tiles_y = tiles_y;
+  cfg->cells_x = 3;
+  cfg->cells_y = 3;
+  cfg->num_eobj = 3;
+  cfg->max_flips = 4;
+  cfg->dx = 0.01 / 60.0;
+  cfg->dy = 0.01 / 60.0;
+  cfg->dz = 0.01 / 180.0;
+  cfg->num_freq = num_freq;
+  for (int i = 0; i < num_freq && i < PNGF_MAX_FREQ; ++i) cfg->freq_hz[i] = freq_hz ? freq_hz[i] : 30e9;
+  cfg->precision = PNGF_PREC_FP64;
+  cfg->defer_rank = 0;
+  cfg->device = 0;
+}
+
+const char *pngf_last_error(const pngf_handle *h) { return h ? H(h)->err.c_str() : "null handle"; }
+
+int pngf_destroy(pngf_handle *ph) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (Freq &q : h->f) {
+    dfree(q.G);
+    dfree(q.gobj);
+    dfree(q.Einc);
+    dfree(q.M64);
+    dfree(q.M32);
+  }
+  dfree(h->d_fconst);
+  dfree(h->d_M64s);
+  dfree(h->d_M32s);
+  dfree(h->d_Eincs);
+  dfree(h->d_tile_map);
+  dfree(h->d_P);
+  dfree(h->d_tiles);
+  dfree(h->d_nflip);
+  dfree(h->d_es);
+  dfree(h->d_ed);
+  dfree(h->d_ek);
+  dfree(h->d_new_eobj);
+  dfree(h->d_Ff);
+  dfree(h->d_perf);
+  dfree(h->d_F);
+  dfree(h->d_first);
+  dfree(h->d_status);
+  dfree(h->d_A);
+  dfree(h->d_W);
+  dfree(h->d_acc_s);
+  dfree(h->d_acc_d);
+  dfree(h->d_LU);
+  dfree(h->d_piv);
+  dfree(h->d_z);
+  dfree(h->d_acc_status);
+  if (h->h_tiles) cudaFreeHost(h->h_tiles);
+  if (h->h_nflip) cudaFreeHost(h->h_nflip);
+  if (h->h_out) cudaFreeHost(h->h_out);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+  return PNGF_OK;
+}
+
+int pngf_create(const pngf_config *cfg, pngf_handle **out) {
+  if (!cfg || !out) return PNGF_ERR_ARG;
+  *out = nullptr;
+  const pngf_config &c = *cfg;
+  if (c.tiles_x < 3 || c.tiles_y < 3 || c.cells_x < 1 || c.cells_y < 2 || c.num_eobj < 1 ||
+      c.num_eobj > PNGF_MAX_EOBJ || c.num_freq < 1 || c.num_freq > PNGF_MAX_FREQ || c.max_flips < 1 ||
+      c.max_flips > 8 || !(c.dx > 0) || !(c.dy > 0) || !(c.dz > 0))
+    return PNGF_ERR_ARG;
+  if (c.precision != PNGF_PREC_FP64) return PNGF_ERR_UNSUPPORTED;
+  const int kmax = c.max_flips * edges_per_tile(c);
+  if (kmax > kMaxEvalK) return PNGF_ERR_UNSUPPORTED;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= c.device || c.device < 0) {
+    cudaGetLastError();
+    return PNGF_ERR_NO_DEVICE;
+  }
+  if (cudaSetDevice(c.device) != cudaSuccess) return PNGF_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, c.device) != cudaSuccess || prop.major * 10 + prop.minor != 103)
+    return PNGF_ERR_NO_DEVICE;  // this library carries sm_103a code only
+
+  Handle *h = new (std::nothrow) Handle();
+  if (!h) return PNGF_ERR_NOMEM;
+  h->cfg = c;
+  h->n = pngf_num_edges(c.tiles_x, c.tiles_y, c.cells_x, c.cells_y);
+  h->E = c.num_eobj;
+  h->ldm = (h->n + 1 + 15) / 16 * 16;
+  h->map_sz = c.tiles_x * c.tiles_y;
+  h->ex_xsz = c.tiles_x * c.cells_x;
+  h->ex_ysz = c.tiles_y * c.cells_y + 1;
+  h->ey_xsz = c.tiles_x * c.cells_x + 1;
+  h->ey_ysz = c.tiles_y * c.cells_y;
+  h->nx = (long)h->ex_xsz * h->ex_ysz;
+  h->kmax = kmax;
+  h->acc_cap = std::max(kmax, kInitChunk);
+  h->f.resize(c.num_freq);
+  h->h_fconst.resize(c.num_freq);
+  h->tile_map.assign(h->map_sz, 0);
+  h->P.assign(h->n, 0);
+  auto fail = [&](int rc) {
+    pngf_destroy(reinterpret_cast<pngf_handle *>(h));
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess) return fail(PNGF_ERR_CUDA);
+  h->stream = h->own_stream;
+  const long n = h->n, rows = n + h->E;
+  int rc;
+  std::vector<void *> m64(c.num_freq), einc(c.num_freq);
+  for (int f = 0; f < c.num_freq; ++f) {
+    Freq &q = h->f[f];
+    if ((rc = dalloc(h, &q.G, (size_t)n * n)) || (rc = dalloc(h, &q.gobj, (size_t)std::max(1, h->E - 1) * n)) ||
+        (rc = dalloc(h, &q.Einc, (size_t)n)) || (rc = dalloc(h, &q.M64, (size_t)rows * h->ldm)))
+      return fail(rc);
+    m64[f] = q.M64;
+    einc[f] = q.Einc;
+  }
+  if ((rc = dalloc(h, &h->d_fconst, (size_t)c.num_freq)) || (rc = dalloc(h, &h->d_M64s, (size_t)c.num_freq)) ||
+      (rc = dalloc(h, &h->d_M32s, (size_t)c.num_freq)) || (rc = dalloc(h, &h->d_Eincs, (size_t)c.num_freq)) ||
+      (rc = dalloc(h, &h->d_tile_map, (size_t)h->map_sz)) || (rc = dalloc(h, &h->d_P, (size_t)n)) ||
+      (rc = dalloc(h, &h->d_first, 1)) || (rc = dalloc(h, &h->d_A, (size_t)rows * h->acc_cap)) ||
+      (rc = dalloc(h, &h->d_W, (size_t)h->acc_cap * h->ldm)) || (rc = dalloc(h, &h->d_acc_s, (size_t)n)) ||
+      (rc = dalloc(h, &h->d_acc_d, (size_t)n)) || (rc = dalloc(h, &h->d_LU, (size_t)h->acc_cap * h->acc_cap)) ||
+      (rc = dalloc(h, &h->d_piv, (size_t)h->acc_cap)) || (rc = dalloc(h, &h->d_z, (size_t)h->acc_cap)) ||
+      (rc = dalloc(h, &h->d_acc_status, 1)))
+    return fail(rc);
+  if (cudaMemcpy(h->d_M64s, m64.data(), sizeof(void *) * c.num_freq, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(h->d_Eincs, einc.data(), sizeof(void *) * c.num_freq, cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(PNGF_ERR_CUDA);
+  if ((rc = ensure_cand_cap(h, 64))) return fail(rc);
+  *out = reinterpret_cast<pngf_handle *>(h);
+  return PNGF_OK;
+}
+
+int pngf_set_stream(pngf_handle *ph, void *stream) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+  return PNGF_OK;
+}
+
+int pngf_dims(const pngf_handle *ph, long *n_edges, long *ld_m) {
+  const Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  if (n_edges) *n_edges = h->n;
+  if (ld_m) *ld_m = h->ldm;
+  return PNGF_OK;
+}
+
+int pngf_load_G(pngf_handle *ph, int f, const double *G, long ldg, const double *gobj_rows) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  if (f < 0 || f >= h->cfg.num_freq || !G || ldg < h->n) return set_error(h, PNGF_ERR_ARG, "pngf_load_G: bad argument");
+  Freq &q = h->f[f];
+  const long n = h->n;
+  PNGF_CUDA(h, cudaMemcpy2DAsync(q.G, sizeof(double2) * n, G, sizeof(double2) * ldg, sizeof(double2) * n, n,
+                                 cudaMemcpyHostToDevice, h->stream));
+  if (h->E > 1) {
+    if (gobj_rows)
+      PNGF_CUDA(h, cudaMemcpyAsync(q.gobj, gobj_rows, sizeof(double2) * (size_t)(h->E - 1) * n,
+                                   cudaMemcpyHostToDevice, h->stream));
+    else
+      PNGF_CUDA(h, cudaMemsetAsync(q.gobj, 0, sizeof(double2) * (size_t)(h->E - 1) * n, h->stream));
+  }
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  q.loaded = true;
+  h->prepared = false;
+  return PNGF_OK;
+}
+
+int pngf_load_G_file(pngf_handle *ph, int f, const char *path) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  if (f < 0 || f >= h->cfg.num_freq || !path) return set_error(h, PNGF_ERR_ARG, "pngf_load_G_file: bad argument");
+  const long n = h->n;
+  std::vector<double> G, gobj;
+  try {
+    G.resize((size_t)n * n * 2);
+    gobj.resize((size_t)std::max(1, h->E - 1) * n * 2);
+  } catch (...) {
+    return set_error(h, PNGF_ERR_NOMEM, "host buffer for G");
+  }
+  const int rc = pngf_read_G_file(path, n, h->E, G.data(), n, gobj.data());
+  if (rc != PNGF_OK) return set_error(h, rc, std::string("cannot read G file ") + path);
+  return pngf_load_G(ph, f, G.data(), n, h->E > 1 ? gobj.data() : nullptr);
+}
+
+int pngf_set_tile_map(pngf_handle *ph, const int *tile_map) {
+  Handle *h = H(ph);
+  if (!h || !tile_map) return PNGF_ERR_ARG;
+  for (int t = 0; t < h->map_sz; ++t) h->tile_map[t] = tile_map[t] ? 1 : 0;
+  compute_P(h, h->tile_map, h->P);
+  PNGF_CUDA(h, cudaMemcpyAsync(h->d_tile_map, h->tile_map.data(), sizeof(int) * h->map_sz, cudaMemcpyHostToDevice,
+                               h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(h->d_P, h->P.data(), h->n, cudaMemcpyHostToDevice, h->stream));
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->have_map = true;
+  h->prepared = false;
+  h->batch_valid = false;
+  return PNGF_OK;
+}
+
+int pngf_get_tile_map(const pngf_handle *ph, int *tile_map) {
+  const Handle *h = H(ph);
+  if (!h || !tile_map) return PNGF_ERR_ARG;
+  std::copy(h->tile_map.begin(), h->tile_map.end(), tile_map);
+  return PNGF_OK;
+}
+
+int pngf_set_source_port(pngf_handle *ph, int tile_x, int tile_y, int y_offset, int y_size) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  const pngf_config &c = h->cfg;
+  if (y_offset < 0 || y_size < 1 || y_offset + y_size > c.cells_y)
+    return set_error(h, PNGF_ERR_ARG, "set_source_port: invalid port y position and height parameters.");
+  if (tile_x < 0 || tile_x >= c.tiles_x || tile_y < 0 || tile_y >= c.tiles_y)
+    return set_error(h, PNGF_ERR_ARG, "set_source_port: port tile outside the map");
+  h->port.clear();
+  for (int jj = 0; jj < y_size; ++jj)
+    for (int ii = 0; ii < c.cells_x; ++ii)
+      h->port.push_back((long)(tile_x * c.cells_x + ii) + (long)(tile_y * c.cells_y + jj + y_offset) * h->ex_xsz);
+  h->have_port = true;
+  h->prepared = false;
+  return PNGF_OK;
+}
+
+int pngf_prepare(pngf_handle *ph) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  for (int f = 0; f < h->cfg.num_freq; ++f)
+    if (!h->f[f].loaded) return set_error(h, PNGF_ERR_STATE, "G not loaded for frequency " + std::to_string(f));
+  if (!h->have_map) return set_error(h, PNGF_ERR_STATE, "tile map not set");
+  if (!h->have_port) return set_error(h, PNGF_ERR_STATE, "source port not set");
+  // Set edges of the design, ascending; M is built from P = 0 by accepting
+  // them in chunks (every chunk is a +1 flip of those edges).
+  std::vector<int> on;
+  for (long e = 0; e < h->n; ++e)
+    if (h->P[e]) on.push_back((int)e);
+  std::vector<signed char> ones(on.size(), 1);
+  if (!on.empty()) {
+    PNGF_CUDA(h, cudaMemcpyAsync(h->d_acc_s, on.data(), sizeof(int) * on.size(), cudaMemcpyHostToDevice, h->stream));
+    PNGF_CUDA(h, cudaMemcpyAsync(h->d_acc_d, ones.data(), on.size(), cudaMemcpyHostToDevice, h->stream));
+  }
+  PNGF_CUDA(h, cudaMemsetAsync(h->d_acc_status, 0, sizeof(int), h->stream));
+  for (int f = 0; f < h->cfg.num_freq; ++f) {
+    PNGF_CUDA(h, launch_init_M(h, f));
+    for (size_t c0 = 0; c0 < on.size(); c0 += kInitChunk) {
+      const int k = (int)std::min<size_t>(kInitChunk, on.size() - c0);
+      PNGF_CUDA(h, launch_accept_edges(h, f, h->d_acc_s + c0, h->d_acc_d + c0, k));
+    }
+  }
+  int st = 0;
+  PNGF_CUDA(h, cudaMemcpyAsync(&st, h->d_acc_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(h->h_fconst.data(), h->d_fconst, sizeof(FreqConst) * h->cfg.num_freq,
+                               cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (st != PNGF_OK) return set_error(h, st, "singular capacitance matrix while building M for the design");
+  h->prepared = true;
+  h->batch_valid = false;
+  return PNGF_OK;
+}
+
+int pngf_get_eobj(pngf_handle *ph, int f, double *eobj, double *vinc_ln) {
+  Handle *h = H(ph);
+  if (!h || f < 0 || f >= h->cfg.num_freq) return PNGF_ERR_ARG;
+  if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
+  if (eobj)
+    for (int e = 0; e < h->E; ++e)
+      PNGF_CUDA(h, cudaMemcpyAsync(eobj + 2 * e, h->f[f].M64 + (size_t)(h->n + e) * h->ldm + h->n, sizeof(double2),
+                                   cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (vinc_ln) {
+    const FreqConst &c = h->h_fconst[f];
+    const double v[6] = {c.vinc.x, c.vinc.y, c.ln1.x, c.ln1.y, c.ln2.x, c.ln2.y};
+    std::memcpy(vinc_ln, v, sizeof(v));
+  }
+  return PNGF_OK;
+}
+
+int pngf_objective(pngf_handle *ph, double *F) {
+  Handle *h = H(ph);
+  if (!h || !F) return PNGF_ERR_ARG;
+  if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
+  PNGF_CUDA(h, launch_current_objective(h));
+  PNGF_CUDA(h, cudaMemcpyAsync(F, h->d_F, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->batch_valid = false;  // d_F was reused
+  return PNGF_OK;
+}
+
+int pngf_eval_candidates(pngf_handle *ph, const int *tiles, const int *nflip, int ncand, double *new_eobj,
+                         double *F) {
+  Handle *h = H(ph);
+  if (!h || !tiles || !nflip) return PNGF_ERR_ARG;
+  EvalOut o;
+  const int rc = eval_batch(h, tiles, nflip, ncand, -std::numeric_limits<double>::infinity(), &o);
+  if (rc) return rc;
+  if (F) std::copy(o.F.begin(), o.F.end(), F);
+  if (new_eobj) std::copy(o.new_eobj.begin(), o.new_eobj.end(), new_eobj);
+  h->last_k = o.k;
+  h->last_status = o.status;
+  return PNGF_OK;
+}
+
+int pngf_eval_candidates_device(pngf_handle *ph, const int *d_tiles, const int *d_nflip, int ncand,
+                                double *d_new_eobj, double *d_F, double F_best, int *d_first) {
+  Handle *h = H(ph);
+  if (!h || !d_tiles || !d_nflip || ncand <= 0) return PNGF_ERR_ARG;
+  if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
+  int rc;
+  if ((rc = ensure_cand_cap(h, ncand))) return rc;
+  const int mf = h->cfg.max_flips, nf = h->cfg.num_freq;
+  PNGF_CUDA(h, cudaMemcpyAsync(h->d_tiles, d_tiles, sizeof(int) * (size_t)ncand * mf, cudaMemcpyDeviceToDevice,
+                               h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(h->d_nflip, d_nflip, sizeof(int) * ncand, cudaMemcpyDeviceToDevice, h->stream));
+  if ((rc = eval_resident(h, ncand, F_best))) return rc;
+  h->batch_tiles.clear();  // tile lists stay on the device; pngf_accept fetches them
+  h->batch_nflip.clear();
+  if (d_new_eobj)
+    PNGF_CUDA(h, cudaMemcpyAsync(d_new_eobj, h->d_new_eobj, sizeof(double2) * (size_t)ncand * nf * h->E,
+                                 cudaMemcpyDeviceToDevice, h->stream));
+  if (d_F) PNGF_CUDA(h, cudaMemcpyAsync(d_F, h->d_F, sizeof(double) * ncand, cudaMemcpyDeviceToDevice, h->stream));
+  if (d_first) PNGF_CUDA(h, cudaMemcpyAsync(d_first, h->d_first, sizeof(int), cudaMemcpyDeviceToDevice, h->stream));
+  h->last_k.clear();
+  h->last_status.clear();
+  return PNGF_OK;
+}
+
+int pngf_accept(pngf_handle *ph, int cand) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  if (!h->batch_valid) return set_error(h, PNGF_ERR_STATE, "pngf_accept without a preceding evaluation");
+  if (cand < 0 || cand >= h->batch_n) return set_error(h, PNGF_ERR_ARG, "candidate index outside the last batch");
+  const int mf = h->cfg.max_flips, nf = h->cfg.num_freq;
+  if (h->last_k.empty()) {  // device-pointer batch: fetch what the host needs
+    int k = 0, nfl = 0;
+    std::vector<int> st(nf), tl(mf);
+    PNGF_CUDA(h, cudaMemcpyAsync(&k, h->d_ek + cand, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    PNGF_CUDA(h, cudaMemcpyAsync(st.data(), h->d_status + (size_t)cand * nf, sizeof(int) * nf,
+                                 cudaMemcpyDeviceToHost, h->stream));
+    PNGF_CUDA(h, cudaMemcpyAsync(&nfl, h->d_nflip + cand, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    PNGF_CUDA(h, cudaMemcpyAsync(tl.data(), h->d_tiles + (size_t)cand * mf, sizeof(int) * mf,
+                                 cudaMemcpyDeviceToHost, h->stream));
+    PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->batch_tiles.assign((size_t)h->batch_n * mf, 0);
+    h->batch_nflip.assign(h->batch_n, 0);
+    std::copy(tl.begin(), tl.end(), h->batch_tiles.begin() + (size_t)cand * mf);
+    h->batch_nflip[cand] = nfl;
+    for (int f = 0; f < nf; ++f)
+      if (st[f] != PNGF_OK) return set_error(h, st[f], "candidate did not evaluate cleanly; not accepted");
+    return accept_cand(h, cand, k);
+  }
+  for (int f = 0; f < nf; ++f)
+    if (h->last_status[(size_t)cand * nf + f] != PNGF_OK)
+      return set_error(h, h->last_status[(size_t)cand * nf + f], "candidate did not evaluate cleanly; not accepted");
+  return accept_cand(h, cand, h->last_k[cand]);
+}
+
+int pngf_drift_check(pngf_handle *ph, int ncols, double *max_rel) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  (void)ncols;
+  (void)max_rel;
+  return set_error(h, PNGF_ERR_UNSUPPORTED, "drift check applies to PNGF_PREC_C64 handles");
+}
+
+int pngf_refresh(pngf_handle *ph) { return pngf_prepare(ph); }
+
+}  // extern "C"

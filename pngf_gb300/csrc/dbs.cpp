@@ -1,0 +1,327 @@
+// Native DBS driver: the loop of pngf-opt/main.cpp:181-459 over the GPU hot
+// path, with speculative batches.
+//
+// The reference evaluates one draw at a time and accepts the first improving
+// one, then refills the hat (main.cpp:343-456). Here each launch evaluates the
+// next B draws of the hat at once; the decisions are then taken in draw
+// order against the same F_best, so the first improving draw of the batch is
+// exactly the reference's next accept. Draws after it were speculative: the
+// hat (engine state, entries, last_tried) is restored to its state at the
+// start of the batch and replayed up to the accepted draw before being
+// refilled, so the random sequence is the reference's.
+//
+// MagicHat (pngf-opt/magichat.hpp:32-111) uses std::mt19937 and
+// std::uniform_int_distribution<>; its draws depend on the C++ library, so
+// this driver stays in C++ and uses the same two standard components.
+#include <algorithm>
+#include <cstdio>
+#include <fstream>
+#include <limits>
+#include <new>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "pngf_internal.h"
+
+namespace {
+
+class Hat {
+ public:
+  Hat(int seed, int entries) : total_(entries), left_(entries), entry_(entries) {
+    gen_.seed(seed);
+    dis_ = std::uniform_int_distribution<>(0, entries - 1);
+    for (int i = 0; i < entries; ++i) entry_[i] = i;
+  }
+  int rand_binary() { return gen_() & 1; }
+  int draw() {
+    if (left_ <= 0) return -1;
+    dis_.param(std::uniform_int_distribution<int>::param_type(0, left_ - 1));
+    const int idx = dis_(gen_);
+    const int val = entry_[idx];
+    entry_[idx] = entry_[left_ - 1];
+    --left_;
+    return val;
+  }
+  void reset() {
+    for (int i = 0; i < total_; ++i) entry_[i] = i;
+    left_ = total_;
+  }
+  int left() const { return left_; }
+
+ private:
+  int total_, left_;
+  std::vector<int> entry_;
+  std::mt19937 gen_;
+  std::uniform_int_distribution<> dis_;
+};
+
+struct Cand {
+  int log_index;  // tx + ty * tiles_x (what Logger::record_flip stores, main.cpp:426)
+  int nflip;
+  int tiles[4];
+};
+
+}  // namespace
+
+struct pngf_dbs {
+  pngf::Handle *h = nullptr;
+  pngf_dbs_params p{};
+  Hat hat{1, 1};
+  int last_tried = -1;
+  int hat_entries = 0;
+  int mid_x = 0, mid_y = 0, qx = 0;
+  bool converged = false, done = false;
+  double F_init = 0.0, F_best = 0.0;
+  std::vector<double> perf0;
+  long evals = 0, accepts = 0, launched = 0;
+  std::vector<int> init_map;
+  // log
+  std::vector<int> lg_tile, lg_acc;
+  std::vector<double> lg_F, lg_Fb, lg_perf;
+};
+
+namespace {
+
+// Draws the next valid candidate (main.cpp:343-392); false when the hat is empty.
+bool next_candidate(pngf_dbs *d, Cand *c) {
+  const int xsz = d->h->cfg.tiles_x, ysz = d->h->cfg.tiles_y;
+  const bool sym = d->p.mode == PNGF_DBS_SYMMETRIC;
+  while (true) {
+    const int r = d->hat.draw();
+    if (r < 0) return false;
+    int tx, ty;
+    if (sym) {
+      ty = r / d->qx;
+      tx = r - ty * d->qx;
+    } else {
+      ty = r / xsz;
+      tx = r - ty * xsz;
+    }
+    if (r == d->last_tried) continue;
+    if (tx == d->mid_x && ty == d->mid_y) continue;      // source tile
+    if (tx == d->mid_x - 1 && ty == d->mid_y) continue;  // metal next to the source
+    if (!sym && tx == d->mid_x + 1 && ty == d->mid_y) continue;
+    d->last_tried = r;
+    c->log_index = tx + ty * xsz;
+    if (!sym) {
+      c->nflip = 1;
+      c->tiles[0] = tx + ty * xsz;
+    } else if (tx == d->mid_x) {
+      c->nflip = 2;
+      c->tiles[0] = tx + ty * xsz;
+      c->tiles[1] = tx + ((ysz - 1) - ty) * xsz;
+    } else if (ty == d->mid_y) {
+      c->nflip = 2;
+      c->tiles[0] = tx + ty * xsz;
+      c->tiles[1] = ((xsz - 1) - tx) + ty * xsz;
+    } else {
+      c->nflip = 4;
+      c->tiles[0] = tx + ty * xsz;
+      c->tiles[1] = ((xsz - 1) - tx) + ty * xsz;
+      c->tiles[2] = tx + ((ysz - 1) - ty) * xsz;
+      c->tiles[3] = ((xsz - 1) - tx) + ((ysz - 1) - ty) * xsz;
+    }
+    return true;
+  }
+}
+
+void log_row(pngf_dbs *d, const Cand &c, int acc, double F, const double *perf, int nf) {
+  d->lg_tile.push_back(c.log_index);
+  d->lg_acc.push_back(acc);
+  d->lg_F.push_back(F);
+  d->lg_Fb.push_back(d->F_best);
+  d->lg_perf.insert(d->lg_perf.end(), perf, perf + 3 * nf);
+}
+
+}  // namespace
+
+extern "C" {
+
+int pngf_dbs_begin(pngf_handle *ph, const pngf_dbs_params *p, pngf_dbs **out) {
+  pngf::Handle *h = reinterpret_cast<pngf::Handle *>(ph);
+  if (!h || !p || !out) return PNGF_ERR_ARG;
+  *out = nullptr;
+  if (p->seed == 0) return pngf::set_error(h, PNGF_ERR_ARG, "seed 0 (random seed) is not reproducible; pass one");
+  if (p->mode != PNGF_DBS_SYMMETRIC && p->mode != PNGF_DBS_SINGLE) return PNGF_ERR_ARG;
+  const int xsz = h->cfg.tiles_x, ysz = h->cfg.tiles_y;
+  const int need_flips = p->mode == PNGF_DBS_SYMMETRIC ? 4 : 1;
+  if (h->cfg.max_flips < need_flips)
+    return pngf::set_error(h, PNGF_ERR_ARG, "handle max_flips too small for this candidate mode");
+  pngf_dbs *d = new (std::nothrow) pngf_dbs();
+  if (!d) return PNGF_ERR_NOMEM;
+  d->h = h;
+  d->p = *p;
+  d->qx = (int)((xsz - 1) * 0.5 + 1);
+  const int qy = (int)((ysz - 1) * 0.5 + 1);
+  d->hat_entries = p->mode == PNGF_DBS_SYMMETRIC ? d->qx * qy - 1 : xsz * ysz;  // main.cpp:181
+  d->hat = Hat(p->seed, d->hat_entries);
+  std::vector<int> tm(xsz * ysz, 0);
+  if (p->init == PNGF_INIT_RANDOM) {
+    if (p->mode == PNGF_DBS_SYMMETRIC) {  // main.cpp:187-208
+      for (int j = 0; j < (ysz - 1) * 0.5 + 1; j++)
+        for (int i = 0; i < (xsz - 1) * 0.5 + 1; i++) {
+          const int st = d->hat.rand_binary();
+          tm[i + j * xsz] = st;
+          if (i < (xsz - 1) * 0.5) tm[((xsz - 1) - i) + j * xsz] = st;
+          if (j < (ysz - 1) * 0.5) {
+            tm[i + ((ysz - 1) - j) * xsz] = st;
+            if (i < (xsz - 1) * 0.5) tm[((xsz - 1) - i) + ((ysz - 1) - j) * xsz] = st;
+          }
+        }
+    } else {
+      for (int i = 0; i < xsz * ysz; ++i) tm[i] = d->hat.rand_binary();
+    }
+  }
+  d->mid_x = (int)((xsz - 1) * 0.5);
+  d->mid_y = (int)((ysz - 1) * 0.5);
+  tm[d->mid_y * xsz + d->mid_x - 1] = 1;  // main.cpp:215-219
+  tm[d->mid_y * xsz + d->mid_x + 1] = 1;
+  tm[d->mid_y * xsz + d->mid_x] = 0;
+  tm[(d->mid_y - 1) * xsz + d->mid_x] = 0;
+  tm[(d->mid_y + 1) * xsz + d->mid_x] = 0;
+  d->init_map = tm;
+  int rc;
+  if ((rc = pngf_set_tile_map(ph, tm.data())) || (rc = pngf_set_source_port(ph, d->mid_x, d->mid_y, 1, 2)) ||
+      (rc = pngf_prepare(ph)) || (rc = pngf_objective(ph, &d->F_best))) {
+    delete d;
+    return rc;
+  }
+  d->perf0.resize(3 * h->cfg.num_freq);
+  cudaMemcpy(d->perf0.data(), h->d_perf, sizeof(double) * d->perf0.size(), cudaMemcpyDeviceToHost);
+  d->F_init = d->F_best;
+  *out = d;
+  return PNGF_OK;
+}
+
+int pngf_dbs_step(pngf_dbs *d, int *accepted) {
+  if (!d) return PNGF_ERR_ARG;
+  if (accepted) *accepted = 0;
+  pngf::Handle *h = d->h;
+  const int nf = h->cfg.num_freq, mf = h->cfg.max_flips;
+  while (!d->done) {
+    long budget = d->p.max_evals > 0 ? d->p.max_evals - d->evals : std::numeric_limits<long>::max();
+    if (budget <= 0) {
+      d->done = true;
+      break;
+    }
+    // Draw a speculative batch in hat order.
+    const Hat hat0 = d->hat;
+    const int last0 = d->last_tried;
+    int B = d->p.batch > 0 ? d->p.batch : std::max(1, d->hat.left());
+    B = (int)std::min<long>(B, budget);
+    std::vector<Cand> cands;
+    cands.reserve(B);
+    bool exhausted = false;
+    while ((int)cands.size() < B) {
+      Cand c;
+      if (!next_candidate(d, &c)) {
+        exhausted = true;
+        break;
+      }
+      cands.push_back(c);
+    }
+    if (cands.empty()) {
+      d->converged = d->done = true;
+      break;
+    }
+    const int nc = (int)cands.size();
+    std::vector<int> tiles((size_t)nc * mf, 0), nflip(nc);
+    for (int i = 0; i < nc; ++i) {
+      nflip[i] = cands[i].nflip;
+      for (int t = 0; t < cands[i].nflip; ++t) tiles[(size_t)i * mf + t] = cands[i].tiles[t];
+    }
+    pngf::EvalOut o;
+    int rc = pngf::eval_batch(h, tiles.data(), nflip.data(), nc, d->F_best, &o);
+    if (rc) return rc;
+    d->launched += nc;
+    const int j = o.first;
+    const int upto = j >= 0 ? j : nc - 1;
+    for (int i = 0; i <= upto; ++i) {
+      for (int f = 0; f < nf; ++f)
+        if (o.status[(size_t)i * nf + f] == PNGF_ERR_ARG)
+          return pngf::set_error(h, PNGF_ERR_ARG, "invalid candidate produced by the driver");
+      log_row(d, cands[i], i == j, o.F[i], o.perf.data() + (size_t)i * nf * 3, nf);
+    }
+    d->evals += upto + 1;
+    if (j >= 0) {
+      if ((rc = pngf::accept_cand(h, j, o.k[j]))) return rc;
+      d->F_best = o.F[j];
+      ++d->accepts;
+      // Replay the hat to just after draw j, then refill it (main.cpp:455).
+      d->hat = hat0;
+      d->last_tried = last0;
+      for (int i = 0; i <= j; ++i) {
+        Cand c;
+        next_candidate(d, &c);
+      }
+      d->hat.reset();
+      if (accepted) *accepted = 1;
+      return PNGF_OK;
+    }
+    if (exhausted) {
+      d->converged = d->done = true;
+      break;
+    }
+  }
+  return PNGF_OK;
+}
+
+int pngf_dbs_stats_get(const pngf_dbs *d, pngf_dbs_stats *out) {
+  if (!d || !out) return PNGF_ERR_ARG;
+  out->evals = d->evals;
+  out->accepts = d->accepts;
+  out->launched = d->launched;
+  out->converged = d->converged ? 1 : 0;
+  out->F_init = d->F_init;
+  out->F_best = d->F_best;
+  return PNGF_OK;
+}
+
+int pngf_dbs_log(const pngf_dbs *d, long cap, int *tile, int *accept, double *F, double *F_best, double *perf,
+                 long *rows) {
+  if (!d) return PNGF_ERR_ARG;
+  const long n = (long)d->lg_tile.size();
+  const long m = std::min(cap, n);
+  const int nf = d->h->cfg.num_freq;
+  if (tile) std::copy(d->lg_tile.begin(), d->lg_tile.begin() + m, tile);
+  if (accept) std::copy(d->lg_acc.begin(), d->lg_acc.begin() + m, accept);
+  if (F) std::copy(d->lg_F.begin(), d->lg_F.begin() + m, F);
+  if (F_best) std::copy(d->lg_Fb.begin(), d->lg_Fb.begin() + m, F_best);
+  if (perf) std::copy(d->lg_perf.begin(), d->lg_perf.begin() + (size_t)m * 3 * nf, perf);
+  if (rows) *rows = n;
+  return PNGF_OK;
+}
+
+// Logger::save's format (logger.hpp:75-106): "seed rows", initial map, one
+// line per record (index, flip index, decision, perf...), final map. The
+// first record is the starting point (main.cpp:328). The final map is the
+// design after the last accept.
+int pngf_dbs_save_log(const pngf_dbs *d, const char *path) {
+  if (!d || !path) return PNGF_ERR_ARG;
+  std::ofstream o(path);
+  if (!o) return PNGF_ERR_IO;
+  const int nf = d->h->cfg.num_freq;
+  const long n = (long)d->lg_tile.size();
+  o << d->p.seed << " " << n + 1 << std::endl;
+  for (int v : d->init_map) o << (v ? "x" : ".");
+  o << std::endl;
+  o << 0 << " " << -1 << " " << -1 << " " << d->F_init << " " << d->F_init << " ";
+  for (int i = 0; i < 3 * nf; ++i) o << d->perf0[i] << " ";
+  o << std::endl;
+  for (long r = 0; r < n; ++r) {
+    o << r + 1 << " " << d->lg_tile[r] << " " << d->lg_acc[r] << " " << d->lg_F[r] << " " << d->lg_Fb[r] << " ";
+    for (int i = 0; i < 3 * nf; ++i) o << d->lg_perf[(size_t)r * 3 * nf + i] << " ";
+    o << std::endl;
+  }
+  for (int v : d->h->tile_map) o << (v ? "x" : ".");
+  o << std::endl;
+  return o ? PNGF_OK : PNGF_ERR_IO;
+}
+
+int pngf_dbs_end(pngf_dbs *d) {
+  delete d;
+  return PNGF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,749 @@
+// FP64 kernels of the PNGF hot path on sm_103a.
+//
+// Layout in HBM, per frequency: M = [[T, y], [R, Eobj]] row-major,
+// (N+E) rows x ldm columns (ldm >= N+1, padded to a multiple of 16 elements);
+// Einc (N); G (N x N column-major, as loaded). P (int8, N) and the tile map
+// are shared by all frequencies.
+//
+// Kernels:
+//   k_init_M        M for P = 0 (T = G - I, R = Gobj, y = 0, Eobj = 0), Einc
+//                   and the port constants (pngfopt.hpp:559-618).
+//   k_edge_lists    flipped-edge list of each candidate: the edges whose P
+//                   changes, ascending, with signs (pngfopt.hpp:384-418).
+//   k_eval          one CTA per (candidate, frequency): gathers T[s,s], y_s,
+//                   R[:,s], forms K = I + T[s,s] D, LU with partial pivoting
+//                   in shared memory, solves, forms newEobj and the objective
+//                   term (pngfopt.hpp:379-539 and main.cpp:406-416).
+//   k_score         F = sum over frequencies, first candidate with F < F_best
+//                   (main.cpp:418-429).
+//   k_acc_factor    accept step: K, its LU and z = D (Einc_s + K^-1 w).
+//   k_acc_W         W = [D K^-1 M[s, 0:N], z] (k x (N+1)).
+//   k_acc_gather    A = M[:, s] ((N+E) x k, column-major).
+//   k_rank_update   M -= A W (replaces update_C_inv's zgemm, pngfopt.hpp:350-358,
+//                   and compute_R_matrix(0)).
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "pngf_internal.h"
+
+namespace pngf {
+
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a - b*c
+__device__ __forceinline__ double2 cfnma(double2 a, double2 b, double2 c) {
+  return make_double2(a.x - b.x * c.x + b.y * c.y, a.y - b.x * c.y - b.y * c.x);
+}
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  const double den = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+
+template <typename T> __device__ __forceinline__ double2 ldM(const T *M, size_t i);
+template <> __device__ __forceinline__ double2 ldM<double2>(const double2 *M, size_t i) { return M[i]; }
+template <> __device__ __forceinline__ double2 ldM<float2>(const float2 *M, size_t i) {
+  const float2 v = M[i];
+  return make_double2(v.x, v.y);
+}
+
+struct Geo {
+  int tiles_x, tiles_y, cells_x, cells_y;
+  int ex_xsz, ey_xsz;
+  long nx;
+  int map_sz;
+  int max_flips;
+  int kmax;
+};
+
+struct ObjConst {
+  double dx, dy, dz;
+};
+
+__host__ Geo make_geo(const Handle *h) {
+  Geo g;
+  g.tiles_x = h->cfg.tiles_x;
+  g.tiles_y = h->cfg.tiles_y;
+  g.cells_x = h->cfg.cells_x;
+  g.cells_y = h->cfg.cells_y;
+  g.ex_xsz = h->ex_xsz;
+  g.ey_xsz = h->ey_xsz;
+  g.nx = h->nx;
+  g.map_sz = h->map_sz;
+  g.max_flips = h->cfg.max_flips;
+  g.kmax = h->kmax;
+  return g;
+}
+
+// One frequency's objective term (main.cpp:407-413). perf = (Re S11, Im S11, D).
+__device__ double objective_term(const double2 *eo, int E, const FreqConst &fc, const ObjConst &oc,
+                                 double *perf) {
+  const double2 v = cadd(eo[0], fc.vinc);
+  double2 zin = make_double2(-v.x * oc.dx * 0.5 / (2.0 * oc.dy * oc.dz),
+                             -v.y * oc.dx * 0.5 / (2.0 * oc.dy * oc.dz));
+  const double2 s11 = cdiv(make_double2(zin.x - 50.0, zin.y), make_double2(zin.x + 50.0, zin.y));
+  double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
+  if (E > 1) a = cadd(eo[1], fc.ln1);
+  if (E > 2) b = cadd(eo[2], fc.ln2);
+  const double eta0 = 3.767303134118051e+02;
+  double D = (fc.k0 * fc.k0 / (32.0 * M_PI * M_PI * eta0)) * (a.x * a.x + a.y * a.y + b.x * b.x + b.y * b.y);
+  const double pin = -v.x * oc.dx * 0.5 * (2.0 * oc.dy * oc.dz) * 0.5;
+  D = 4.0 * M_PI * D / pin;
+  const double m = hypot(s11.x, s11.y);
+  perf[0] = s11.x;
+  perf[1] = s11.y;
+  perf[2] = D;
+  return 200.0 * m * m + (15.0 - D) * (15.0 - D);
+}
+
+// ---------------------------------------------------------------------------
+// init
+
+__global__ void k_init_M_tile(const double2 *__restrict__ G, long n, long ldm, double2 *__restrict__ M) {
+  // 32x32 tile transpose: M[i][j] = G(i, j) - delta_ij, G column-major.
+  __shared__ double2 tile[32][33];
+  const long j0 = (long)blockIdx.x * 32, i0 = (long)blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 8
+  for (int r = ty; r < 32; r += 8) {
+    const long j = j0 + r, i = i0 + tx;
+    tile[r][tx] = (i < n && j < n) ? G[(size_t)j * n + i] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const long i = i0 + r, j = j0 + tx;
+    if (i < n && j < ldm) {
+      double2 v = (j < n) ? tile[tx][r] : make_double2(0.0, 0.0);
+      if (i == j) v.x -= 1.0;
+      M[(size_t)i * ldm + j] = v;
+    }
+  }
+}
+
+// Objective rows of M (rows N..N+E-1), Einc, and column N zeroed.
+__global__ void k_init_M_rows(const double2 *__restrict__ G, const double2 *__restrict__ gobj, long n, int E,
+                              long ldm, const long *__restrict__ port, int nport, double2 *__restrict__ M,
+                              double2 *__restrict__ Einc) {
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ldm) return;
+  if (j < n) {
+    double2 g0 = make_double2(0.0, 0.0), e = make_double2(0.0, 0.0);
+    for (int p = 0; p < nport; ++p) {
+      g0 = cadd(g0, G[(size_t)j * n + port[p]]);  // row p of G: Gobj row 0 (pngfopt.hpp:592)
+      e = cadd(e, G[(size_t)port[p] * n + j]);    // column p of G: Einc (pngfopt.hpp:594)
+    }
+    M[(size_t)n * ldm + j] = g0;
+    Einc[j] = e;
+    for (int r = 1; r < E; ++r) M[(size_t)(n + r) * ldm + j] = gobj[(size_t)(r - 1) * n + j];
+  } else {
+    for (int r = 0; r < E; ++r) M[(size_t)(n + r) * ldm + j] = make_double2(0.0, 0.0);
+  }
+  if (j < n + E) M[(size_t)j * ldm + n] = make_double2(0.0, 0.0);  // y = 0, Eobj = 0 for P = 0
+}
+
+__global__ void k_port_const(const double2 *__restrict__ Einc, const double2 *__restrict__ gobj, long n, int E,
+                             const long *__restrict__ port, int nport, double k0, FreqConst *out) {
+  FreqConst c;
+  c.vinc = c.ln1 = c.ln2 = make_double2(0.0, 0.0);
+  for (int p = 0; p < nport; ++p) {
+    if (E > 1) c.ln1 = cadd(c.ln1, gobj[port[p]]);
+    if (E > 2) c.ln2 = cadd(c.ln2, gobj[(size_t)n + port[p]]);
+  }
+  for (int p = 0; p < nport; ++p) c.vinc = cadd(c.vinc, Einc[port[p]]);
+  c.k0 = k0;
+  c.pad = 0.0;
+  *out = c;
+}
+
+// ---------------------------------------------------------------------------
+// candidate edge lists
+
+__device__ __forceinline__ int flipped_parity(const int *tl, int nf, int t) {
+  int p = 0;
+  for (int i = 0; i < nf; ++i) p ^= (tl[i] == t);
+  return p;
+}
+
+// One warp per candidate. Output: es[c*kmax + q], ed[...], ek[c]; ek = -1 on
+// an invalid tile index or flip count.
+__global__ void k_edge_lists(Geo g, int ncand, const int *__restrict__ tiles, const int *__restrict__ nflip,
+                             const int *__restrict__ tile_map, const signed char *__restrict__ P,
+                             int *__restrict__ es, signed char *__restrict__ ed, int *__restrict__ ek) {
+  extern __shared__ int sh[];
+  const int warps = blockDim.x / 32;
+  const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int c = blockIdx.x * warps + w;
+  const int slots = g.max_flips * ((g.cells_x) * (g.cells_y + 1) + (g.cells_x + 1) * g.cells_y);
+  int *cg = sh + w * 2 * slots;          // candidate edge index per slot (-1 = none)
+  int *cd = cg + slots;                  // sign per slot
+  if (c >= ncand) return;
+  const int nfl = nflip[c];
+  const int *tl = tiles + (size_t)c * g.max_flips;
+  bool bad = nfl < 0 || nfl > g.max_flips;
+  for (int i = 0; i < nfl && !bad; ++i) bad = tl[i] < 0 || tl[i] >= g.map_sz;
+  if (bad) {
+    if (lane == 0) ek[c] = -1;
+    return;
+  }
+  const int nex = g.cells_x * (g.cells_y + 1);
+  const int ne = nex + (g.cells_x + 1) * g.cells_y;
+  const int total = nfl * ne;
+  for (int q = lane; q < total; q += 32) {
+    const int t = tl[q / ne], e = q % ne;
+    const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
+    long gi;
+    int o1 = t, o2 = -1;
+    if (e < nex) {
+      const int jj = e / g.cells_x, ii = e % g.cells_x;
+      gi = (long)(tx * g.cells_x + ii) + (long)(ty * g.cells_y + jj) * g.ex_xsz;
+      if (jj == 0 && ty > 0) o2 = t - g.tiles_x;
+      if (jj == g.cells_y && ty + 1 < g.tiles_y) o2 = t + g.tiles_x;
+    } else {
+      const int e2 = e - nex;
+      const int jj = e2 / (g.cells_x + 1), ii = e2 % (g.cells_x + 1);
+      gi = g.nx + (long)(tx * g.cells_x + ii) + (long)(ty * g.cells_y + jj) * g.ey_xsz;
+      if (ii == 0 && tx > 0) o2 = t - 1;
+      if (ii == g.cells_x && tx + 1 < g.tiles_x) o2 = t + 1;
+    }
+    int pn = tile_map[o1] ^ flipped_parity(tl, nfl, o1);
+    if (o2 >= 0) pn |= tile_map[o2] ^ flipped_parity(tl, nfl, o2);
+    const int dv = pn - (int)P[gi];
+    cg[q] = dv != 0 ? (int)gi : -1;
+    cd[q] = dv;
+  }
+  __syncwarp();
+  // Deduplicate (keep first occurrence) and rank by edge index.
+  int cnt = 0;
+  for (int q = lane; q < total; q += 32) {
+    const int gq = cg[q];
+    bool keep = gq >= 0;
+    for (int r = 0; r < q && keep; ++r) keep = cg[r] != gq;
+    if (keep) ++cnt;
+  }
+  for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  for (int q = lane; q < total; q += 32) {
+    const int gq = cg[q];
+    bool keep = gq >= 0;
+    for (int r = 0; r < q && keep; ++r) keep = cg[r] != gq;
+    if (!keep) continue;
+    // rank = number of distinct valid edge indices below gq
+    int rank = 0;
+    for (int r = 0; r < total; ++r) {
+      const int gr = cg[r];
+      if (gr >= 0 && gr < gq) {
+        bool first = true;
+        for (int u = 0; u < r && first; ++u) first = cg[u] != gr;
+        rank += first;
+      }
+    }
+    if (rank < g.kmax) {
+      es[(size_t)c * g.kmax + rank] = gq;
+      ed[(size_t)c * g.kmax + rank] = (signed char)cd[q];
+    }
+  }
+  if (lane == 0) ek[c] = cnt <= g.kmax ? cnt : -1;
+}
+
+// ---------------------------------------------------------------------------
+// cooperative LU of K (column-major, leading dimension ld) in shared memory
+
+// Returns 0 on success, j+1 if pivot j is exactly zero (LAPACK's info).
+__device__ int cta_lu(double2 *K, int ld, int k, int *piv, double *red_v, int *red_i) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  __shared__ int s_info;
+  if (tid == 0) s_info = 0;
+  for (int j = 0; j < k; ++j) {
+    if (tid < 32) {  // pivot: largest |re|+|im| (first on ties), as izamax
+      double bv = -1.0;
+      int bi = j;
+      for (int i = j + tid; i < k; i += 32) {
+        const double v = cabs1(K[i + j * ld]);
+        if (v > bv) { bv = v; bi = i; }
+      }
+      for (int o = 16; o; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+      }
+      if (tid == 0) {
+        piv[j] = bi;
+        red_v[0] = bv;
+        if (bv == 0.0 && s_info == 0) s_info = j + 1;
+      }
+    }
+    __syncthreads();
+    const int p = piv[j];
+    if (p != j)
+      for (int c = tid; c < k; c += nt) {
+        const double2 t = K[j + c * ld];
+        K[j + c * ld] = K[p + c * ld];
+        K[p + c * ld] = t;
+      }
+    __syncthreads();
+    if (red_v[0] != 0.0) {
+      const double2 pv = K[j + j * ld];
+      const double den = pv.x * pv.x + pv.y * pv.y;
+      const double2 r = make_double2(pv.x / den, -pv.y / den);
+      for (int i = j + 1 + tid; i < k; i += nt) K[i + j * ld] = cmul(K[i + j * ld], r);
+    }
+    __syncthreads();
+    const int m = k - j - 1;
+    for (int idx = tid; idx < m * m; idx += nt) {
+      const int i = j + 1 + idx % m, c = j + 1 + idx / m;
+      K[i + c * ld] = cfnma(K[i + c * ld], K[i + j * ld], K[j + c * ld]);
+    }
+    __syncthreads();
+  }
+  (void)red_i;
+  return s_info;
+}
+
+// Solves K x = b in place (b in shared memory) with the LU from cta_lu.
+__device__ void cta_lu_solve(const double2 *K, int ld, int k, const int *piv, double2 *b) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0)
+    for (int j = 0; j < k; ++j) {
+      const int p = piv[j];
+      if (p != j) {
+        const double2 t = b[j];
+        b[j] = b[p];
+        b[p] = t;
+      }
+    }
+  __syncthreads();
+  for (int j = 0; j < k; ++j) {  // unit lower
+    const double2 bj = b[j];
+    for (int i = j + 1 + tid; i < k; i += nt) b[i] = cfnma(b[i], K[i + j * ld], bj);
+    __syncthreads();
+  }
+  for (int j = k - 1; j >= 0; --j) {  // upper
+    if (tid == 0) b[j] = cdiv(b[j], K[j + j * ld]);
+    __syncthreads();
+    const double2 bj = b[j];
+    for (int i = tid; i < j; i += nt) b[i] = cfnma(b[i], K[i + j * ld], bj);
+    __syncthreads();
+  }
+}
+
+// Shared prologue of evaluation and accept: gathers K = I + T[s,s] D and
+// w = y_s - T[s,s] D Einc_s, factors K, solves K x = w and forms
+// z = D (Einc_s + x). Uses shared buffers K (ld x k), vec (k), einc (k),
+// piv (k). Returns LAPACK-style info.
+template <typename TM>
+__device__ int cta_capacitance(const TM *__restrict__ M, long ldm, long n, const double2 *__restrict__ Einc,
+                               const int *s, const signed char *d, int k, double2 *K, int ld, double2 *vec,
+                               double2 *einc, int *piv, double *red) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int c = tid; c < k; c += nt) einc[c] = Einc[s[c]];
+  for (int idx = tid; idx < k * k; idx += nt) {
+    const int r = idx / k, c = idx % k;  // consecutive threads read along a row of M
+    double2 v = ldM(M, (size_t)s[r] * ldm + s[c]);
+    if (d[c] < 0) v = make_double2(-v.x, -v.y);
+    K[r + c * ld] = v;  // T[s,s] D
+  }
+  __syncthreads();
+  for (int r = tid; r < k; r += nt) {
+    double2 w = ldM(M, (size_t)s[r] * ldm + n);
+    for (int c = 0; c < k; ++c) w = cfnma(w, K[r + c * ld], einc[c]);
+    vec[r] = w;
+  }
+  __syncthreads();
+  for (int r = tid; r < k; r += nt) K[r + r * ld].x += 1.0;
+  __syncthreads();
+  const int info = cta_lu(K, ld, k, piv, red, nullptr);
+  if (info == 0) cta_lu_solve(K, ld, k, piv, vec);
+  __syncthreads();
+  for (int c = tid; c < k; c += nt) {
+    double2 z = cadd(einc[c], vec[c]);
+    if (d[c] < 0) z = make_double2(-z.x, -z.y);
+    vec[c] = z;
+  }
+  __syncthreads();
+  return info;
+}
+
+// ---------------------------------------------------------------------------
+// evaluation
+
+template <typename TM>
+__global__ void __launch_bounds__(128) k_eval(const TM *const *__restrict__ Ms, const double2 *const *__restrict__ Eincs,
+                                              long ldm, long n, int E, int kmax, const int *__restrict__ es,
+                                              const signed char *__restrict__ ed, const int *__restrict__ ek,
+                                              const FreqConst *__restrict__ fconst, ObjConst oc, int nf,
+                                              double2 *__restrict__ new_eobj, double *__restrict__ Ff,
+                                              double *__restrict__ perf, int *__restrict__ status) {
+  extern __shared__ double2 smem[];
+  const int c = blockIdx.x, f = blockIdx.y;
+  const int tid = threadIdx.x;
+  const int ld = kmax;  // K is kmax x kmax
+  double2 *K = smem;
+  double2 *vec = K + (size_t)kmax * kmax;
+  double2 *einc = vec + kmax;
+  int *s = reinterpret_cast<int *>(einc + kmax);
+  signed char *d = reinterpret_cast<signed char *>(s + kmax);
+  __shared__ int piv[kMaxK];
+  __shared__ double red[2];
+  __shared__ double2 eo[PNGF_MAX_EOBJ];
+  const TM *M = Ms[f];
+  const int k = ek[c];
+  if (k < 0) {  // invalid candidate
+    if (tid == 0) {
+      Ff[(size_t)c * nf + f] = nan("");
+      status[(size_t)c * nf + f] = PNGF_ERR_ARG;
+    }
+    return;
+  }
+  for (int q = tid; q < k; q += blockDim.x) {
+    s[q] = es[(size_t)c * kmax + q];
+    d[q] = ed[(size_t)c * kmax + q];
+  }
+  __syncthreads();
+  const int info = cta_capacitance(M, ldm, n, Eincs[f], s, d, k, K, ld, vec, einc, piv, red);
+  // newEobj = Eobj - R[:,s] z, one warp per objective row.
+  const int w = tid / 32, lane = tid % 32;
+  for (int e = w; e < E; e += blockDim.x / 32) {
+    double2 acc = make_double2(0.0, 0.0);
+    const size_t row = (size_t)(n + e) * ldm;
+    for (int q = lane; q < k; q += 32) acc = cadd(acc, cmul(ldM(M, row + s[q]), vec[q]));
+    for (int o = 16; o; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane == 0) eo[e] = csub(ldM(M, row + n), acc);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const size_t cf = (size_t)c * nf + f;
+    for (int e = 0; e < E; ++e) new_eobj[cf * E + e] = eo[e];
+    double pf[3];
+    double F = objective_term(eo, E, fconst[f], oc, pf);
+    if (info != 0) F = nan("");
+    Ff[cf] = F;
+    perf[cf * 3 + 0] = pf[0];
+    perf[cf * 3 + 1] = pf[1];
+    perf[cf * 3 + 2] = pf[2];
+    status[cf] = info != 0 ? PNGF_ERR_SINGULAR : PNGF_OK;
+  }
+}
+
+// Sums F over frequencies in frequency order and finds the first candidate
+// with F < F_best (a NaN F never passes, as in the reference's compare).
+__global__ void k_score(int ncand, int nf, const double *__restrict__ Ff, double F_best, double *__restrict__ F,
+                        int *__restrict__ first) {
+  __shared__ int s_first;
+  if (threadIdx.x == 0) s_first = 0x7fffffff;
+  __syncthreads();
+  for (int c = threadIdx.x; c < ncand; c += blockDim.x) {
+    double acc = 0.0;
+    for (int f = 0; f < nf; ++f) acc += Ff[(size_t)c * nf + f];
+    F[c] = acc;
+    if (acc < F_best) atomicMin(&s_first, c);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *first = s_first == 0x7fffffff ? -1 : s_first;
+}
+
+// Objective of the current state (F of the design M encodes) into F[0],
+// per-frequency perf into perf[f*3..].
+template <typename TM>
+__global__ void k_current_objective(const TM *const *__restrict__ Ms, long ldm, long n, int E,
+                                    const FreqConst *__restrict__ fconst, ObjConst oc, int nf, double *F,
+                                    double *perf) {
+  if (threadIdx.x != 0) return;
+  double acc = 0.0;
+  for (int f = 0; f < nf; ++f) {
+    double2 eo[PNGF_MAX_EOBJ];
+    for (int e = 0; e < E; ++e) eo[e] = ldM(Ms[f], (size_t)(n + e) * ldm + n);
+    acc += objective_term(eo, E, fconst[f], oc, perf + 3 * f);
+  }
+  *F = acc;
+}
+
+// ---------------------------------------------------------------------------
+// accept
+
+// One CTA: factors K for the edge list and stores the LU, pivots and z.
+template <typename TM>
+__global__ void __launch_bounds__(256) k_acc_factor(const TM *__restrict__ M, long ldm, long n,
+                                                    const double2 *__restrict__ Einc, const int *__restrict__ gs,
+                                                    const signed char *__restrict__ gd, int k, double2 *__restrict__ LU,
+                                                    int *__restrict__ gpiv, double2 *__restrict__ z,
+                                                    int *__restrict__ status) {
+  extern __shared__ double2 smem[];
+  double2 *K = smem;
+  double2 *vec = K + (size_t)k * k;
+  double2 *einc = vec + k;
+  int *s = reinterpret_cast<int *>(einc + k);
+  signed char *d = reinterpret_cast<signed char *>(s + k);
+  __shared__ int piv[kMaxK];
+  __shared__ double red[2];
+  for (int q = threadIdx.x; q < k; q += blockDim.x) {
+    s[q] = gs[q];
+    d[q] = gd[q];
+  }
+  __syncthreads();
+  const int info = cta_capacitance(M, ldm, n, Einc, s, d, k, K, k, vec, einc, piv, red);
+  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) LU[idx] = K[idx];
+  for (int q = threadIdx.x; q < k; q += blockDim.x) {
+    gpiv[q] = piv[q];
+    z[q] = vec[q];
+  }
+  if (threadIdx.x == 0 && info != 0) *status = PNGF_ERR_SINGULAR;  // sticky until the host clears it
+}
+
+// W[r][j] = d_r (K^-1 M[s, j])_r for j < N, W[r][N] = z_r. One thread per
+// column, blockDim.x (32 or 64) columns per CTA; K's LU in shared memory.
+template <typename TM>
+__global__ void __launch_bounds__(64) k_acc_W(const TM *__restrict__ M, long ldm, long n, const int *__restrict__ gs,
+                                              const signed char *__restrict__ gd, int k, const double2 *__restrict__ LU,
+                                              const int *__restrict__ gpiv, const double2 *__restrict__ z,
+                                              double2 *__restrict__ W, long ldw) {
+  extern __shared__ double2 smem[];
+  double2 *K = smem;                         // k x k
+  double2 *X = K + (size_t)k * k;            // k x bw, column j at X[j*k ..]
+  const int bw = blockDim.x;
+  __shared__ int s[kMaxK];
+  __shared__ int piv[kMaxK];
+  __shared__ signed char d[kMaxK];
+  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) K[idx] = LU[idx];
+  for (int q = threadIdx.x; q < k; q += blockDim.x) {
+    s[q] = gs[q];
+    piv[q] = gpiv[q];
+    d[q] = gd[q];
+  }
+  __syncthreads();
+  const long j0 = (long)blockIdx.x * bw;
+  // coalesced load of the column block of rows s
+  for (int idx = threadIdx.x; idx < k * bw; idx += blockDim.x) {
+    const int r = idx / bw, jj = idx % bw;
+    const long j = j0 + jj;
+    X[(size_t)jj * k + r] = j < n ? ldM(M, (size_t)s[r] * ldm + j) : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  const long j = j0 + threadIdx.x;
+  double2 *x = X + (size_t)threadIdx.x * k;
+  if (j < n) {
+    for (int q = 0; q < k; ++q) {
+      const int p = piv[q];
+      if (p != q) {
+        const double2 t = x[q];
+        x[q] = x[p];
+        x[p] = t;
+      }
+    }
+    for (int q = 0; q < k; ++q) {
+      const double2 xq = x[q];
+      for (int i = q + 1; i < k; ++i) x[i] = cfnma(x[i], K[i + q * k], xq);
+    }
+    for (int q = k - 1; q >= 0; --q) {
+      const double2 xq = cdiv(x[q], K[q + q * k]);
+      x[q] = xq;
+      for (int i = 0; i < q; ++i) x[i] = cfnma(x[i], K[i + q * k], xq);
+    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < k * bw; idx += blockDim.x) {
+    const int r = idx / bw, jj = idx % bw;
+    const long jw = j0 + jj;
+    if (jw < ldw) {
+      double2 v;
+      if (jw < n) {
+        v = X[(size_t)jj * k + r];
+        if (d[r] < 0) v = make_double2(-v.x, -v.y);
+      } else if (jw == n) {
+        v = z[r];
+      } else {
+        v = make_double2(0.0, 0.0);
+      }
+      W[(size_t)r * ldw + jw] = v;
+    }
+  }
+}
+
+// A[i + r*lda] = M[i][s_r], i < N+E.
+template <typename TM>
+__global__ void k_acc_gather(const TM *__restrict__ M, long ldm, long rows, const int *__restrict__ gs, int k,
+                             double2 *__restrict__ A, long lda) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows) return;
+  for (int r = 0; r < k; ++r) A[(size_t)r * lda + i] = ldM(M, (size_t)i * ldm + gs[r]);
+}
+
+// M[i][j] -= sum_r A[i][r] W[r][j] for i < rows, j < cols. 64x64 tile per
+// CTA of 256 threads, 4x4 complex outputs per thread, k in steps of 8.
+constexpr int RU_T = 64, RU_KS = 8;
+__global__ void __launch_bounds__(256) k_rank_update(double2 *__restrict__ M, long ldm, long rows, long cols,
+                                                     const double2 *__restrict__ A, long lda,
+                                                     const double2 *__restrict__ W, long ldw, int k) {
+  __shared__ double2 As[RU_KS][RU_T];
+  __shared__ double2 Ws[RU_KS][RU_T];
+  const int tid = threadIdx.x;
+  const int ti = tid / 16, tj = tid % 16;
+  const long i0 = (long)blockIdx.y * RU_T, j0 = (long)blockIdx.x * RU_T;
+  double2 acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = make_double2(0.0, 0.0);
+  for (int r0 = 0; r0 < k; r0 += RU_KS) {
+    for (int idx = tid; idx < RU_KS * RU_T; idx += 256) {
+      const int rr = idx / RU_T, q = idx % RU_T;
+      const int r = r0 + rr;
+      const long i = i0 + q, j = j0 + q;
+      As[rr][q] = (r < k && i < rows) ? A[(size_t)r * lda + i] : make_double2(0.0, 0.0);
+      Ws[rr][q] = (r < k && j < cols) ? W[(size_t)r * ldw + j] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int rr = 0; rr < RU_KS; ++rr) {
+      double2 a[4], w[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a[q] = As[rr][ti + 16 * q];
+        w[q] = Ws[rr][tj + 16 * q];
+      }
+#pragma unroll
+      for (int qa = 0; qa < 4; ++qa)
+#pragma unroll
+        for (int qb = 0; qb < 4; ++qb) {
+          acc[qa][qb].x = fma(a[qa].x, w[qb].x, acc[qa][qb].x);
+          acc[qa][qb].x = fma(-a[qa].y, w[qb].y, acc[qa][qb].x);
+          acc[qa][qb].y = fma(a[qa].x, w[qb].y, acc[qa][qb].y);
+          acc[qa][qb].y = fma(a[qa].y, w[qb].x, acc[qa][qb].y);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int qa = 0; qa < 4; ++qa) {
+    const long i = i0 + ti + 16 * qa;
+    if (i >= rows) continue;
+#pragma unroll
+    for (int qb = 0; qb < 4; ++qb) {
+      const long j = j0 + tj + 16 * qb;
+      if (j >= cols) continue;
+      double2 *p = M + (size_t)i * ldm + j;
+      *p = csub(*p, acc[qa][qb]);
+    }
+  }
+}
+
+__global__ void k_commit(int kmax, int c, const int *__restrict__ es, const signed char *__restrict__ ed,
+                         const int *__restrict__ ek, int max_flips, const int *__restrict__ tiles,
+                         const int *__restrict__ nflip, signed char *__restrict__ P, int *__restrict__ tile_map) {
+  const int k = ek[c];
+  for (int q = threadIdx.x; q < k; q += blockDim.x) {
+    const int e = es[(size_t)c * kmax + q];
+    P[e] = (signed char)(P[e] + ed[(size_t)c * kmax + q]);
+  }
+  if (threadIdx.x == 0)
+    for (int i = 0; i < nflip[c]; ++i) tile_map[tiles[(size_t)c * max_flips + i]] ^= 1;
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+
+static ObjConst obj_const(const Handle *h) { return ObjConst{h->cfg.dx, h->cfg.dy, h->cfg.dz}; }
+
+cudaError_t launch_init_M(Handle *h, int f) {
+  Freq &q = h->f[f];
+  const long n = h->n;
+  dim3 tb(32, 8), tg((unsigned)((h->ldm + 31) / 32), (unsigned)((n + 31) / 32));
+  k_init_M_tile<<<tg, tb, 0, h->stream>>>(q.G, n, h->ldm, q.M64);
+  long *d_port = nullptr;
+  cudaError_t e = cudaMallocAsync(&d_port, sizeof(long) * h->port.size(), h->stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpyAsync(d_port, h->port.data(), sizeof(long) * h->port.size(), cudaMemcpyHostToDevice, h->stream);
+  if (e != cudaSuccess) return e;
+  k_init_M_rows<<<(unsigned)((h->ldm + 255) / 256), 256, 0, h->stream>>>(q.G, q.gobj, n, h->E, h->ldm, d_port,
+                                                                         (int)h->port.size(), q.M64, q.Einc);
+  const double k0 = 2.0 * M_PI * h->cfg.freq_hz[f] / 2.997924579998211e8;
+  k_port_const<<<1, 1, 0, h->stream>>>(q.Einc, q.gobj, n, h->E, d_port, (int)h->port.size(), k0,
+                                       h->d_fconst + f);
+  cudaFreeAsync(d_port, h->stream);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const int *d_nflip) {
+  const Geo g = make_geo(h);
+  const int slots = g.max_flips * ((g.cells_x) * (g.cells_y + 1) + (g.cells_x + 1) * g.cells_y);
+  const int warps = 4;
+  const size_t sm = sizeof(int) * 2 * slots * warps;
+  k_edge_lists<<<(ncand + warps - 1) / warps, 32 * warps, sm, h->stream>>>(g, ncand, d_tiles, d_nflip, h->d_tile_map,
+                                                                          h->d_P, h->d_es, h->d_ed, h->d_ek);
+  return cudaGetLastError();
+}
+
+static size_t eval_smem(int kmax) {
+  return sizeof(double2) * ((size_t)kmax * kmax + 2 * kmax) + sizeof(int) * kmax + kmax + 16;
+}
+
+template <typename TM> static cudaError_t launch_eval_t(Handle *h, const TM *const *dMs, int ncand) {
+  const int nf = h->cfg.num_freq;
+  const size_t sm = eval_smem(h->kmax);
+  cudaError_t e = cudaFuncSetAttribute(k_eval<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_eval<TM><<<dim3(ncand, nf), 128, sm, h->stream>>>(dMs, reinterpret_cast<const double2 *const *>(h->d_Eincs),
+                                                     h->ldm, h->n, h->E, h->kmax, h->d_es, h->d_ed, h->d_ek,
+                                                     h->d_fconst, obj_const(h), nf, h->d_new_eobj, h->d_Ff,
+                                                     h->d_perf, h->d_status);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_eval(Handle *h, int ncand, double F_best) {
+  cudaError_t e;
+  if (h->cfg.precision == PNGF_PREC_FP64)
+    e = launch_eval_t<double2>(h, reinterpret_cast<const double2 *const *>(h->d_M64s), ncand);
+  else
+    e = launch_eval_t<float2>(h, reinterpret_cast<const float2 *const *>(h->d_M32s), ncand);
+  if (e != cudaSuccess) return e;
+  k_score<<<1, 256, 0, h->stream>>>(ncand, h->cfg.num_freq, h->d_Ff, F_best, h->d_F, h->d_first);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_current_objective(Handle *h) {
+  if (h->cfg.precision == PNGF_PREC_FP64)
+    k_current_objective<double2><<<1, 32, 0, h->stream>>>(reinterpret_cast<const double2 *const *>(h->d_M64s),
+                                                          h->ldm, h->n, h->E, h->d_fconst, obj_const(h),
+                                                          h->cfg.num_freq, h->d_F, h->d_perf);
+  else
+    k_current_objective<float2><<<1, 32, 0, h->stream>>>(reinterpret_cast<const float2 *const *>(h->d_M32s),
+                                                         h->ldm, h->n, h->E, h->d_fconst, obj_const(h),
+                                                         h->cfg.num_freq, h->d_F, h->d_perf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k) {
+  Freq &q = h->f[f];
+  const long n = h->n, rows = n + h->E;
+  if (k <= 0) return cudaSuccess;
+  const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
+  cudaError_t e = cudaFuncSetAttribute(k_acc_factor<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+  if (e != cudaSuccess) return e;
+  k_acc_factor<double2><<<1, 256, smf, h->stream>>>(q.M64, h->ldm, n, q.Einc, d_s, d_d, k, h->d_LU, h->d_piv,
+                                                    h->d_z, h->d_acc_status);
+  const int wc = k <= 64 ? 64 : 32;  // columns per CTA, so that K and the block fit in shared memory
+  const size_t smw = sizeof(double2) * ((size_t)k * k + (size_t)k * wc);
+  e = cudaFuncSetAttribute(k_acc_W<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
+  if (e != cudaSuccess) return e;
+  k_acc_W<double2><<<(unsigned)((h->ldm + wc - 1) / wc), wc, smw, h->stream>>>(q.M64, h->ldm, n, d_s, d_d, k,
+                                                                              h->d_LU, h->d_piv, h->d_z, h->d_W,
+                                                                              h->ldm);
+  k_acc_gather<double2><<<(unsigned)((rows + 255) / 256), 256, 0, h->stream>>>(q.M64, h->ldm, rows, d_s, k, h->d_A,
+                                                                              rows);
+  dim3 g((unsigned)((n + 1 + RU_T - 1) / RU_T), (unsigned)((rows + RU_T - 1) / RU_T));
+  k_rank_update<<<g, 256, 0, h->stream>>>(q.M64, h->ldm, rows, n + 1, h->d_A, rows, h->d_W, h->ldm, k);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_commit(Handle *h, int c) {
+  k_commit<<<1, 128, 0, h->stream>>>(h->kmax, c, h->d_es, h->d_ed, h->d_ek, h->cfg.max_flips, h->d_tiles,
+                                      h->d_nflip, h->d_P, h->d_tile_map);
+  return cudaGetLastError();
+}
+
+}  // namespace pngf

@@ -1,0 +1,130 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pngf_gb300.h"
+
+namespace pngf {
+
+// Largest capacitance matrix a launch handles (edges flipped at once). The
+// candidate kernel keeps K (kmax^2 complex128) in shared memory.
+constexpr int kMaxK = 192;
+// Largest k the candidate kernel supports (K must fit in shared memory).
+constexpr int kMaxEvalK = 104;
+// Edges accepted per chunk when M is built from G for a design.
+constexpr int kInitChunk = 96;
+
+struct FreqConst {   // per-frequency scalars used by the objective
+  double2 vinc, ln1, ln2;
+  double k0;
+  double pad;
+};
+
+struct Freq {
+  double2 *G = nullptr;      // N x N column-major, as loaded (kept for refresh / drift check)
+  double2 *gobj = nullptr;   // (E-1) x N row-major objective rows from the file
+  double2 *Einc = nullptr;   // N
+  double2 *M64 = nullptr;    // (N+E) x ldm row-major, FP64 mode (or FP64 staging)
+  float2 *M32 = nullptr;     // (N+E) x ldm row-major, C64 mode
+  bool loaded = false;
+};
+
+struct Handle {
+  pngf_config cfg{};
+  long n = 0;        // design edges
+  int E = 3;
+  long ldm = 0;      // leading dimension of M (elements)
+  int map_sz = 0;
+  int ex_xsz = 0, ex_ysz = 0, ey_xsz = 0, ey_ysz = 0;
+  long nx = 0;       // number of Ex edges
+  int kmax = 0;      // most edges one candidate flips
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  std::vector<Freq> f;
+  FreqConst *d_fconst = nullptr;
+  void **d_M64s = nullptr;     // device array of per-frequency M64 pointers
+  void **d_M32s = nullptr;     // device array of per-frequency M32 pointers
+  void **d_Eincs = nullptr;    // device array of per-frequency Einc pointers
+  std::vector<FreqConst> h_fconst;
+
+  // design
+  std::vector<int> tile_map;
+  std::vector<signed char> P;
+  std::vector<long> port;
+  int *d_tile_map = nullptr;
+  signed char *d_P = nullptr;
+  bool have_map = false, have_port = false, prepared = false;
+
+  // candidate batch
+  int cand_cap = 0;
+  int *d_tiles = nullptr, *d_nflip = nullptr;   // ncand x max_flips, ncand
+  int *d_es = nullptr;                          // ncand x kmax edge indices
+  signed char *d_ed = nullptr;                  // ncand x kmax signs
+  int *d_ek = nullptr;                          // ncand
+  double2 *d_new_eobj = nullptr;                // ncand x nf x E
+  double *d_Ff = nullptr;                       // ncand x nf
+  double *d_perf = nullptr;                     // ncand x nf x 3 (Re S11, Im S11, D)
+  double *d_F = nullptr;                        // ncand
+  int *d_first = nullptr;
+  int *d_status = nullptr;                      // per-candidate LU status
+  int batch_n = 0;
+  bool batch_valid = false;
+  std::vector<int> batch_tiles, batch_nflip;
+  std::vector<int> last_k, last_status;   // per-candidate edge count / status of the host-API batch
+
+  // accept scratch
+  int acc_cap = 0;                  // columns of A / rows of W
+  double2 *d_A = nullptr;           // (N+E) x acc_cap, column-major (ld = N+E)
+  double2 *d_W = nullptr;           // acc_cap x ldm row-major
+  int *d_acc_s = nullptr;            // explicit edge list (init chunks)
+  signed char *d_acc_d = nullptr;
+  double2 *d_LU = nullptr;          // acc_cap^2
+  int *d_piv = nullptr;             // acc_cap
+  double2 *d_z = nullptr;           // acc_cap
+  int *d_acc_status = nullptr;
+
+  // host staging (pinned)
+  int *h_tiles = nullptr, *h_nflip = nullptr;
+  double *h_out = nullptr;
+  size_t h_out_cap = 0;
+
+  std::string err;
+};
+
+int set_error(Handle *h, int code, const std::string &msg);
+int cuda_check(Handle *h, cudaError_t e, const char *what);
+
+// Host copy of one evaluated batch.
+struct EvalOut {
+  std::vector<double> F;         // ncand
+  std::vector<double> perf;      // ncand x nf x 3
+  std::vector<double> new_eobj;  // ncand x nf x E x 2
+  std::vector<int> k;            // flipped-edge count per candidate (-1 = invalid)
+  std::vector<int> status;       // ncand x nf
+  int first = -1;                // first candidate with F < F_best
+};
+// Evaluates a batch of host tile lists (validated) and reads the results back.
+int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best, EvalOut *out);
+// Applies candidate c (k flipped edges) of the last batch at every frequency.
+int accept_cand(Handle *h, int c, int k);
+
+// ---- kernels (kernels_fp64.cu) ----
+// Builds M for P = 0 from G and the objective rows; computes Einc and the
+// port constants.
+cudaError_t launch_init_M(Handle *h, int f);
+// Per-candidate flipped-edge lists (sorted, deduplicated) from tile lists.
+cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const int *d_nflip);
+// Candidate evaluation + objective at every frequency, then the score.
+cudaError_t launch_eval(Handle *h, int ncand, double F_best);
+// Objective of the current design (from M's Eobj entries) into d_F[0].
+cudaError_t launch_current_objective(Handle *h);
+// Rank-k accept of an explicit edge list (device arrays s, d of length k) at
+// frequency f.
+cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k);
+// Commits P and the tile map on the device for candidate c of the batch.
+cudaError_t launch_commit(Handle *h, int c);
+
+}  // namespace pngf

@@ -1,0 +1,292 @@
+"""ctypes binding of libpngf_gb300.so (the C ABI in include/pngf_gb300.h).
+
+The library is loaded from this package directory. There is no fallback: if
+the shared object is missing, or no sm_103a device is present when a handle
+is created, these calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpngf_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "pngf_gb300.h")
+
+PNGF_OK = 0
+ERRORS = {1: "PNGF_ERR_ARG", 2: "PNGF_ERR_CUDA", 3: "PNGF_ERR_NOMEM", 4: "PNGF_ERR_IO", 5: "PNGF_ERR_SINGULAR",
+          6: "PNGF_ERR_STATE", 7: "PNGF_ERR_TIMEOUT", 8: "PNGF_ERR_UNSUPPORTED", 9: "PNGF_ERR_NO_DEVICE"}
+PREC_FP64, PREC_C64 = 0, 1
+DBS_SYMMETRIC, DBS_SINGLE = 0, 1
+INIT_EMPTY, INIT_RANDOM = 0, 1
+MAX_FREQ = 16
+
+
+class PngfError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [("tiles_x", C.c_int), ("tiles_y", C.c_int), ("cells_x", C.c_int), ("cells_y", C.c_int),
+                ("num_eobj", C.c_int), ("max_flips", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
+                ("dz", C.c_double), ("num_freq", C.c_int), ("freq_hz", C.c_double * MAX_FREQ),
+                ("precision", C.c_int), ("defer_rank", C.c_int), ("device", C.c_int)]
+
+
+class DbsParams(C.Structure):
+    _fields_ = [("mode", C.c_int), ("init", C.c_int), ("seed", C.c_int), ("run_index", C.c_int),
+                ("max_evals", C.c_long), ("batch", C.c_int)]
+
+
+class DbsStats(C.Structure):
+    _fields_ = [("evals", C.c_long), ("accepts", C.c_long), ("launched", C.c_long), ("converged", C.c_int),
+                ("F_init", C.c_double), ("F_best", C.c_double)]
+
+
+_lib = None
+
+
+def load():
+    """Loads the in-tree shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libpngf_gb300.so not built (run __graft_entry__.build() or python -m pngf_gb300.build)")
+    L = C.CDLL(LIB_PATH)
+    P, I, D, L_, V = C.c_void_p, C.c_int, C.c_double, C.c_long, None
+    sig = {
+        "pngf_config_default": (V, [P, I, I, I, P]),
+        "pngf_num_edges": (L_, [I, I, I, I]),
+        "pngf_synth_G": (I, [I, I, I, I, D, D, D, D, D, C.c_ulonglong, P, L_]),
+        "pngf_write_G_file": (I, [C.c_char_p, L_, I, P, L_, P]),
+        "pngf_read_G_file": (I, [C.c_char_p, L_, I, P, L_, P]),
+        "pngf_create": (I, [P, P]),
+        "pngf_destroy": (I, [P]),
+        "pngf_set_stream": (I, [P, P]),
+        "pngf_last_error": (C.c_char_p, [P]),
+        "pngf_dims": (I, [P, P, P]),
+        "pngf_load_G": (I, [P, I, P, L_, P]),
+        "pngf_load_G_file": (I, [P, I, C.c_char_p]),
+        "pngf_set_tile_map": (I, [P, P]),
+        "pngf_get_tile_map": (I, [P, P]),
+        "pngf_set_source_port": (I, [P, I, I, I, I]),
+        "pngf_prepare": (I, [P]),
+        "pngf_get_eobj": (I, [P, I, P, P]),
+        "pngf_objective": (I, [P, P]),
+        "pngf_eval_candidates": (I, [P, P, P, I, P, P]),
+        "pngf_eval_candidates_device": (I, [P, P, P, I, P, P, D, P]),
+        "pngf_accept": (I, [P, I]),
+        "pngf_drift_check": (I, [P, I, P]),
+        "pngf_refresh": (I, [P]),
+        "pngf_dbs_begin": (I, [P, P, P]),
+        "pngf_dbs_step": (I, [P, P]),
+        "pngf_dbs_stats_get": (I, [P, P]),
+        "pngf_dbs_log": (I, [P, L_, P, P, P, P, P, P]),
+        "pngf_dbs_save_log": (I, [P, C.c_char_p]),
+        "pngf_dbs_end": (I, [P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def header_symbols(path: str = HEADER):
+    """Function names declared in the public header."""
+    src = open(path).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"//[^\n]*", "", src)
+    return sorted(set(re.findall(r"\b(pngf_[A-Za-z0-9_]+)\s*\(", src)))
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def num_edges(tiles_x, tiles_y, cells_x=3, cells_y=3):
+    return load().pngf_num_edges(tiles_x, tiles_y, cells_x, cells_y)
+
+
+def synth_G(tiles_x, tiles_y, freq_hz, seed=1, eps_r=2.25, cells=3, dx=0.01 / 60, dy=0.01 / 60, dz=0.01 / 180):
+    """Synthetic complex-symmetric G (N x N, complex128, column-major)."""
+    n = num_edges(tiles_x, tiles_y, cells, cells)
+    G = np.empty((n, n), dtype=np.complex128, order="F")
+    rc = load().pngf_synth_G(tiles_x, tiles_y, cells, cells, dx, dy, dz, freq_hz, eps_r, seed, _ptr(G), n)
+    if rc:
+        raise PngfError(rc, "pngf_synth_G")
+    return G
+
+
+def write_G_file(path, G, gobj_rows=None, num_eobj=3):
+    G = np.asfortranarray(G, dtype=np.complex128)
+    go = None if gobj_rows is None else np.ascontiguousarray(gobj_rows, dtype=np.complex128)
+    rc = load().pngf_write_G_file(path.encode(), G.shape[0], num_eobj, _ptr(G), G.shape[0], _ptr(go))
+    if rc:
+        raise PngfError(rc, "pngf_write_G_file " + path)
+
+
+class Handle:
+    """Owns one pngf_handle (all frequencies of one DBS instance)."""
+
+    def __init__(self, tiles_x, tiles_y, freqs, precision=PREC_FP64, max_flips=4, num_eobj=3, defer_rank=0,
+                 device=0):
+        L = load()
+        self.L = L
+        cfg = Config()
+        fa = (C.c_double * MAX_FREQ)(*freqs)
+        L.pngf_config_default(C.byref(cfg), tiles_x, tiles_y, len(freqs), fa)
+        cfg.max_flips = max_flips
+        cfg.num_eobj = num_eobj
+        cfg.precision = precision
+        cfg.defer_rank = defer_rank
+        cfg.device = device
+        self.cfg = cfg
+        self.nf = len(freqs)
+        self.E = num_eobj
+        self.max_flips = max_flips
+        self.map_sz = tiles_x * tiles_y
+        h = C.c_void_p()
+        rc = L.pngf_create(C.byref(cfg), C.byref(h))
+        if rc:
+            raise PngfError(rc, "pngf_create")
+        self.h = h
+        n, ld = C.c_long(), C.c_long()
+        L.pngf_dims(h, C.byref(n), C.byref(ld))
+        self.n, self.ldm = n.value, ld.value
+
+    def _chk(self, rc, what):
+        if rc:
+            raise PngfError(rc, "%s: %s" % (what, self.L.pngf_last_error(self.h).decode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.pngf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_ptr):
+        self._chk(self.L.pngf_set_stream(self.h, C.c_void_p(stream_ptr)), "pngf_set_stream")
+
+    def load_G(self, f, G, gobj_rows=None):
+        G = np.asfortranarray(G, dtype=np.complex128)
+        go = None if gobj_rows is None else np.ascontiguousarray(gobj_rows, dtype=np.complex128)
+        self._chk(self.L.pngf_load_G(self.h, f, _ptr(G), G.shape[0], _ptr(go)), "pngf_load_G")
+
+    def load_G_file(self, f, path):
+        self._chk(self.L.pngf_load_G_file(self.h, f, path.encode()), "pngf_load_G_file")
+
+    def set_tile_map(self, tm):
+        a = np.ascontiguousarray(tm, dtype=np.int32)
+        self._chk(self.L.pngf_set_tile_map(self.h, _ptr(a)), "pngf_set_tile_map")
+
+    def tile_map(self):
+        a = np.zeros(self.map_sz, dtype=np.int32)
+        self._chk(self.L.pngf_get_tile_map(self.h, _ptr(a)), "pngf_get_tile_map")
+        return a
+
+    def set_source_port(self, tx, ty, yoff=1, ysz=2):
+        self._chk(self.L.pngf_set_source_port(self.h, tx, ty, yoff, ysz), "pngf_set_source_port")
+
+    def prepare(self):
+        self._chk(self.L.pngf_prepare(self.h), "pngf_prepare")
+
+    def eobj(self, f):
+        e = np.zeros(self.E, dtype=np.complex128)
+        v = np.zeros(3, dtype=np.complex128)
+        self._chk(self.L.pngf_get_eobj(self.h, f, _ptr(e), _ptr(v)), "pngf_get_eobj")
+        return e, v
+
+    def objective(self):
+        F = np.zeros(1)
+        self._chk(self.L.pngf_objective(self.h, _ptr(F)), "pngf_objective")
+        return float(F[0])
+
+    def pack(self, cands):
+        t = np.zeros((len(cands), self.max_flips), dtype=np.int32)
+        nfl = np.zeros(len(cands), dtype=np.int32)
+        for i, c in enumerate(cands):
+            t[i, :len(c)] = c
+            nfl[i] = len(c)
+        return t, nfl
+
+    def eval_candidates(self, cands):
+        t, nfl = self.pack(cands)
+        eo = np.zeros((len(cands), self.nf, self.E), dtype=np.complex128)
+        F = np.zeros(len(cands))
+        self._chk(self.L.pngf_eval_candidates(self.h, _ptr(t), _ptr(nfl), len(cands), _ptr(eo), _ptr(F)),
+                  "pngf_eval_candidates")
+        return eo, F
+
+    def accept(self, c):
+        self._chk(self.L.pngf_accept(self.h, c), "pngf_accept")
+
+
+class Dbs:
+    """The native DBS driver over a prepared-able handle (G loaded)."""
+
+    def __init__(self, handle: Handle, mode=DBS_SYMMETRIC, init=INIT_RANDOM, seed=1, max_evals=0, batch=0,
+                 run_index=0):
+        self.hd = handle
+        self.max_evals = max_evals
+        p = DbsParams(mode, init, seed, run_index, max_evals, batch)
+        d = C.c_void_p()
+        handle._chk(handle.L.pngf_dbs_begin(handle.h, C.byref(p), C.byref(d)), "pngf_dbs_begin")
+        self.d = d
+
+    def step(self):
+        a = C.c_int()
+        self.hd._chk(self.hd.L.pngf_dbs_step(self.d, C.byref(a)), "pngf_dbs_step")
+        return bool(a.value)
+
+    def stats(self):
+        s = DbsStats()
+        self.hd._chk(self.hd.L.pngf_dbs_stats_get(self.d, C.byref(s)), "pngf_dbs_stats_get")
+        return s
+
+    def run(self):
+        """Steps until the hat runs out (or the evaluation cap is reached)."""
+        while True:
+            self.step()
+            s = self.stats()
+            if s.converged or (0 < self.max_evals <= s.evals):
+                return s
+
+    def log(self):
+        L, nf = self.hd.L, self.hd.nf
+        rows = C.c_long()
+        L.pngf_dbs_log(self.d, 0, None, None, None, None, None, C.byref(rows))
+        n = rows.value
+        tile = np.zeros(n, dtype=np.int32)
+        acc = np.zeros(n, dtype=np.int32)
+        F = np.zeros(n)
+        Fb = np.zeros(n)
+        perf = np.zeros((n, 3 * nf))
+        L.pngf_dbs_log(self.d, n, _ptr(tile), _ptr(acc), _ptr(F), _ptr(Fb), _ptr(perf), C.byref(rows))
+        return dict(tile=tile, accept=acc, F=F, F_best=Fb, perf=perf)
+
+    def save_log(self, path):
+        self.hd._chk(self.hd.L.pngf_dbs_save_log(self.d, path.encode()), "pngf_dbs_save_log")
+
+    def close(self):
+        if getattr(self, "d", None):
+            self.hd.L.pngf_dbs_end(self.d)
+            self.d = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
