@@ -1,0 +1,393 @@
+#!/usr/bin/env python3
+"""DBS flip-evaluation throughput of the PNGF hot path on GB300.
+
+Workload (the plain wideband case): 21 x 21 tiles of 3 x 3 Yee cells
+(N = 8064 design edges), 5 frequencies (27, 28.5, 30, 31.5, 33 GHz), one
+synthetic complex128 G per frequency, single-tile candidates (441 per pass),
+DBS from a 50%-fill random design drawn from seed 1, plain FP64 form.
+
+A step is one DBS decision through the public C ABI (pngf_dbs_step): the
+next draws of the hat are evaluated at every frequency in one speculative
+launch, the first improving draw in hat order is accepted (rank-k update of
+M at every frequency) and the hat is refilled -- exactly the reference's
+sequence of evaluations and accepts. The metric counts flip evaluations in
+the reference's sense (its flip_count), so speculative evaluations past the
+accepted draw do not count.
+
+  value  flip evals / device time of the hot-path kernels (CUDA events on the
+         handle's stream around each launch group; G and M resident in HBM)
+  e2e    flip evals / wall time of the same steps through the C ABI, host
+         candidate lists in and results out every step
+
+--impl reference times the reference algorithm (the oracle's C restatement
+of pngf-opt/pngfopt.hpp on C^-1, OpenMP + OpenBLAS on every host core) on the
+same workload, same steps.
+
+Multi-GPU (--gpus N under torchrun): one independent DBS instance per GPU
+(seed 1 + rank), no data-path exchange; weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+# The CPU legs run OpenMP loops next to OpenBLAS's own thread pool; idle
+# OpenMP threads must sleep rather than spin or the two pools fight for the
+# cores (measured 4x slower). Set before any OpenMP runtime loads.
+os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
+
+import numpy as np  # noqa: E402
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+FREQS = [27.0e9, 28.5e9, 30.0e9, 31.5e9, 33.0e9]
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "rank_update_fp64_21x21.json")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--tiles", type=int, default=21)
+    ap.add_argument("--mode", choices=["single", "sym"], default="single")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.2)
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(f[1]), smax=float(f[2]), power=float(f[3]), hw=f[5], hwt=f[6], swt=f[7],
+                                 pcap=f[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        reasons = set()
+        for r in rows:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"),
+                              ("swt", "sw_thermal_slowdown"), ("pcap", "sw_power_cap")):
+                if r[key].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in rows), "sm_max_mhz": max(r["smax"] for r in rows),
+                "power_w_max": max(r["power"] for r in rows), "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            return json.load(fh), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def fp64_gemm_peak_tflops():
+    """FP64 GEMM throughput of this GPU (cuBLAS DGEMM through torch, best of 5),
+    the denominator for FP64-pipe-bound kernels (no FP64 figure is in the
+    measured peaks)."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    del a, b
+    torch.cuda.empty_cache()
+    return best
+
+
+def make_Gs(tiles, freqs):
+    from pngf_gb300 import lib
+    return [lib.synth_G(tiles, tiles, f, seed=1) for f in freqs]
+
+
+def cpu_baseline_sample(tiles, mode, seed, freq, gpu_evals, gpu_accepts, nf, budget_s=20.0):
+    """The reference algorithm (C restatement, all host cores) on one of the
+    frequencies: init, then DBS steps until ~budget_s of evaluation/accept work.
+    Returns per-frequency eval and accept times and the modelled throughput on
+    the GPU run's eval/accept mix at nf frequencies."""
+    from oracle.dbs import DbsRunner
+    from oracle.port import threads
+    from pngf_gb300 import lib
+    G = np.ascontiguousarray(lib.synth_G(tiles, tiles, freq, seed=1))
+    gobj = np.zeros((2, G.shape[0]), dtype=np.complex128)
+    t0 = time.perf_counter()
+    r = DbsRunner([G], [gobj], [freq], tiles, tiles, seed, sym=(mode == "sym"), algebra="port")
+    t_init = time.perf_counter() - t0
+    st = r.states[0]
+    acc = {"eval": 0.0, "n_eval": 0, "accept": 0.0, "n_accept": 0}
+    ev, ac = st.eval, st.accept
+
+    def timed_eval(s, d):
+        t = time.perf_counter()
+        out = ev(s, d)
+        acc["eval"] += time.perf_counter() - t
+        acc["n_eval"] += 1
+        return out
+
+    def timed_accept(ne=None):
+        t = time.perf_counter()
+        ac(ne)
+        acc["accept"] += time.perf_counter() - t
+        acc["n_accept"] += 1
+
+    st.eval, st.accept = timed_eval, timed_accept
+    t0 = time.perf_counter()
+    while not r.done and (acc["eval"] + acc["accept"]) < budget_s and (acc["n_accept"] < 8):
+        r.step()
+    wall = time.perf_counter() - t0
+    te = acc["eval"] / max(1, acc["n_eval"])
+    ta = acc["accept"] / max(1, acc["n_accept"])
+    model_s = nf * (gpu_evals * te + gpu_accepts * ta)
+    return {
+        "value": gpu_evals / model_s if model_s > 0 else None,
+        "unit": "flip_evals/s",
+        "cores": threads(),
+        "kind": "port",
+        "sample": ("1 of %d frequencies at %dx%d (N=%d): init %.1f s, then %d evals and %d accepts of the same DBS "
+                   "in %.1f s; per-frequency eval %.2f ms and accept %.0f ms, scaled x%d frequencies and applied to "
+                   "the GPU run's %d evals / %d accepts") % (
+                       nf, tiles, tiles, G.shape[0], t_init, acc["n_eval"], acc["n_accept"], wall, te * 1e3,
+                       ta * 1e3, nf, gpu_evals, gpu_accepts),
+        "eval_ms_per_freq": te * 1e3,
+        "accept_ms_per_freq": ta * 1e3,
+    }
+
+
+def gpu_arm(a, world, rank, local):
+    import torch
+    from pngf_gb300 import lib
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    peaks, peak_src = measured_peaks()
+    fp64_peak = fp64_gemm_peak_tflops()
+    nf = len(FREQS)
+    t_setup = time.perf_counter()
+    Gs = make_Gs(a.tiles, FREQS)
+    h = lib.Handle(a.tiles, a.tiles, FREQS, max_flips=1 if a.mode == "single" else 4, device=local)
+    for f, G in enumerate(Gs):
+        h.load_G(f, G, None)
+    del Gs
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE if a.mode == "single" else lib.DBS_SYMMETRIC, init=lib.INIT_RANDOM,
+                seed=a.seed + rank, batch=0)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(a.warmup):
+        d.step()
+    s0 = d.stats()
+    sampler = ClockSampler(local)
+    sampler.start()
+    h.timing_enable(True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        d.step()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    tm = h.timing()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    s1 = d.stats()
+    evals = s1.evals - s0.evals
+    accepts = s1.accepts - s0.accepts
+    launched = s1.launched - s0.launched
+    dev_s = (tm["eval_ms"] + tm["accept_ms"]) * 1e-3
+    vec = torch.tensor([wall, dev_s, evals, accepts, launched], dtype=torch.float64, device="cuda")
+    if dist:
+        mx = vec.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = vec.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        wall_m, dev_m = mx[0].item(), mx[1].item()
+        evals_t, accepts_t, launched_t = sm[2].item(), sm[3].item(), sm[4].item()
+    else:
+        wall_m, dev_m, evals_t, accepts_t, launched_t = wall, dev_s, evals, accepts, launched
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    n = h.n
+    upd_s = tm["update_ms"] * 1e-3
+    achieved = tm["update_flop"] / upd_s / 1e12 if upd_s > 0 else None
+    traffic = None
+    if os.path.exists(PROFILE_SUMMARY):
+        with open(PROFILE_SUMMARY) as fh:
+            traffic = json.load(fh).get("dram_bytes_per_launch")
+    roofline = {
+        "kernel": "k_rank_update (FP64 complex rank-k update of M, accept step)",
+        "bound": "fp64",
+        "achieved": achieved,
+        "peak": fp64_peak,
+        "unit": "TFLOP/s",
+        "frac": achieved / fp64_peak if achieved else None,
+        "peak_source": "measured on this GPU in this run: cuBLAS DGEMM 4096^3 via torch, best of 5 "
+                       "(MEASURED_PEAKS.json has no FP64 figure)",
+        "traffic": traffic,
+        "algorithmic_flop_per_launch": tm["update_flop"] / max(1, tm["update_launches"]),
+        "algorithmic_bytes_per_launch": tm["update_bytes"] / max(1, tm["update_launches"]),
+        "launch_ms": tm["update_ms"] / max(1, tm["update_launches"]),
+        "hbm_view": {"achieved_gbs": tm["update_bytes"] / upd_s / 1e9 if upd_s > 0 else None,
+                     "peak_gbs": peaks["hbm_gbs"], "peak_source": peak_src},
+        "share_of_device_time": tm["update_ms"] / max(1e-9, tm["eval_ms"] + tm["accept_ms"]),
+    }
+    eval_s = tm["eval_ms"] * 1e-3
+    line = {
+        "metric": "DBS flip evals/s, 21x21 tiles x 5 frequencies, plain FP64 form",
+        "value": evals_t / dev_m if dev_m > 0 else None,
+        "unit": "flip_evals/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": wall_m / a.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {
+            "workload": "wideband %dx%d tiles x %d frequencies (27-33 GHz), N=%d edges, %s-tile DBS from a "
+                        "50%%-fill random design (seed %d), synthetic complex-symmetric dyadic G" % (
+                            a.tiles, a.tiles, nf, n, a.mode, a.seed),
+            "tiles": a.tiles, "freqs_ghz": [f / 1e9 for f in FREQS], "edges": n,
+            "candidates_per_pass": a.tiles * a.tiles if a.mode == "single" else None,
+            "precision": "fp64", "parallelism": "one DBS instance per GPU" if world > 1 else "single GPU",
+            "l2": "inputs larger than L2: M is %.2f GB per frequency" % ((n + 3) * h.ldm * 16 / 1e9),
+            "step": "one DBS decision (speculative batch of the remaining hat, first improving draw accepted)",
+            "value_timing": "sum of CUDA-event spans of the hot-path launch groups on the handle's stream",
+        },
+        "e2e": {"value": evals_t / wall_m, "unit": "flip_evals/s",
+                "h2d_bytes_per_step": tm["h2d_bytes"] / a.steps, "d2h_bytes_per_step": tm["d2h_bytes"] / a.steps},
+        "roofline": roofline,
+        "clocks": clocks,
+        "gpu_launches": tm["kernel_launches"],
+        "detail": {
+            "evals": evals_t, "accepts": accepts_t, "launched_candidates": launched_t,
+            "accepted_updates_per_s": accepts_t / wall_m,
+            "cand_freq_evals_per_s_device": tm["eval_cf"] / eval_s if eval_s > 0 else None,
+            "eval_kernel_gbs": tm["eval_bytes"] / eval_s / 1e9 if eval_s > 0 else None,
+            "eval_kernel_fp64_tflops": tm["eval_flop"] / eval_s / 1e12 if eval_s > 0 else None,
+            "eval_ms": tm["eval_ms"], "accept_ms": tm["accept_ms"], "update_ms": tm["update_ms"],
+            "setup_s": setup_s, "F_init": s1.F_init, "F_best": s1.F_best,
+            "fp64_gemm_tflops": fp64_peak,
+        },
+    }
+    if world == 1 and not a.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(a.tiles, a.mode, a.seed, FREQS[0], evals, accepts, nf)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def reference_arm(a, world, rank):
+    if rank != 0:
+        return
+    from oracle.dbs import DbsRunner
+    from oracle.port import threads
+    nf = len(FREQS)
+    t0 = time.perf_counter()
+    Gs = [np.ascontiguousarray(G) for G in make_Gs(a.tiles, FREQS)]
+    gobj = [np.zeros((2, Gs[0].shape[0]), dtype=np.complex128) for _ in Gs]
+    r = DbsRunner(Gs, gobj, FREQS, a.tiles, a.tiles, a.seed, sym=(a.mode == "sym"), algebra="port")
+    del Gs
+    setup_s = time.perf_counter() - t0
+    for _ in range(a.warmup):
+        r.step()
+    e0 = r.log.evals
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        r.step()
+    wall = time.perf_counter() - t0
+    evals = r.log.evals - e0
+    v = evals / wall
+    line = {
+        "metric": "DBS flip evals/s, 21x21 tiles x 5 frequencies, plain FP64 form",
+        "impl": "reference", "value": v, "unit": "flip_evals/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": wall / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "wideband %dx%d tiles x %d frequencies (27-33 GHz), %s-tile DBS from a 50%%-fill "
+                               "random design (seed %d)" % (a.tiles, a.tiles, nf, a.mode, a.seed),
+                   "step": "one DBS decision (evaluations until the first improving draw, then its accept)"},
+        "cpu_baseline": {"value": v, "unit": "flip_evals/s", "cores": threads(), "kind": "port",
+                         "sample": "%d DBS decisions (%d evals) after %d warm-up decisions, all %d frequencies; "
+                                   "setup (G, LU inverse of C) %.1f s untimed" % (a.steps, evals, a.warmup, nf,
+                                                                                  setup_s)},
+        "e2e": {"value": v, "unit": "flip_evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    world, rank, local = dist_env()
+    if a.impl == "reference":
+        reference_arm(a, world, rank)
+    else:
+        gpu_arm(a, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -159,6 +159,34 @@ int pngf_drift_check(pngf_handle *h, int ncols, double *max_rel);
 /* Rebuilds M from G for the current design (drift refresh). */
 int pngf_refresh(pngf_handle *h);
 
+/* ---- measurement (no reference counterpart: the reference has wall timers only,
+ * pngf-opt/acmetime.hpp:21-50) ---- */
+
+/* Device time of the hot-path kernels, measured with CUDA events recorded on
+ * the handle's stream around each launch group, and the algorithmic work
+ * those launches did. */
+typedef struct pngf_timing {
+  double eval_ms;       /* edge lists + candidate kernel + score */
+  long eval_launches;   /* candidate-kernel launches */
+  double eval_cf;       /* candidate x frequency evaluations */
+  double eval_bytes;    /* algorithmic gather bytes: per (cand, freq) s_M k^2 + 16 (E+2) k + 16 E */
+  double eval_flop;     /* algorithmic FP64 flops: per (cand, freq) 8/3 k^3 + 8 k^2 (2 + ...) */
+  double accept_ms;     /* whole accept step (factor, W solve, gather, update) */
+  long accepts;         /* accept steps (one per frequency) */
+  double update_ms;     /* rank-k update kernel alone */
+  long update_launches;
+  double update_flop;   /* 8 k (N+E)(N+1) per update */
+  double update_bytes;  /* 2 s_M (N+E)(N+1) + 16 k ((N+E) + (N+1)) per update */
+  long kernel_launches; /* every kernel this handle launched while timing was on */
+  double h2d_bytes;     /* host-to-device bytes of candidate batches */
+  double d2h_bytes;     /* device-to-host bytes of batch results */
+} pngf_timing;
+
+/* Turns event timing on (resets the counters) or off. */
+int pngf_timing_enable(pngf_handle *h, int on);
+/* Synchronizes the handle's stream and returns the accumulated counters. */
+int pngf_timing_get(pngf_handle *h, pngf_timing *out);
+
 /* ---- DBS driver (host, native): pngf-opt/main.cpp:181-459 ---- */
 
 #define PNGF_DBS_SYMMETRIC 0 /* 4-fold mirror quarter hat, main.cpp:181, 343-392 */

@@ -108,68 +108,90 @@ class DbsLog:
     converged: bool = False
 
 
-def run_dbs(Gs, gobj_rows, freqs, tiles_x, tiles_y, seed, sym=True, random_init=True,
-            max_evals=0, algebra="ref", run_index=0):
-    """Runs DBS on numpy states. Gs: list of N x N complex G per frequency."""
-    geo = Geometry(tiles_x, tiles_y)
-    hat = MagicHat(seed, run_index, hat_size(geo, sym))
-    tm = initial_design(geo, hat, sym, random_init)
-    P = geo.compute_P(tm)
-    mx, my = int((tiles_x - 1) * 0.5), int((tiles_y - 1) * 0.5)
-    port = geo.port_indices(mx, my, 1, 2)
-    states, consts = [], []
-    for f, G in enumerate(Gs):
-        Gobj, Einc, vinc, ln1, ln2 = port_setup(G, gobj_rows[f], port)
-        if algebra == "ref":
-            st = RefState(G, Gobj, Einc, P)
-        elif algebra == "port":
-            from .port import PortState
-            st = PortState(G, Gobj, Einc, P, kmax=96 if sym else 24)
-        else:
-            st = MState.build(G, Gobj, Einc, P)
-        states.append(st)
-        consts.append((vinc, ln1, ln2, 2.0 * np.pi * freqs[f] / C0))
+class DbsRunner:
+    """DBS on per-frequency CPU states, one decision per ``step()``.
 
-    def score(eobjs):
+    Gs: list of N x N complex G per frequency; algebra: "ref" (numpy on C^-1),
+    "port" (the C restatement on C^-1) or "m" (numpy on M)."""
+
+    def __init__(self, Gs, gobj_rows, freqs, tiles_x, tiles_y, seed, sym=True, random_init=True,
+                 max_evals=0, algebra="ref", run_index=0):
+        self.geo = geo = Geometry(tiles_x, tiles_y)
+        self.sym, self.max_evals, self.algebra = sym, max_evals, algebra
+        self.hat = MagicHat(seed, run_index, hat_size(geo, sym))
+        self.tm = initial_design(geo, self.hat, sym, random_init)
+        self.P = geo.compute_P(self.tm)
+        mx, my = int((tiles_x - 1) * 0.5), int((tiles_y - 1) * 0.5)
+        port = geo.port_indices(mx, my, 1, 2)
+        self.states, self.consts = [], []
+        for f, G in enumerate(Gs):
+            Gobj, Einc, vinc, ln1, ln2 = port_setup(G, gobj_rows[f], port)
+            if algebra == "ref":
+                st = RefState(G, Gobj, Einc, self.P)
+            elif algebra == "port":
+                from .port import PortState
+                st = PortState(G, Gobj, Einc, self.P, kmax=96 if sym else 24)
+            else:
+                st = MState.build(G, Gobj, Einc, self.P)
+            self.states.append(st)
+            self.consts.append((vinc, ln1, ln2, 2.0 * np.pi * freqs[f] / C0))
+        self.F_best, perf0 = self.score([st.Eobj for st in self.states])
+        self.log = DbsLog(init_map=list(self.tm), start_F=self.F_best, start_perf=perf0)
+        self.last = -1
+        self.done = False
+
+    def score(self, eobjs):
         F, perf = 0.0, []
         for f, eo in enumerate(eobjs):
-            vinc, ln1, ln2, k0 = consts[f]
+            vinc, ln1, ln2, k0 = self.consts[f]
             Ff, s11, D = objective(eo, vinc, ln1, ln2, k0, DX, DY, DZ)
             F += Ff
             perf += [s11.real, s11.imag, D]
         return F, perf
 
-    F_best, perf0 = score([st.Eobj for st in states])
-    log = DbsLog(init_map=list(tm), start_F=F_best, start_perf=perf0)
-    last = -1
-    while True:
-        if max_evals and log.evals >= max_evals:
-            break
-        c = next_candidate(geo, hat, sym, last)
-        if c is None:
-            log.converged = True
-            break
-        idx, tiles, last = c
-        s, d = geo.flip_set(tm, P, tiles)
-        news = [st.eval(s, d) for st in states]
-        F, perf = score(news)
-        acc = F < F_best
-        log.rows.append((log.evals, idx, int(acc), F, F_best, perf))
-        if acc:
-            F_best = F
-            for st, ne in zip(states, news):
-                if algebra in ("ref", "port"):
-                    st.accept(ne)
-                else:
-                    st.accept()
-            for t in tiles:
-                tm[t] ^= 1
-            P = geo.compute_P(tm)
-            hat.reset()
-            log.accepts += 1
-        log.evals += 1
-    log.final_map = list(tm)
-    return log
+    def step(self):
+        """Evaluates draws until the first improving flip (accepted) or the
+        end of the hat / evaluation cap. Returns True if a flip was accepted."""
+        log = self.log
+        while not self.done:
+            if self.max_evals and log.evals >= self.max_evals:
+                self.done = True
+                break
+            c = next_candidate(self.geo, self.hat, self.sym, self.last)
+            if c is None:
+                log.converged = self.done = True
+                break
+            idx, tiles, self.last = c
+            s, d = self.geo.flip_set(self.tm, self.P, tiles)
+            news = [st.eval(s, d) for st in self.states]
+            F, perf = self.score(news)
+            acc = F < self.F_best
+            log.rows.append((log.evals, idx, int(acc), F, self.F_best, perf))
+            log.evals += 1
+            if acc:
+                self.F_best = F
+                for st, ne in zip(self.states, news):
+                    if self.algebra in ("ref", "port"):
+                        st.accept(ne)
+                    else:
+                        st.accept()
+                for t in tiles:
+                    self.tm[t] ^= 1
+                self.P = self.geo.compute_P(self.tm)
+                self.hat.reset()
+                log.accepts += 1
+                return True
+        return False
+
+
+def run_dbs(Gs, gobj_rows, freqs, tiles_x, tiles_y, seed, sym=True, random_init=True,
+            max_evals=0, algebra="ref", run_index=0):
+    """Runs DBS to convergence (or the evaluation cap) and returns the log."""
+    r = DbsRunner(Gs, gobj_rows, freqs, tiles_x, tiles_y, seed, sym, random_init, max_evals, algebra, run_index)
+    while not r.done:
+        r.step()
+    r.log.final_map = list(r.tm)
+    return r.log
 
 
 def parse_ref_log(path):

@@ -25,6 +25,52 @@ int cuda_check(Handle *h, cudaError_t e, const char *what) {
   return set_error(h, PNGF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
+cudaEvent_t timing_mark(Handle *h) {
+  if (!h->timing) return nullptr;
+  cudaEvent_t e;
+  if (!h->ev_pool.empty()) {
+    e = h->ev_pool.back();
+    h->ev_pool.pop_back();
+  } else if (cudaEventCreate(&e) != cudaSuccess) {
+    return nullptr;
+  }
+  cudaEventRecord(e, h->stream);
+  return e;
+}
+
+void timing_close(Handle *h, cudaEvent_t start, int cat, double x1, double x2, double x3) {
+  if (!start) return;
+  cudaEvent_t stop = timing_mark(h);
+  if (!stop) return;
+  h->pending.push_back({start, stop, cat, x1, x2, x3});
+}
+
+static void timing_collect(Handle *h) {
+  for (auto &p : h->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    pngf_timing &t = h->tacc;
+    if (p.cat == T_EVAL) {
+      t.eval_ms += ms;
+      t.eval_launches += 1;
+      t.eval_cf += p.x1;
+      t.eval_bytes += p.x2;
+      t.eval_flop += p.x3;
+    } else if (p.cat == T_ACCEPT) {
+      t.accept_ms += ms;
+      t.accepts += 1;
+    } else {
+      t.update_ms += ms;
+      t.update_launches += 1;
+      t.update_flop += p.x1;
+      t.update_bytes += p.x2;
+    }
+    h->ev_pool.push_back(p.a);
+    h->ev_pool.push_back(p.b);
+  }
+  h->pending.clear();
+}
+
 #define PNGF_CUDA(h, call)                                   \
   do {                                                       \
     const int _rc = cuda_check((h), (call), #call);          \
@@ -126,8 +172,10 @@ static int check_tiles(Handle *h, const int *tiles, const int *nflip, int ncand)
 
 // Evaluates a batch whose tile lists are already in h->d_tiles / h->d_nflip.
 static int eval_resident(Handle *h, int ncand, double F_best) {
+  cudaEvent_t t0 = timing_mark(h);
   PNGF_CUDA(h, launch_edge_lists(h, ncand, h->d_tiles, h->d_nflip));
   PNGF_CUDA(h, launch_eval(h, ncand, F_best));
+  timing_close(h, t0, T_EVAL, (double)ncand * h->cfg.num_freq, 0.0, 0.0);
   h->batch_n = ncand;
   h->batch_valid = true;
   return PNGF_OK;
@@ -170,6 +218,16 @@ int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double 
   out->first = hint[0];
   out->k.assign(hint + 1, hint + 1 + ncand);
   out->status.assign(hint + 1 + ncand, hint + 1 + ncand + (size_t)ncand * nf);
+  if (h->timing) {  // algorithmic work of this batch, from the actual flip sizes
+    h->tacc.h2d_bytes += sizeof(int) * (double)ncand * (mf + 1);
+    h->tacc.d2h_bytes += sizeof(double) * (double)(nF + nperf + neo) + sizeof(int) * (double)nint;
+    const double sM = h->cfg.precision == PNGF_PREC_FP64 ? 16.0 : 8.0;
+    for (int c = 0; c < ncand; ++c) {
+      const double k = std::max(0, out->k[c]);
+      h->tacc.eval_bytes += nf * (sM * (k * k + (h->E + 1) * k + h->E) + 21.0 * k);
+      h->tacc.eval_flop += nf * (8.0 / 3.0 * k * k * k + 16.0 * k * k + 8.0 * h->E * k);
+    }
+  }
   return PNGF_OK;
 }
 
@@ -178,8 +236,11 @@ int accept_cand(Handle *h, int c, int k) {
   if (c < 0 || c >= h->batch_n) return set_error(h, PNGF_ERR_ARG, "candidate index outside the last batch");
   if (k < 0 || k > h->kmax) return set_error(h, PNGF_ERR_ARG, "invalid flipped-edge count");
   PNGF_CUDA(h, cudaMemsetAsync(h->d_acc_status, 0, sizeof(int), h->stream));
-  for (int f = 0; f < h->cfg.num_freq; ++f)
+  for (int f = 0; f < h->cfg.num_freq; ++f) {
+    cudaEvent_t t0 = timing_mark(h);
     PNGF_CUDA(h, launch_accept_edges(h, f, h->d_es + (size_t)c * h->kmax, h->d_ed + (size_t)c * h->kmax, k));
+    timing_close(h, t0, T_ACCEPT, 0.0, 0.0, 0.0);
+  }
   PNGF_CUDA(h, launch_commit(h, c));
   // host mirror of the design (update_C_inv commits the flip, pngfopt.hpp:360-366)
   const int mf = h->cfg.max_flips;
@@ -570,5 +631,26 @@ int pngf_drift_check(pngf_handle *ph, int ncols, double *max_rel) {
 }
 
 int pngf_refresh(pngf_handle *ph) { return pngf_prepare(ph); }
+
+int pngf_timing_enable(pngf_handle *ph, int on) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  timing_collect(h);
+  h->tacc = pngf_timing{};
+  h->nlaunch = 0;
+  h->timing = on != 0;
+  return PNGF_OK;
+}
+
+int pngf_timing_get(pngf_handle *ph, pngf_timing *out) {
+  Handle *h = H(ph);
+  if (!h || !out) return PNGF_ERR_ARG;
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  timing_collect(h);
+  *out = h->tacc;
+  out->kernel_launches = h->nlaunch;
+  return PNGF_OK;
+}
 
 }  // extern "C"

@@ -665,6 +665,7 @@ cudaError_t launch_init_M(Handle *h, int f) {
   k_port_const<<<1, 1, 0, h->stream>>>(q.Einc, q.gobj, n, h->E, d_port, (int)h->port.size(), k0,
                                        h->d_fconst + f);
   cudaFreeAsync(d_port, h->stream);
+  h->nlaunch += 3;
   return cudaGetLastError();
 }
 
@@ -675,6 +676,7 @@ cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const in
   const size_t sm = sizeof(int) * 2 * slots * warps;
   k_edge_lists<<<(ncand + warps - 1) / warps, 32 * warps, sm, h->stream>>>(g, ncand, d_tiles, d_nflip, h->d_tile_map,
                                                                           h->d_P, h->d_es, h->d_ed, h->d_ek);
+  h->nlaunch += 1;
   return cudaGetLastError();
 }
 
@@ -702,6 +704,7 @@ cudaError_t launch_eval(Handle *h, int ncand, double F_best) {
     e = launch_eval_t<float2>(h, reinterpret_cast<const float2 *const *>(h->d_M32s), ncand);
   if (e != cudaSuccess) return e;
   k_score<<<1, 256, 0, h->stream>>>(ncand, h->cfg.num_freq, h->d_Ff, F_best, h->d_F, h->d_first);
+  h->nlaunch += 2;
   return cudaGetLastError();
 }
 
@@ -714,6 +717,7 @@ cudaError_t launch_current_objective(Handle *h) {
     k_current_objective<float2><<<1, 32, 0, h->stream>>>(reinterpret_cast<const float2 *const *>(h->d_M32s),
                                                          h->ldm, h->n, h->E, h->d_fconst, obj_const(h),
                                                          h->cfg.num_freq, h->d_F, h->d_perf);
+  h->nlaunch += 1;
   return cudaGetLastError();
 }
 
@@ -736,13 +740,18 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   k_acc_gather<double2><<<(unsigned)((rows + 255) / 256), 256, 0, h->stream>>>(q.M64, h->ldm, rows, d_s, k, h->d_A,
                                                                               rows);
   dim3 g((unsigned)((n + 1 + RU_T - 1) / RU_T), (unsigned)((rows + RU_T - 1) / RU_T));
+  cudaEvent_t t0 = timing_mark(h);
   k_rank_update<<<g, 256, 0, h->stream>>>(q.M64, h->ldm, rows, n + 1, h->d_A, rows, h->d_W, h->ldm, k);
+  const double cells = (double)rows * (double)(n + 1);
+  timing_close(h, t0, T_UPDATE, 8.0 * k * cells, 2.0 * 16.0 * cells + 16.0 * k * (double)(rows + n + 1), 0.0);
+  h->nlaunch += 4;
   return cudaGetLastError();
 }
 
 cudaError_t launch_commit(Handle *h, int c) {
   k_commit<<<1, 128, 0, h->stream>>>(h->kmax, c, h->d_es, h->d_ed, h->d_ek, h->cfg.max_flips, h->d_tiles,
                                       h->d_nflip, h->d_P, h->d_tile_map);
+  h->nlaunch += 1;
   return cudaGetLastError();
 }
 

@@ -91,8 +91,28 @@ struct Handle {
   double *h_out = nullptr;
   size_t h_out_cap = 0;
 
+  // measurement
+  bool timing = false;
+  pngf_timing tacc{};
+  struct Pending {
+    cudaEvent_t a, b;
+    int cat;
+    double x1, x2, x3;
+  };
+  std::vector<Pending> pending;
+  std::vector<cudaEvent_t> ev_pool;
+  long nlaunch = 0;
+
   std::string err;
 };
+
+// Timing categories.
+enum { T_EVAL = 0, T_ACCEPT = 1, T_UPDATE = 2 };
+// Records an event on the handle's stream if timing is on (else nullptr).
+cudaEvent_t timing_mark(Handle *h);
+// Closes a span opened by timing_mark: category and algorithmic work
+// (T_EVAL: cand x freq, bytes, flops; T_UPDATE: flops, bytes).
+void timing_close(Handle *h, cudaEvent_t start, int cat, double x1, double x2, double x3);
 
 int set_error(Handle *h, int code, const std::string &msg);
 int cuda_check(Handle *h, cudaError_t e, const char *what);

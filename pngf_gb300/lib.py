@@ -48,6 +48,17 @@ class DbsStats(C.Structure):
                 ("F_init", C.c_double), ("F_best", C.c_double)]
 
 
+class Timing(C.Structure):
+    _fields_ = [("eval_ms", C.c_double), ("eval_launches", C.c_long), ("eval_cf", C.c_double),
+                ("eval_bytes", C.c_double), ("eval_flop", C.c_double), ("accept_ms", C.c_double),
+                ("accepts", C.c_long), ("update_ms", C.c_double), ("update_launches", C.c_long),
+                ("update_flop", C.c_double), ("update_bytes", C.c_double), ("kernel_launches", C.c_long),
+                ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -84,6 +95,8 @@ def load():
         "pngf_accept": (I, [P, I]),
         "pngf_drift_check": (I, [P, I, P]),
         "pngf_refresh": (I, [P]),
+        "pngf_timing_enable": (I, [P, I]),
+        "pngf_timing_get": (I, [P, P]),
         "pngf_dbs_begin": (I, [P, P, P]),
         "pngf_dbs_step": (I, [P, P]),
         "pngf_dbs_stats_get": (I, [P, P]),
@@ -176,6 +189,14 @@ class Handle:
             self.close()
         except Exception:
             pass
+
+    def timing_enable(self, on=True):
+        self._chk(self.L.pngf_timing_enable(self.h, 1 if on else 0), "pngf_timing_enable")
+
+    def timing(self):
+        t = Timing()
+        self._chk(self.L.pngf_timing_get(self.h, C.byref(t)), "pngf_timing_get")
+        return t.as_dict()
 
     def set_stream(self, stream_ptr):
         self._chk(self.L.pngf_set_stream(self.h, C.c_void_p(stream_ptr)), "pngf_set_stream")
