@@ -131,6 +131,12 @@ int pngf_get_eobj(pngf_handle *h, int f, double *eobj, double *vinc_ln);
 /* Objective F = sum_f 200|S11|^2 + (15-D)^2 of the current design
  * (main.cpp:271-302). */
 int pngf_objective(pngf_handle *h, double *F);
+/* Copies frequency f's M ((N+E) x (N+1), row-major complex, leading
+ * dimension ld >= N+1) to host memory, and Einc (N complex) if einc is not
+ * NULL. The reference keeps its state in the public members C, R, S
+ * (pngfopt.hpp:21-26); M holds the same information (see the top of this
+ * header). */
+int pngf_get_M(pngf_handle *h, int f, double *M, long ld, double *einc);
 
 /* ---- hot path ---- */
 

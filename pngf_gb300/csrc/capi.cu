@@ -554,6 +554,19 @@ int pngf_objective(pngf_handle *ph, double *F) {
   return PNGF_OK;
 }
 
+int pngf_get_M(pngf_handle *ph, int f, double *M, long ld, double *einc) {
+  Handle *h = H(ph);
+  if (!h || !M || f < 0 || f >= h->cfg.num_freq || ld < h->n + 1) return PNGF_ERR_ARG;
+  if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
+  const long rows = h->n + h->E;
+  PNGF_CUDA(h, cudaMemcpy2DAsync(M, sizeof(double2) * ld, h->f[f].M64, sizeof(double2) * h->ldm,
+                                 sizeof(double2) * (h->n + 1), rows, cudaMemcpyDeviceToHost, h->stream));
+  if (einc)
+    PNGF_CUDA(h, cudaMemcpyAsync(einc, h->f[f].Einc, sizeof(double2) * h->n, cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  return PNGF_OK;
+}
+
 int pngf_eval_candidates(pngf_handle *ph, const int *tiles, const int *nflip, int ncand, double *new_eobj,
                          double *F) {
   Handle *h = H(ph);

@@ -90,6 +90,7 @@ def load():
         "pngf_prepare": (I, [P]),
         "pngf_get_eobj": (I, [P, I, P, P]),
         "pngf_objective": (I, [P, P]),
+        "pngf_get_M": (I, [P, I, P, L_, P]),
         "pngf_eval_candidates": (I, [P, P, P, I, P, P]),
         "pngf_eval_candidates_device": (I, [P, P, P, I, P, P, D, P]),
         "pngf_accept": (I, [P, I]),
@@ -229,6 +230,13 @@ class Handle:
         v = np.zeros(3, dtype=np.complex128)
         self._chk(self.L.pngf_get_eobj(self.h, f, _ptr(e), _ptr(v)), "pngf_get_eobj")
         return e, v
+
+    def get_M(self, f):
+        """(M, Einc) of frequency f: M is (N+E) x (N+1) complex128."""
+        M = np.zeros((self.n + self.E, self.n + 1), dtype=np.complex128)
+        e = np.zeros(self.n, dtype=np.complex128)
+        self._chk(self.L.pngf_get_M(self.h, f, _ptr(M), self.n + 1, _ptr(e)), "pngf_get_M")
+        return M, e
 
     def objective(self):
         F = np.zeros(1)

@@ -114,6 +114,35 @@ def test_eval_and_accept_match_oracle(cases, built_lib):
     assert list(h.tile_map()) == tm
 
 
+def test_prepared_M_matches_oracle(cases, built_lib):
+    """M built on the GPU from G (chunked accepts of the design's edges)
+    against the oracle's M algebra and against H C^-1 from a direct inverse."""
+    from oracle.geometry import Geometry, port_setup
+    from oracle.refalg import MState
+    from pngf_gb300 import lib
+    c = cases["sym_7x7_f1_seed1"]
+    Gs, gobj = case_G(c, built_lib)
+    geo = Geometry(7, 7)
+    tm = list(np.random.default_rng(3).integers(0, 2, 49))
+    P = geo.compute_P(tm)
+    Gobj, Einc, _, _, _ = port_setup(Gs[0], gobj[0], geo.port_indices(3, 3, 1, 2))
+    h = lib.Handle(7, 7, c["freqs"], max_flips=4)
+    h.load_G(0, Gs[0], gobj[0])
+    h.set_tile_map(tm)
+    h.set_source_port(3, 3, 1, 2)
+    h.prepare()
+    M, e = h.get_M(0)
+    np.testing.assert_allclose(e, Einc, rtol=1e-14, atol=0)
+    ref = MState.build(Gs[0], Gobj, Einc, P).M
+    scale = np.abs(ref).max()
+    assert np.abs(M - ref).max() <= 1e-11 * scale
+    n = Gs[0].shape[0]
+    C = np.eye(n, dtype=complex)
+    C[P.astype(bool)] = Gs[0][P.astype(bool)]
+    T = (Gs[0] - np.eye(n)) @ np.linalg.inv(C)
+    assert np.abs(M[:n, :n] - T).max() <= 1e-10 * np.abs(T).max()
+
+
 def test_api_errors(cases, built_lib):
     from pngf_gb300 import lib
     c = cases["sym_7x7_f1_seed1"]
