@@ -133,8 +133,8 @@ def measured_peaks():
 
 def fp64_gemm_peak_tflops():
     """FP64 GEMM throughput of this GPU (cuBLAS DGEMM through torch, best of 5),
-    the denominator for FP64-pipe-bound kernels (no FP64 figure is in the
-    measured peaks)."""
+    the denominator for FP64-pipe-bound kernels (the measured-peaks file has
+    no FP64 figure)."""
     import torch
     n = 4096
     a = torch.randn(n, n, dtype=torch.float64, device="cuda")
