@@ -42,6 +42,7 @@ extern "C" {
 #define PNGF_ERR_TIMEOUT 7     /* a bounded device wait ran out */
 #define PNGF_ERR_UNSUPPORTED 8 /* configuration not supported by this build */
 #define PNGF_ERR_NO_DEVICE 9   /* no usable CUDA device / kernel image */
+#define PNGF_ERR_SCRATCH 10    /* request larger than the fixed scratch of pngf_accept_edges_noalloc */
 
 /* ---- precision modes ---- */
 #define PNGF_PREC_FP64 0 /* M in complex128, all arithmetic FP64 */
@@ -158,6 +159,23 @@ int pngf_eval_candidates_device(pngf_handle *h, const int *d_tiles, const int *d
  * rank-k update of M, then P and the tile map are committed. Replaces
  * update_C_inv + compute_PEinc + compute_R_matrix(0) (main.cpp:447-452). */
 int pngf_accept(pngf_handle *h, int cand);
+
+/* Accept step on caller-owned device memory that allocates nothing. No
+ * counterpart in the reference. For callers that cannot allocate device
+ * memory (a framework allocator that owns the GPU, an FFI host that cannot
+ * free foreign allocations, a loop that cannot afford cudaMalloc's device
+ * synchronisation). Applies the rank-k update M <- M - M[:,s] W for the
+ * flip of edges s (k of them, signs d = +-1) to the augmented matrix M
+ * ((N+E) x ldm row-major complex128, the layout pngf_get_M returns) with
+ * Einc (N complex), all device pointers, asynchronously on `stream`
+ * (cudaStream_t, NULL = default). Scratch lives in one fixed 8 MiB device
+ * array: (N+E+ldm) k 16 + k^2 16 + 20 k bytes (plus alignment) must fit, and
+ * k <= 104, else PNGF_ERR_SCRATCH / PNGF_ERR_ARG. The first call on a device
+ * looks up that array's address (do it before any stream capture). Calls
+ * share the array: calls that overlap on the GPU race. *status (device int,
+ * may be NULL) is cleared, then set to PNGF_ERR_SINGULAR if K is singular. */
+int pngf_accept_edges_noalloc(double *M, long ldm, long n, int num_eobj, const double *Einc, const int *s,
+                              const signed char *d, int k, int *status, void *stream);
 
 /* Largest relative deviation of the maintained M from one rebuilt from G in
  * FP64 on `ncols` sampled columns (drift check for PNGF_PREC_C64). */

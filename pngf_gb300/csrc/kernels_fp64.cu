@@ -748,6 +748,26 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   return cudaGetLastError();
 }
 
+cudaError_t launch_accept_raw(double2 *M, long ldm, long n, int E, const double2 *Einc, const int *d_s,
+                              const signed char *d_d, int k, double2 *LU, int *piv, double2 *z, double2 *A,
+                              double2 *W, int *status, cudaStream_t stream) {
+  const long rows = n + E;
+  if (k <= 0) return cudaSuccess;
+  const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
+  cudaError_t e = cudaFuncSetAttribute(k_acc_factor<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+  if (e != cudaSuccess) return e;
+  k_acc_factor<double2><<<1, 256, smf, stream>>>(M, ldm, n, Einc, d_s, d_d, k, LU, piv, z, status);
+  const int wc = k <= 64 ? 64 : 32;
+  const size_t smw = sizeof(double2) * ((size_t)k * k + (size_t)k * wc);
+  e = cudaFuncSetAttribute(k_acc_W<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
+  if (e != cudaSuccess) return e;
+  k_acc_W<double2><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(M, ldm, n, d_s, d_d, k, LU, piv, z, W, ldm);
+  k_acc_gather<double2><<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(M, ldm, rows, d_s, k, A, rows);
+  dim3 g((unsigned)((n + 1 + RU_T - 1) / RU_T), (unsigned)((rows + RU_T - 1) / RU_T));
+  k_rank_update<<<g, 256, 0, stream>>>(M, ldm, rows, n + 1, A, rows, W, ldm, k);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_commit(Handle *h, int c) {
   k_commit<<<1, 128, 0, h->stream>>>(h->kmax, c, h->d_es, h->d_ed, h->d_ek, h->cfg.max_flips, h->d_tiles,
                                       h->d_nflip, h->d_P, h->d_tile_map);

@@ -146,5 +146,10 @@ cudaError_t launch_current_objective(Handle *h);
 cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k);
 // Commits P and the tile map on the device for candidate c of the batch.
 cudaError_t launch_commit(Handle *h, int c);
+// The accept kernels on caller-supplied buffers (no handle): scratch LU (k^2),
+// piv (k), z (k), A ((n+E) x k), W (k x ldm), status (1, sticky).
+cudaError_t launch_accept_raw(double2 *M, long ldm, long n, int E, const double2 *Einc, const int *d_s,
+                              const signed char *d_d, int k, double2 *LU, int *piv, double2 *z, double2 *A,
+                              double2 *W, int *status, cudaStream_t stream);
 
 }  // namespace pngf

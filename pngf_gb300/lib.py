@@ -18,7 +18,8 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "pngf_gb300.h")
 
 PNGF_OK = 0
 ERRORS = {1: "PNGF_ERR_ARG", 2: "PNGF_ERR_CUDA", 3: "PNGF_ERR_NOMEM", 4: "PNGF_ERR_IO", 5: "PNGF_ERR_SINGULAR",
-          6: "PNGF_ERR_STATE", 7: "PNGF_ERR_TIMEOUT", 8: "PNGF_ERR_UNSUPPORTED", 9: "PNGF_ERR_NO_DEVICE"}
+          6: "PNGF_ERR_STATE", 7: "PNGF_ERR_TIMEOUT", 8: "PNGF_ERR_UNSUPPORTED", 9: "PNGF_ERR_NO_DEVICE",
+          10: "PNGF_ERR_SCRATCH"}
 PREC_FP64, PREC_C64 = 0, 1
 DBS_SYMMETRIC, DBS_SINGLE = 0, 1
 INIT_EMPTY, INIT_RANDOM = 0, 1
@@ -95,6 +96,7 @@ def load():
         "pngf_eval_candidates_device": (I, [P, P, P, I, P, P, D, P]),
         "pngf_accept": (I, [P, I]),
         "pngf_drift_check": (I, [P, I, P]),
+        "pngf_accept_edges_noalloc": (I, [P, L_, L_, I, P, P, P, I, P, P]),
         "pngf_refresh": (I, [P]),
         "pngf_timing_enable": (I, [P, I]),
         "pngf_timing_get": (I, [P, P]),
