@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--mode", choices=["single", "sym"], default="single")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forms", default="fp64,c64", help="precision forms to run; the first is the headline")
+    ap.add_argument("--nfreq", type=int, default=5, help="use the first NFREQ of the five frequencies")
     return ap.parse_args()
 
 
@@ -212,23 +214,15 @@ def cpu_baseline_sample(tiles, mode, seed, freq, gpu_evals, gpu_accepts, nf, bud
     }
 
 
-def gpu_arm(a, world, rank, local):
+def run_form(a, precision, Gs, rank, local, dist):
+    """Runs W + K DBS decisions of one precision form; returns its counters."""
     import torch
     from pngf_gb300 import lib
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    peaks, peak_src = measured_peaks()
-    fp64_peak = fp64_gemm_peak_tflops()
-    nf = len(FREQS)
     t_setup = time.perf_counter()
-    Gs = make_Gs(a.tiles, FREQS)
-    h = lib.Handle(a.tiles, a.tiles, FREQS, max_flips=1 if a.mode == "single" else 4, device=local)
+    h = lib.Handle(a.tiles, a.tiles, FREQS, precision=precision, max_flips=1 if a.mode == "single" else 4,
+                   device=local)
     for f, G in enumerate(Gs):
         h.load_G(f, G, None)
-    del Gs
     d = lib.Dbs(h, mode=lib.DBS_SINGLE if a.mode == "single" else lib.DBS_SYMMETRIC, init=lib.INIT_RANDOM,
                 seed=a.seed + rank, batch=0)
     torch.cuda.synchronize()
@@ -252,25 +246,58 @@ def gpu_arm(a, world, rank, local):
         dist.barrier()
     clocks = sampler.stop()
     s1 = d.stats()
-    evals = s1.evals - s0.evals
-    accepts = s1.accepts - s0.accepts
-    launched = s1.launched - s0.launched
-    dev_s = (tm["eval_ms"] + tm["accept_ms"]) * 1e-3
-    vec = torch.tensor([wall, dev_s, evals, accepts, launched], dtype=torch.float64, device="cuda")
-    if dist:
-        mx = vec.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = vec.clone()
-        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        wall_m, dev_m = mx[0].item(), mx[1].item()
-        evals_t, accepts_t, launched_t = sm[2].item(), sm[3].item(), sm[4].item()
-    else:
-        wall_m, dev_m, evals_t, accepts_t, launched_t = wall, dev_s, evals, accepts, launched
+    out = dict(evals=s1.evals - s0.evals, accepts=s1.accepts - s0.accepts, launched=s1.launched - s0.launched,
+               wall=wall, dev_s=(tm["eval_ms"] + tm["accept_ms"]) * 1e-3, tm=tm, clocks=clocks, setup_s=setup_s,
+               F_init=s1.F_init, F_best=s1.F_best, n=h.n, ldm=h.ldm)
+    d.close()
+    h.close()
+    torch.cuda.empty_cache()
+    return out
+
+
+def reduce_form(r, dist):
+    """Whole-job figures: sums of work over ranks, max of times over ranks."""
+    import torch
+    vec = torch.tensor([r["wall"], r["dev_s"], r["evals"], r["accepts"], r["launched"]], dtype=torch.float64,
+                       device="cuda")
+    if not dist:
+        return r["wall"], r["dev_s"], r["evals"], r["accepts"], r["launched"]
+    mx, sm = vec.clone(), vec.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return mx[0].item(), mx[1].item(), sm[2].item(), sm[3].item(), sm[4].item()
+
+
+def gpu_arm(a, world, rank, local):
+    import torch
+    from pngf_gb300 import lib
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    peaks, peak_src = measured_peaks()
+    fp64_peak = fp64_gemm_peak_tflops()
+    nf = len(FREQS)
+    Gs = make_Gs(a.tiles, FREQS)
+    forms = a.forms.split(",")
+    r64 = r32 = None
+    if "fp64" in forms:
+        r64 = run_form(a, lib.PREC_FP64, Gs, rank, local, dist)
+        wall_m, dev_m, evals_t, accepts_t, launched_t = reduce_form(r64, dist)
+    if "c64" in forms:
+        r32 = run_form(a, lib.PREC_C64, Gs, rank, local, dist)
+        c64_red = reduce_form(r32, dist)
+    del Gs
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
-    n = h.n
+    if r64 is None:  # complex64 form alone (profiling runs)
+        print(json.dumps({"c64_only": {k: v for k, v in r32.items() if k != "tm"}, "timing": r32["tm"]}),
+              flush=True)
+        return
+    tm, n = r64["tm"], r64["n"]
     upd_s = tm["update_ms"] * 1e-3
     achieved = tm["update_flop"] / upd_s / 1e12 if upd_s > 0 else None
     traffic = None
@@ -315,14 +342,14 @@ def gpu_arm(a, world, rank, local):
             "tiles": a.tiles, "freqs_ghz": [f / 1e9 for f in FREQS], "edges": n,
             "candidates_per_pass": a.tiles * a.tiles if a.mode == "single" else None,
             "precision": "fp64", "parallelism": "one DBS instance per GPU" if world > 1 else "single GPU",
-            "l2": "inputs larger than L2: M is %.2f GB per frequency" % ((n + 3) * h.ldm * 16 / 1e9),
+            "l2": "inputs larger than L2: M is %.2f GB per frequency" % ((n + 3) * r64["ldm"] * 16 / 1e9),
             "step": "one DBS decision (speculative batch of the remaining hat, first improving draw accepted)",
             "value_timing": "sum of CUDA-event spans of the hot-path launch groups on the handle's stream",
         },
         "e2e": {"value": evals_t / wall_m, "unit": "flip_evals/s",
                 "h2d_bytes_per_step": tm["h2d_bytes"] / a.steps, "d2h_bytes_per_step": tm["d2h_bytes"] / a.steps},
         "roofline": roofline,
-        "clocks": clocks,
+        "clocks": r64["clocks"],
         "gpu_launches": tm["kernel_launches"],
         "detail": {
             "evals": evals_t, "accepts": accepts_t, "launched_candidates": launched_t,
@@ -331,12 +358,38 @@ def gpu_arm(a, world, rank, local):
             "eval_kernel_gbs": tm["eval_bytes"] / eval_s / 1e9 if eval_s > 0 else None,
             "eval_kernel_fp64_tflops": tm["eval_flop"] / eval_s / 1e12 if eval_s > 0 else None,
             "eval_ms": tm["eval_ms"], "accept_ms": tm["accept_ms"], "update_ms": tm["update_ms"],
-            "setup_s": setup_s, "F_init": s1.F_init, "F_best": s1.F_best,
+            "setup_s": r64["setup_s"], "F_init": r64["F_init"], "F_best": r64["F_best"],
             "fp64_gemm_tflops": fp64_peak,
         },
     }
+    if r32 is not None:
+        w32, d32, e32, acc32, l32 = c64_red
+        t32 = r32["tm"]
+        u32 = t32["update_ms"] * 1e-3
+        line["c64_form"] = {
+            "what": "T in complex64, rank-k update on tcgen05 tensor cores (kind::tf32, 3xTF32 split products, "
+                    "FP32 accumulation in TMEM); capacitance LU, y, R, Eobj, objective and accept test in FP64; "
+                    "same workload and steps",
+            "value": e32 / d32 if d32 > 0 else None, "e2e": e32 / w32, "unit": "flip_evals/s",
+            "evals": e32, "accepts": acc32, "F_init": r32["F_init"], "F_best": r32["F_best"],
+            "F_best_rel_diff_vs_fp64": abs(r32["F_best"] - r64["F_best"]) / abs(r64["F_best"]),
+            "eval_ms_fp64_form": tm["eval_ms"],
+            "eval_ms": t32["eval_ms"], "accept_ms": t32["accept_ms"], "update_ms": t32["update_ms"],
+            "roofline": {
+                "kernel": "k_tc_update (tcgen05 complex rank-k update of T)",
+                "bound": "hbm",
+                "achieved": t32["update_bytes"] / u32 / 1e9 if u32 > 0 else None,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": (t32["update_bytes"] / u32 / 1e9) / peaks["hbm_gbs"] if u32 > 0 else None,
+                "peak_source": peak_src,
+                "launch_ms": t32["update_ms"] / max(1, t32["update_launches"]),
+                "algorithmic_bytes_per_launch": t32["update_bytes"] / max(1, t32["update_launches"]),
+            },
+            "clocks": r32["clocks"], "gpu_launches": t32["kernel_launches"], "setup_s": r32["setup_s"],
+        }
     if world == 1 and not a.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline_sample(a.tiles, a.mode, a.seed, FREQS[0], evals, accepts, nf)
+        line["cpu_baseline"] = cpu_baseline_sample(a.tiles, a.mode, a.seed, FREQS[0], r64["evals"],
+                                                   r64["accepts"], nf)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -381,7 +434,9 @@ def reference_arm(a, world, rank):
 
 
 def main():
+    global FREQS
     a = parse()
+    FREQS = FREQS[:max(1, min(a.nfreq, len(FREQS)))]
     world, rank, local = dist_env()
     if a.impl == "reference":
         reference_arm(a, world, rank)

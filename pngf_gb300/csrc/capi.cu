@@ -238,10 +238,21 @@ int accept_cand(Handle *h, int c, int k) {
   PNGF_CUDA(h, cudaMemsetAsync(h->d_acc_status, 0, sizeof(int), h->stream));
   for (int f = 0; f < h->cfg.num_freq; ++f) {
     cudaEvent_t t0 = timing_mark(h);
-    PNGF_CUDA(h, launch_accept_edges(h, f, h->d_es + (size_t)c * h->kmax, h->d_ed + (size_t)c * h->kmax, k));
+    PNGF_CUDA(h, launch_accept_edges(h, f, h->d_es + (size_t)c * h->kmax, h->d_ed + (size_t)c * h->kmax, k,
+                                     h->cfg.precision));
     timing_close(h, t0, T_ACCEPT, 0.0, 0.0, 0.0);
   }
   PNGF_CUDA(h, launch_commit(h, c));
+  if (h->cfg.precision == PNGF_PREC_C64) {  // the tensor-core kernel's bounded waits report here
+    int tc = 0;
+    PNGF_CUDA(h, cudaMemcpyAsync(&tc, h->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (tc != 0) {
+      cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->stream);
+      h->batch_valid = false;
+      return set_error(h, PNGF_ERR_TIMEOUT, "tensor-core update gave up waiting (code " + std::to_string(tc) + ")");
+    }
+  }
   // host mirror of the design (update_C_inv commits the flip, pngfopt.hpp:360-366)
   const int mf = h->cfg.max_flips;
   for (int i = 0; i < h->batch_nflip[c]; ++i) h->tile_map[h->batch_tiles[(size_t)c * mf + i]] ^= 1;
@@ -289,12 +300,16 @@ int pngf_destroy(pngf_handle *ph) {
     dfree(q.gobj);
     dfree(q.Einc);
     dfree(q.M64);
-    dfree(q.M32);
+    dfree(q.T32);
+    dfree(q.y64);
+    dfree(q.R64);
   }
   dfree(h->d_fconst);
-  dfree(h->d_M64s);
-  dfree(h->d_M32s);
+  dfree(h->d_views);
   dfree(h->d_Eincs);
+  dfree(h->d_Aop);
+  dfree(h->d_Bop);
+  dfree(h->d_tc_err);
   dfree(h->d_tile_map);
   dfree(h->d_P);
   dfree(h->d_tiles);
@@ -332,7 +347,7 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
       c.num_eobj > PNGF_MAX_EOBJ || c.num_freq < 1 || c.num_freq > PNGF_MAX_FREQ || c.max_flips < 1 ||
       c.max_flips > 8 || !(c.dx > 0) || !(c.dy > 0) || !(c.dz > 0))
     return PNGF_ERR_ARG;
-  if (c.precision != PNGF_PREC_FP64) return PNGF_ERR_UNSUPPORTED;
+  if (c.precision != PNGF_PREC_FP64 && c.precision != PNGF_PREC_C64) return PNGF_ERR_ARG;
   const int kmax = c.max_flips * edges_per_tile(c);
   if (kmax > kMaxEvalK) return PNGF_ERR_UNSUPPORTED;
   int ndev = 0;
@@ -371,17 +386,36 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
   h->stream = h->own_stream;
   const long n = h->n, rows = n + h->E;
   int rc;
-  std::vector<void *> m64(c.num_freq), einc(c.num_freq);
+  const bool c64 = c.precision == PNGF_PREC_C64;
+  std::vector<void *> einc(c.num_freq);
   for (int f = 0; f < c.num_freq; ++f) {
     Freq &q = h->f[f];
     if ((rc = dalloc(h, &q.G, (size_t)n * n)) || (rc = dalloc(h, &q.gobj, (size_t)std::max(1, h->E - 1) * n)) ||
         (rc = dalloc(h, &q.Einc, (size_t)n)) || (rc = dalloc(h, &q.M64, (size_t)rows * h->ldm)))
       return fail(rc);
-    m64[f] = q.M64;
+    if (c64 && ((rc = dalloc(h, &q.T32, (size_t)n * h->ldm)) || (rc = dalloc(h, &q.y64, (size_t)n)) ||
+                (rc = dalloc(h, &q.R64, (size_t)h->E * h->ldm))))
+      return fail(rc);
     einc[f] = q.Einc;
   }
-  if ((rc = dalloc(h, &h->d_fconst, (size_t)c.num_freq)) || (rc = dalloc(h, &h->d_M64s, (size_t)c.num_freq)) ||
-      (rc = dalloc(h, &h->d_M32s, (size_t)c.num_freq)) || (rc = dalloc(h, &h->d_Eincs, (size_t)c.num_freq)) ||
+  if (c64) {  // tensor-core operands: rows padded to the 128-row tile, zero outside what each update writes
+    h->kt_cap = (6 * kmax + 31) / 32 * 32;
+    h->aop_rows = (n + 127) / 128 * 128;
+    h->bop_rows = (2 * n + 127) / 128 * 128;
+    if ((rc = dalloc(h, &h->d_Aop, (size_t)h->aop_rows * h->kt_cap)) ||
+        (rc = dalloc(h, &h->d_Bop, (size_t)h->bop_rows * h->kt_cap)) || (rc = dalloc(h, &h->d_tc_err, 1)))
+      return fail(rc);
+    if (cudaMemset(h->d_Aop, 0, sizeof(float) * h->aop_rows * h->kt_cap) != cudaSuccess ||
+        cudaMemset(h->d_Bop, 0, sizeof(float) * h->bop_rows * h->kt_cap) != cudaSuccess ||
+        cudaMemset(h->d_tc_err, 0, sizeof(int)) != cudaSuccess)
+      return fail(PNGF_ERR_CUDA);
+  }
+  {
+    void *v = nullptr;
+    if (cudaMalloc(&v, view_bytes() * c.num_freq) != cudaSuccess) return fail(PNGF_ERR_NOMEM);
+    h->d_views = v;
+  }
+  if ((rc = dalloc(h, &h->d_fconst, (size_t)c.num_freq)) || (rc = dalloc(h, &h->d_Eincs, (size_t)c.num_freq)) ||
       (rc = dalloc(h, &h->d_tile_map, (size_t)h->map_sz)) || (rc = dalloc(h, &h->d_P, (size_t)n)) ||
       (rc = dalloc(h, &h->d_first, 1)) || (rc = dalloc(h, &h->d_A, (size_t)rows * h->acc_cap)) ||
       (rc = dalloc(h, &h->d_W, (size_t)h->acc_cap * h->ldm)) || (rc = dalloc(h, &h->d_acc_s, (size_t)n)) ||
@@ -389,8 +423,8 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
       (rc = dalloc(h, &h->d_piv, (size_t)h->acc_cap)) || (rc = dalloc(h, &h->d_z, (size_t)h->acc_cap)) ||
       (rc = dalloc(h, &h->d_acc_status, 1)))
     return fail(rc);
-  if (cudaMemcpy(h->d_M64s, m64.data(), sizeof(void *) * c.num_freq, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(h->d_Eincs, einc.data(), sizeof(void *) * c.num_freq, cudaMemcpyHostToDevice) != cudaSuccess)
+  if (cudaMemcpy(h->d_Eincs, einc.data(), sizeof(void *) * c.num_freq, cudaMemcpyHostToDevice) != cudaSuccess ||
+      setup_views(h) != cudaSuccess)
     return fail(PNGF_ERR_CUDA);
   if ((rc = ensure_cand_cap(h, 64))) return fail(rc);
   *out = reinterpret_cast<pngf_handle *>(h);
@@ -512,8 +546,9 @@ int pngf_prepare(pngf_handle *ph) {
     PNGF_CUDA(h, launch_init_M(h, f));
     for (size_t c0 = 0; c0 < on.size(); c0 += kInitChunk) {
       const int k = (int)std::min<size_t>(kInitChunk, on.size() - c0);
-      PNGF_CUDA(h, launch_accept_edges(h, f, h->d_acc_s + c0, h->d_acc_d + c0, k));
+      PNGF_CUDA(h, launch_accept_edges(h, f, h->d_acc_s + c0, h->d_acc_d + c0, k, PNGF_PREC_FP64));
     }
+    if (h->cfg.precision == PNGF_PREC_C64) PNGF_CUDA(h, launch_split_M(h, f));
   }
   int st = 0;
   PNGF_CUDA(h, cudaMemcpyAsync(&st, h->d_acc_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -532,7 +567,11 @@ int pngf_get_eobj(pngf_handle *ph, int f, double *eobj, double *vinc_ln) {
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
   if (eobj)
     for (int e = 0; e < h->E; ++e)
-      PNGF_CUDA(h, cudaMemcpyAsync(eobj + 2 * e, h->f[f].M64 + (size_t)(h->n + e) * h->ldm + h->n, sizeof(double2),
+      PNGF_CUDA(h, cudaMemcpyAsync(eobj + 2 * e,
+                                   h->cfg.precision == PNGF_PREC_C64
+                                       ? h->f[f].R64 + (size_t)e * h->ldm + h->n
+                                       : h->f[f].M64 + (size_t)(h->n + e) * h->ldm + h->n,
+                                   sizeof(double2),
                                    cudaMemcpyDeviceToHost, h->stream));
   PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
   if (vinc_ln) {
@@ -559,6 +598,7 @@ int pngf_get_M(pngf_handle *ph, int f, double *M, long ld, double *einc) {
   if (!h || !M || f < 0 || f >= h->cfg.num_freq || ld < h->n + 1) return PNGF_ERR_ARG;
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
   const long rows = h->n + h->E;
+  if (h->cfg.precision == PNGF_PREC_C64) PNGF_CUDA(h, launch_merge_M(h, f));  // M64 is staging in this mode
   PNGF_CUDA(h, cudaMemcpy2DAsync(M, sizeof(double2) * ld, h->f[f].M64, sizeof(double2) * h->ldm,
                                  sizeof(double2) * (h->n + 1), rows, cudaMemcpyDeviceToHost, h->stream));
   if (einc)

@@ -1,0 +1,426 @@
+// Complex64 form of the accept step: T is stored in complex64 and its rank-k
+// update T -= A W runs on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// Complex to real: with T viewed as a real matrix of 2N interleaved (re, im)
+// columns, T_real -= A_real B_real^T where A_real[i, 2r..2r+1] = (Re, Im) of
+// A[i, r] and, for output column 2j (real part) B_real[2j, 2r..2r+1] =
+// (Re W[r,j], -Im W[r,j]) and for 2j+1 (imaginary part) (Im W[r,j], Re W[r,j]).
+// Precision: 3xTF32 split products (x = hi + lo with hi, lo TF32), laid out
+// along K as [A_hi | A_hi | A_lo] . [B_hi | B_lo | B_hi], so a single GEMM with
+// K = 6k accumulates hi*hi + hi*lo + lo*hi in FP32 (TMEM). The small parts of
+// the state that feed the objective (y, R, Eobj) are updated in FP64.
+//
+// Kernel k_tc_update: one CTA per 128 x 128 output tile, 6 warps:
+//   warp 0  TMA producer: 128B-swizzled K-major tiles of A_op and B_op into a
+//           3-stage shared-memory ring (mbarrier complete_tx);
+//   warp 1  TMEM allocation and a single elected thread issuing
+//           tcgen05.mma.cta_group::1.kind::tf32 (M=128, N=128, K=8) into a
+//           128-column FP32 accumulator in TMEM, tcgen05.commit per stage;
+//   warps 2-5 epilogue: tcgen05.ld 32x32b rows of the accumulator, D -= acc.
+// Every mbarrier wait is bounded; on timeout the kernel records an error code,
+// drains its own TMA copies, frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+#include <mutex>
+
+#include "pngf_internal.h"
+
+namespace pngf {
+
+namespace {
+
+constexpr int TC_BM = 128;       // rows per tile (MMA M)
+constexpr int TC_BN = 128;       // fp32 columns per tile (MMA N)
+constexpr int TC_BK = 32;        // fp32 K elements per stage = one 128-byte swizzle row
+constexpr int TC_ST = 3;         // pipeline stages
+constexpr uint32_t A_BYTES = TC_BM * TC_BK * 4;
+constexpr uint32_t B_BYTES = TC_BN * TC_BK * 4;
+constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr size_t TC_SMEM = TC_ST * STAGE_BYTES + 1024 + 256;
+constexpr uint32_t kSpinLimit = 1u << 24;
+
+// Instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
+// (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdescTF32 =
+    (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor for a K-major tile with 128-byte swizzle:
+// start address >> 4 (bits 0-13), leading byte offset 16 B (unused for this
+// layout, bits 16-29), stride byte offset 1024 B between 8-row groups (bits
+// 32-45), descriptor version 1 (bits 46-47), layout SWIZZLE_128B = 2 (bits 61-63).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
+}
+
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// D[i, j] -= sum_k Aop[i, k] Bop[j, k] for i < rows, j < cols (fp32, D row-major
+// with leading dimension ldd). Aop / Bop come through TMA maps (K-major, 128B
+// swizzle). nkb = K / 32.
+__global__ void __launch_bounds__(192, 1) k_tc_update(const __grid_constant__ CUtensorMap tmA,
+                                                      const __grid_constant__ CUtensorMap tmB, float *__restrict__ D,
+                                                      long ldd, int rows, int cols, int nkb, int *err) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                          ~static_cast<uintptr_t>(1023));
+  const uint32_t sbase = smem_u32(base);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(base + TC_ST * STAGE_BYTES);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2 * TC_ST + 1);
+  const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * TC_ST, done = full0 + 16 * TC_ST;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_ST; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"((uint32_t)TC_BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued = 0;
+      bool ok = true;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % TC_ST;
+        if (kb >= TC_ST && !mbar_wait(empty0 + 8 * s, ((kb / TC_ST) - 1) & 1)) {
+          ok = false;
+          break;
+        }
+        mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
+        tma_load_2d(sbase + s * STAGE_BYTES, &tmA, kb * TC_BK, m0, full0 + 8 * s);
+        tma_load_2d(sbase + s * STAGE_BYTES + A_BYTES, &tmB, kb * TC_BK, n0, full0 + 8 * s);
+        ++issued;
+      }
+      if (!ok) atomicExch(err, 1);
+      // Drain: every copy this thread issued has landed before the CTA exits.
+      for (int kb = issued > TC_ST ? issued - TC_ST : 0; kb < issued; ++kb)
+        if (!mbar_wait(full0 + 8 * (kb % TC_ST), (kb / TC_ST) & 1)) atomicExch(err, 4);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      bool ok = true;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % TC_ST;
+        if (!mbar_wait(full0 + 8 * s, (kb / TC_ST) & 1)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint64_t ad = sw128_desc(sbase + s * STAGE_BYTES);
+        const uint64_t bd = sw128_desc(sbase + s * STAGE_BYTES + A_BYTES);
+#pragma unroll
+        for (int kk = 0; kk < TC_BK / 8; ++kk)  // K = 8 tf32 = 32 bytes per MMA: +2 in 16-byte units
+          mma_tf32(tmem, ad + 2 * kk, bd + 2 * kk, kIdescTF32, (kb | kk) != 0);
+        mma_commit(empty0 + 8 * s);
+      }
+      mma_commit(done);
+      if (!ok) atomicExch(err, 2);
+    }
+    __syncwarp();
+  } else {
+    // warp-uniform outcome: tcgen05.ld below is .sync.aligned
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
+    tc_fence_after();
+    if (!ok) {
+      if (lane == 0) atomicExch(err, 3);
+    } else {
+      const int q = warp & 3;  // this warp may access TMEM lanes 32q .. 32q+31
+      const int row = m0 + q * 32 + lane;
+      float *drow = D + (size_t)row * ldd;
+#pragma unroll 1
+      for (int c = 0; c < TC_BN / 16; ++c) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 16), v);
+        const int col0 = n0 + c * 16;
+        if (row < rows) {
+          if (col0 + 16 <= cols) {
+            float4 *p = reinterpret_cast<float4 *>(drow + col0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              float4 x = p[u];
+              x.x -= v[4 * u];
+              x.y -= v[4 * u + 1];
+              x.z -= v[4 * u + 2];
+              x.w -= v[4 * u + 3];
+              p[u] = x;
+            }
+          } else {
+            for (int u = 0; u < 16; ++u)
+              if (col0 + u < cols) drow[col0 + u] -= v[u];
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)TC_BN) : "memory");
+  }
+}
+
+// A_op rows i < n: 3xTF32 segments of the interleaved real form of A[i, :].
+__global__ void k_build_Aop(const double2 *__restrict__ A, long lda, long n, int k, int Kt, long ldk,
+                            float *__restrict__ Aop) {
+  const long i = (long)blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || c >= Kt) return;
+  float v = 0.f;
+  const int k2 = 2 * k;
+  if (c < 3 * k2) {
+    const int seg = c / k2, w = c - seg * k2, r = w >> 1;
+    const double2 a = A[(size_t)r * lda + i];
+    const float x = (float)((w & 1) ? a.y : a.x);
+    const float hi = to_tf32(x);
+    v = seg == 2 ? to_tf32(x - hi) : hi;
+  }
+  Aop[(size_t)i * ldk + c] = v;
+}
+
+// B_op rows j' < 2n: output column j' = 2j (real part) or 2j+1 (imaginary).
+__global__ void k_build_Bop(const double2 *__restrict__ W, long ldw, long n, int k, int Kt, long ldk,
+                            float *__restrict__ Bop) {
+  const long jp = (long)blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jp >= 2 * n || c >= Kt) return;
+  float v = 0.f;
+  const int k2 = 2 * k;
+  if (c < 3 * k2) {
+    const int seg = c / k2, w = c - seg * k2, r = w >> 1;
+    const double2 wv = W[(size_t)r * ldw + (jp >> 1)];
+    double b;
+    if ((jp & 1) == 0) b = (w & 1) ? -wv.y : wv.x;  // Re out: Re A Re W - Im A Im W
+    else b = (w & 1) ? wv.x : wv.y;                 // Im out: Re A Im W + Im A Re W
+    const float x = (float)b;
+    const float hi = to_tf32(x);
+    v = seg == 1 ? to_tf32(x - hi) : hi;
+  }
+  Bop[(size_t)jp * ldk + c] = v;
+}
+
+// FP64 part of the complex64 accept: y_i -= sum_r A[i,r] W[r,N] (i < N) and
+// R[e, j] -= sum_r A[N+e, r] W[r, j] (j <= N).
+__global__ void k_c64_side_update(double2 *__restrict__ y64, double2 *__restrict__ R64, long n, int E, long ldm,
+                                  const double2 *__restrict__ A, long lda, const double2 *__restrict__ W, int k) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int r = 0; r < k; ++r) {
+      const double2 a = A[(size_t)r * lda + t], w = W[(size_t)r * ldm + n];
+      acc.x += a.x * w.x - a.y * w.y;
+      acc.y += a.x * w.y + a.y * w.x;
+    }
+    y64[t].x -= acc.x;
+    y64[t].y -= acc.y;
+    return;
+  }
+  const long u = t - n;
+  if (u >= (long)E * (n + 1)) return;
+  const int e = (int)(u / (n + 1));
+  const long j = u - (long)e * (n + 1);
+  double2 acc = make_double2(0.0, 0.0);
+  for (int r = 0; r < k; ++r) {
+    const double2 a = A[(size_t)r * lda + n + e], w = W[(size_t)r * ldm + j];
+    acc.x += a.x * w.x - a.y * w.y;
+    acc.y += a.x * w.y + a.y * w.x;
+  }
+  double2 *p = R64 + (size_t)e * ldm + j;
+  p->x -= acc.x;
+  p->y -= acc.y;
+}
+
+__global__ void k_split_M(const double2 *__restrict__ M, long n, int E, long ldm, float2 *__restrict__ T32,
+                          double2 *__restrict__ y64, double2 *__restrict__ R64) {
+  const long i = blockIdx.y;
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ldm) return;
+  const double2 v = M[(size_t)i * ldm + j];
+  if (i < n) {
+    T32[(size_t)i * ldm + j] = j < n ? make_float2((float)v.x, (float)v.y) : make_float2(0.f, 0.f);
+    if (j == n) y64[i] = v;
+  } else {
+    R64[(size_t)(i - n) * ldm + j] = v;
+  }
+}
+
+__global__ void k_merge_M(const float2 *__restrict__ T32, const double2 *__restrict__ y64,
+                          const double2 *__restrict__ R64, long n, int E, long ldm, double2 *__restrict__ M) {
+  const long i = blockIdx.y;
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ldm) return;
+  double2 v;
+  if (i < n) {
+    if (j < n) {
+      const float2 t = T32[(size_t)i * ldm + j];
+      v = make_double2(t.x, t.y);
+    } else {
+      v = j == n ? y64[i] : make_double2(0.0, 0.0);
+    }
+  } else {
+    v = R64[(size_t)(i - n) * ldm + j];
+  }
+  M[(size_t)i * ldm + j] = v;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+cudaError_t get_encoder() {
+  std::call_once(g_encode_once, [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  });
+  return g_encode ? cudaSuccess : cudaErrorNotSupported;
+}
+
+// 2-D fp32 tensor map over rows x K (K contiguous, row pitch ldk floats),
+// box 32 x 128, 128-byte swizzle.
+cudaError_t make_map(CUtensorMap *m, const float *base, long rows, int K, long ldk) {
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ldk * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)TC_BM};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box,
+                              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+cudaError_t launch_split_M(Handle *h, int f) {
+  Freq &q = h->f[f];
+  dim3 g((unsigned)((h->ldm + 255) / 256), (unsigned)(h->n + h->E));
+  k_split_M<<<g, 256, 0, h->stream>>>(q.M64, h->n, h->E, h->ldm, q.T32, q.y64, q.R64);
+  h->nlaunch += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_merge_M(Handle *h, int f) {
+  Freq &q = h->f[f];
+  dim3 g((unsigned)((h->ldm + 255) / 256), (unsigned)(h->n + h->E));
+  k_merge_M<<<g, 256, 0, h->stream>>>(q.T32, q.y64, q.R64, h->n, h->E, h->ldm, q.M64);
+  h->nlaunch += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_c64_update(Handle *h, int f, int k) {
+  Freq &q = h->f[f];
+  const long n = h->n, rows = n + h->E;
+  cudaError_t e = get_encoder();
+  if (e != cudaSuccess) return e;
+  const int Kt = (6 * k + TC_BK - 1) / TC_BK * TC_BK;
+  if (Kt > h->kt_cap) return cudaErrorInvalidValue;
+  // FP64 side: y and R/Eobj
+  const long side = n + (long)h->E * (n + 1);
+  k_c64_side_update<<<(unsigned)((side + 255) / 256), 256, 0, h->stream>>>(q.y64, q.R64, n, h->E, h->ldm, h->d_A,
+                                                                           rows, h->d_W, k);
+  // tensor-core operands
+  const dim3 ga((unsigned)((Kt + 127) / 128), (unsigned)n), gb((unsigned)((Kt + 127) / 128), (unsigned)(2 * n));
+  k_build_Aop<<<ga, 128, 0, h->stream>>>(h->d_A, rows, n, k, Kt, h->kt_cap, h->d_Aop);
+  k_build_Bop<<<gb, 128, 0, h->stream>>>(h->d_W, h->ldm, n, k, Kt, h->kt_cap, h->d_Bop);
+  CUtensorMap ma, mb;
+  if ((e = make_map(&ma, h->d_Aop, h->aop_rows, Kt, h->kt_cap)) != cudaSuccess) return e;
+  if ((e = make_map(&mb, h->d_Bop, h->bop_rows, Kt, h->kt_cap)) != cudaSuccess) return e;
+  if ((e = cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM)) !=
+      cudaSuccess)
+    return e;
+  const int dcols = (int)(2 * n);
+  dim3 g((unsigned)((dcols + TC_BN - 1) / TC_BN), (unsigned)((n + TC_BM - 1) / TC_BM));
+  cudaEvent_t t0 = timing_mark(h);
+  k_tc_update<<<g, 192, TC_SMEM, h->stream>>>(ma, mb, reinterpret_cast<float *>(q.T32), 2 * h->ldm, (int)n, dcols,
+                                               Kt / TC_BK, h->d_tc_err);
+  const double cells = (double)n * (double)n;  // complex entries of T updated
+  timing_close(h, t0, T_UPDATE, 8.0 * k * cells,
+               2.0 * 8.0 * cells + 4.0 * Kt * ((double)h->aop_rows + (double)h->bop_rows), 0.0);
+  h->nlaunch += 4;
+  return cudaGetLastError();
+}
+
+}  // namespace pngf

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <vector>
 
 #include "pngf_internal.h"
 
@@ -51,6 +52,23 @@ template <> __device__ __forceinline__ double2 ldM<float2>(const float2 *M, size
   const float2 v = M[i];
   return make_double2(v.x, v.y);
 }
+
+// Read-only view of one frequency's state: the T block (N x N, leading
+// dimension ldt, FP64 or complex64), the y column (y_i = y[i*ys]) and the E
+// objective rows (R[e*ldr + j], with Eobj_e at column N). In the FP64 layout
+// all three live in M; in the complex64 layout T is stored in complex64 and y,
+// R, Eobj stay in FP64.
+template <typename TM> struct SV {
+  const TM *T;
+  long ldt;
+  const double2 *y;
+  long ys;
+  const double2 *R;
+  long ldr;
+  __device__ __forceinline__ double2 t(size_t i, size_t j) const { return ldM(T, i * ldt + j); }
+  __device__ __forceinline__ double2 yv(size_t i) const { return y[i * ys]; }
+  __device__ __forceinline__ double2 r(int e, size_t j) const { return R[(size_t)e * ldr + j]; }
+};
 
 struct Geo {
   int tiles_x, tiles_y, cells_x, cells_y;
@@ -334,20 +352,20 @@ __device__ void cta_lu_solve(const double2 *K, int ld, int k, const int *piv, do
 // z = D (Einc_s + x). Uses shared buffers K (ld x k), vec (k), einc (k),
 // piv (k). Returns LAPACK-style info.
 template <typename TM>
-__device__ int cta_capacitance(const TM *__restrict__ M, long ldm, long n, const double2 *__restrict__ Einc,
+__device__ int cta_capacitance(const SV<TM> &M, long n, const double2 *__restrict__ Einc,
                                const int *s, const signed char *d, int k, double2 *K, int ld, double2 *vec,
                                double2 *einc, int *piv, double *red) {
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int c = tid; c < k; c += nt) einc[c] = Einc[s[c]];
   for (int idx = tid; idx < k * k; idx += nt) {
     const int r = idx / k, c = idx % k;  // consecutive threads read along a row of M
-    double2 v = ldM(M, (size_t)s[r] * ldm + s[c]);
+    double2 v = M.t(s[r], s[c]);
     if (d[c] < 0) v = make_double2(-v.x, -v.y);
     K[r + c * ld] = v;  // T[s,s] D
   }
   __syncthreads();
   for (int r = tid; r < k; r += nt) {
-    double2 w = ldM(M, (size_t)s[r] * ldm + n);
+    double2 w = M.yv(s[r]);
     for (int c = 0; c < k; ++c) w = cfnma(w, K[r + c * ld], einc[c]);
     vec[r] = w;
   }
@@ -370,8 +388,8 @@ __device__ int cta_capacitance(const TM *__restrict__ M, long ldm, long n, const
 // evaluation
 
 template <typename TM>
-__global__ void __launch_bounds__(128) k_eval(const TM *const *__restrict__ Ms, const double2 *const *__restrict__ Eincs,
-                                              long ldm, long n, int E, int kmax, const int *__restrict__ es,
+__global__ void __launch_bounds__(128) k_eval(const SV<TM> *__restrict__ Ms, const double2 *const *__restrict__ Eincs,
+                                              long n, int E, int kmax, const int *__restrict__ es,
                                               const signed char *__restrict__ ed, const int *__restrict__ ek,
                                               const FreqConst *__restrict__ fconst, ObjConst oc, int nf,
                                               double2 *__restrict__ new_eobj, double *__restrict__ Ff,
@@ -388,7 +406,7 @@ __global__ void __launch_bounds__(128) k_eval(const TM *const *__restrict__ Ms, 
   __shared__ int piv[kMaxK];
   __shared__ double red[2];
   __shared__ double2 eo[PNGF_MAX_EOBJ];
-  const TM *M = Ms[f];
+  const SV<TM> M = Ms[f];
   const int k = ek[c];
   if (k < 0) {  // invalid candidate
     if (tid == 0) {
@@ -402,18 +420,17 @@ __global__ void __launch_bounds__(128) k_eval(const TM *const *__restrict__ Ms, 
     d[q] = ed[(size_t)c * kmax + q];
   }
   __syncthreads();
-  const int info = cta_capacitance(M, ldm, n, Eincs[f], s, d, k, K, ld, vec, einc, piv, red);
+  const int info = cta_capacitance(M, n, Eincs[f], s, d, k, K, ld, vec, einc, piv, red);
   // newEobj = Eobj - R[:,s] z, one warp per objective row.
   const int w = tid / 32, lane = tid % 32;
   for (int e = w; e < E; e += blockDim.x / 32) {
     double2 acc = make_double2(0.0, 0.0);
-    const size_t row = (size_t)(n + e) * ldm;
-    for (int q = lane; q < k; q += 32) acc = cadd(acc, cmul(ldM(M, row + s[q]), vec[q]));
+    for (int q = lane; q < k; q += 32) acc = cadd(acc, cmul(M.r(e, s[q]), vec[q]));
     for (int o = 16; o; o >>= 1) {
       acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
       acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
     }
-    if (lane == 0) eo[e] = csub(ldM(M, row + n), acc);
+    if (lane == 0) eo[e] = csub(M.r(e, n), acc);
   }
   __syncthreads();
   if (tid == 0) {
@@ -450,14 +467,14 @@ __global__ void k_score(int ncand, int nf, const double *__restrict__ Ff, double
 // Objective of the current state (F of the design M encodes) into F[0],
 // per-frequency perf into perf[f*3..].
 template <typename TM>
-__global__ void k_current_objective(const TM *const *__restrict__ Ms, long ldm, long n, int E,
+__global__ void k_current_objective(const SV<TM> *__restrict__ Ms, long n, int E,
                                     const FreqConst *__restrict__ fconst, ObjConst oc, int nf, double *F,
                                     double *perf) {
   if (threadIdx.x != 0) return;
   double acc = 0.0;
   for (int f = 0; f < nf; ++f) {
     double2 eo[PNGF_MAX_EOBJ];
-    for (int e = 0; e < E; ++e) eo[e] = ldM(Ms[f], (size_t)(n + e) * ldm + n);
+    for (int e = 0; e < E; ++e) eo[e] = Ms[f].r(e, n);
     acc += objective_term(eo, E, fconst[f], oc, perf + 3 * f);
   }
   *F = acc;
@@ -468,7 +485,7 @@ __global__ void k_current_objective(const TM *const *__restrict__ Ms, long ldm, 
 
 // One CTA: factors K for the edge list and stores the LU, pivots and z.
 template <typename TM>
-__global__ void __launch_bounds__(256) k_acc_factor(const TM *__restrict__ M, long ldm, long n,
+__global__ void __launch_bounds__(256) k_acc_factor(const SV<TM> M, long n,
                                                     const double2 *__restrict__ Einc, const int *__restrict__ gs,
                                                     const signed char *__restrict__ gd, int k, double2 *__restrict__ LU,
                                                     int *__restrict__ gpiv, double2 *__restrict__ z,
@@ -486,7 +503,7 @@ __global__ void __launch_bounds__(256) k_acc_factor(const TM *__restrict__ M, lo
     d[q] = gd[q];
   }
   __syncthreads();
-  const int info = cta_capacitance(M, ldm, n, Einc, s, d, k, K, k, vec, einc, piv, red);
+  const int info = cta_capacitance(M, n, Einc, s, d, k, K, k, vec, einc, piv, red);
   for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) LU[idx] = K[idx];
   for (int q = threadIdx.x; q < k; q += blockDim.x) {
     gpiv[q] = piv[q];
@@ -498,7 +515,7 @@ __global__ void __launch_bounds__(256) k_acc_factor(const TM *__restrict__ M, lo
 // W[r][j] = d_r (K^-1 M[s, j])_r for j < N, W[r][N] = z_r. One thread per
 // column, blockDim.x (32 or 64) columns per CTA; K's LU in shared memory.
 template <typename TM>
-__global__ void __launch_bounds__(64) k_acc_W(const TM *__restrict__ M, long ldm, long n, const int *__restrict__ gs,
+__global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int *__restrict__ gs,
                                               const signed char *__restrict__ gd, int k, const double2 *__restrict__ LU,
                                               const int *__restrict__ gpiv, const double2 *__restrict__ z,
                                               double2 *__restrict__ W, long ldw) {
@@ -521,7 +538,7 @@ __global__ void __launch_bounds__(64) k_acc_W(const TM *__restrict__ M, long ldm
   for (int idx = threadIdx.x; idx < k * bw; idx += blockDim.x) {
     const int r = idx / bw, jj = idx % bw;
     const long j = j0 + jj;
-    X[(size_t)jj * k + r] = j < n ? ldM(M, (size_t)s[r] * ldm + j) : make_double2(0.0, 0.0);
+    X[(size_t)jj * k + r] = j < n ? M.t(s[r], j) : make_double2(0.0, 0.0);
   }
   __syncthreads();
   const long j = j0 + threadIdx.x;
@@ -566,11 +583,14 @@ __global__ void __launch_bounds__(64) k_acc_W(const TM *__restrict__ M, long ldm
 
 // A[i + r*lda] = M[i][s_r], i < N+E.
 template <typename TM>
-__global__ void k_acc_gather(const TM *__restrict__ M, long ldm, long rows, const int *__restrict__ gs, int k,
+__global__ void k_acc_gather(const SV<TM> M, long n, long rows, const int *__restrict__ gs, int k,
                              double2 *__restrict__ A, long lda) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= rows) return;
-  for (int r = 0; r < k; ++r) A[(size_t)r * lda + i] = ldM(M, (size_t)i * ldm + gs[r]);
+  if (i < n)
+    for (int r = 0; r < k; ++r) A[(size_t)r * lda + i] = M.t(i, gs[r]);
+  else
+    for (int r = 0; r < k; ++r) A[(size_t)r * lda + i] = M.r((int)(i - n), gs[r]);
 }
 
 // M[i][j] -= sum_r A[i][r] W[r][j] for i < rows, j < cols. 64x64 tile per
@@ -649,6 +669,30 @@ __global__ void k_commit(int kmax, int c, const int *__restrict__ es, const sign
 
 static ObjConst obj_const(const Handle *h) { return ObjConst{h->cfg.dx, h->cfg.dy, h->cfg.dz}; }
 
+// Views of frequency f: the FP64 layout (everything in M64) and the complex64
+// layout (T in T32, y and R/Eobj in FP64).
+static SV<double2> view64(const Handle *h, int f) {
+  const double2 *M = h->f[f].M64;
+  return SV<double2>{M, h->ldm, M + h->n, h->ldm, M + (size_t)h->n * h->ldm, h->ldm};
+}
+static SV<float2> view32(const Handle *h, int f) {
+  return SV<float2>{h->f[f].T32, h->ldm, h->f[f].y64, 1, h->f[f].R64, h->ldm};
+}
+
+cudaError_t setup_views(Handle *h) {
+  const int nf = h->cfg.num_freq;
+  if (h->cfg.precision == PNGF_PREC_FP64) {
+    std::vector<SV<double2>> v(nf);
+    for (int f = 0; f < nf; ++f) v[f] = view64(h, f);
+    return cudaMemcpy(h->d_views, v.data(), sizeof(SV<double2>) * nf, cudaMemcpyHostToDevice);
+  }
+  std::vector<SV<float2>> v(nf);
+  for (int f = 0; f < nf; ++f) v[f] = view32(h, f);
+  return cudaMemcpy(h->d_views, v.data(), sizeof(SV<float2>) * nf, cudaMemcpyHostToDevice);
+}
+
+size_t view_bytes() { return sizeof(SV<double2>) > sizeof(SV<float2>) ? sizeof(SV<double2>) : sizeof(SV<float2>); }
+
 cudaError_t launch_init_M(Handle *h, int f) {
   Freq &q = h->f[f];
   const long n = h->n;
@@ -684,24 +728,24 @@ static size_t eval_smem(int kmax) {
   return sizeof(double2) * ((size_t)kmax * kmax + 2 * kmax) + sizeof(int) * kmax + kmax + 16;
 }
 
-template <typename TM> static cudaError_t launch_eval_t(Handle *h, const TM *const *dMs, int ncand) {
+template <typename TM> static cudaError_t launch_eval_t(Handle *h, int ncand) {
   const int nf = h->cfg.num_freq;
   const size_t sm = eval_smem(h->kmax);
   cudaError_t e = cudaFuncSetAttribute(k_eval<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k_eval<TM><<<dim3(ncand, nf), 128, sm, h->stream>>>(dMs, reinterpret_cast<const double2 *const *>(h->d_Eincs),
-                                                     h->ldm, h->n, h->E, h->kmax, h->d_es, h->d_ed, h->d_ek,
-                                                     h->d_fconst, obj_const(h), nf, h->d_new_eobj, h->d_Ff,
-                                                     h->d_perf, h->d_status);
+  k_eval<TM><<<dim3(ncand, nf), 128, sm, h->stream>>>(
+      static_cast<const SV<TM> *>(h->d_views), reinterpret_cast<const double2 *const *>(h->d_Eincs), h->n, h->E,
+      h->kmax, h->d_es, h->d_ed, h->d_ek, h->d_fconst, obj_const(h), nf, h->d_new_eobj, h->d_Ff, h->d_perf,
+      h->d_status);
   return cudaGetLastError();
 }
 
 cudaError_t launch_eval(Handle *h, int ncand, double F_best) {
   cudaError_t e;
   if (h->cfg.precision == PNGF_PREC_FP64)
-    e = launch_eval_t<double2>(h, reinterpret_cast<const double2 *const *>(h->d_M64s), ncand);
+    e = launch_eval_t<double2>(h, ncand);
   else
-    e = launch_eval_t<float2>(h, reinterpret_cast<const float2 *const *>(h->d_M32s), ncand);
+    e = launch_eval_t<float2>(h, ncand);
   if (e != cudaSuccess) return e;
   k_score<<<1, 256, 0, h->stream>>>(ncand, h->cfg.num_freq, h->d_Ff, F_best, h->d_F, h->d_first);
   h->nlaunch += 2;
@@ -710,35 +754,52 @@ cudaError_t launch_eval(Handle *h, int ncand, double F_best) {
 
 cudaError_t launch_current_objective(Handle *h) {
   if (h->cfg.precision == PNGF_PREC_FP64)
-    k_current_objective<double2><<<1, 32, 0, h->stream>>>(reinterpret_cast<const double2 *const *>(h->d_M64s),
-                                                          h->ldm, h->n, h->E, h->d_fconst, obj_const(h),
-                                                          h->cfg.num_freq, h->d_F, h->d_perf);
+    k_current_objective<double2><<<1, 32, 0, h->stream>>>(static_cast<const SV<double2> *>(h->d_views), h->n, h->E,
+                                                          h->d_fconst, obj_const(h), h->cfg.num_freq, h->d_F,
+                                                          h->d_perf);
   else
-    k_current_objective<float2><<<1, 32, 0, h->stream>>>(reinterpret_cast<const float2 *const *>(h->d_M32s),
-                                                         h->ldm, h->n, h->E, h->d_fconst, obj_const(h),
-                                                         h->cfg.num_freq, h->d_F, h->d_perf);
+    k_current_objective<float2><<<1, 32, 0, h->stream>>>(static_cast<const SV<float2> *>(h->d_views), h->n, h->E,
+                                                         h->d_fconst, obj_const(h), h->cfg.num_freq, h->d_F,
+                                                         h->d_perf);
   h->nlaunch += 1;
   return cudaGetLastError();
 }
 
-cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k) {
+// Accept prologue on either layout: K's LU and z, W = [D K^-1 T[s,:], z],
+// A = [T; R][:, s] (FP64, column-major with leading dimension N+E).
+template <typename TM>
+static cudaError_t accept_prologue(const SV<TM> &v, long n, int E, long ldm, const double2 *Einc, const int *d_s,
+                                   const signed char *d_d, int k, double2 *LU, int *piv, double2 *z, double2 *A,
+                                   double2 *W, int *status, cudaStream_t stream) {
+  const long rows = n + E;
+  const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
+  cudaError_t e = cudaFuncSetAttribute(k_acc_factor<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+  if (e != cudaSuccess) return e;
+  k_acc_factor<TM><<<1, 256, smf, stream>>>(v, n, Einc, d_s, d_d, k, LU, piv, z, status);
+  const int wc = k <= 64 ? 64 : 32;  // columns per CTA, so that K and the block fit in shared memory
+  const size_t smw = sizeof(double2) * ((size_t)k * k + (size_t)k * wc);
+  e = cudaFuncSetAttribute(k_acc_W<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
+  if (e != cudaSuccess) return e;
+  k_acc_W<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, LU, piv, z, W, ldm);
+  k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(v, n, rows, d_s, k, A, rows);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k, int layout) {
   Freq &q = h->f[f];
   const long n = h->n, rows = n + h->E;
   if (k <= 0) return cudaSuccess;
-  const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
-  cudaError_t e = cudaFuncSetAttribute(k_acc_factor<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+  cudaError_t e;
+  if (layout == PNGF_PREC_C64) {
+    e = accept_prologue<float2>(view32(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, h->d_LU, h->d_piv, h->d_z,
+                                h->d_A, h->d_W, h->d_acc_status, h->stream);
+    if (e != cudaSuccess) return e;
+    h->nlaunch += 3;
+    return launch_c64_update(h, f, k);
+  }
+  e = accept_prologue<double2>(view64(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, h->d_LU, h->d_piv, h->d_z,
+                               h->d_A, h->d_W, h->d_acc_status, h->stream);
   if (e != cudaSuccess) return e;
-  k_acc_factor<double2><<<1, 256, smf, h->stream>>>(q.M64, h->ldm, n, q.Einc, d_s, d_d, k, h->d_LU, h->d_piv,
-                                                    h->d_z, h->d_acc_status);
-  const int wc = k <= 64 ? 64 : 32;  // columns per CTA, so that K and the block fit in shared memory
-  const size_t smw = sizeof(double2) * ((size_t)k * k + (size_t)k * wc);
-  e = cudaFuncSetAttribute(k_acc_W<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
-  if (e != cudaSuccess) return e;
-  k_acc_W<double2><<<(unsigned)((h->ldm + wc - 1) / wc), wc, smw, h->stream>>>(q.M64, h->ldm, n, d_s, d_d, k,
-                                                                              h->d_LU, h->d_piv, h->d_z, h->d_W,
-                                                                              h->ldm);
-  k_acc_gather<double2><<<(unsigned)((rows + 255) / 256), 256, 0, h->stream>>>(q.M64, h->ldm, rows, d_s, k, h->d_A,
-                                                                              rows);
   dim3 g((unsigned)((n + 1 + RU_T - 1) / RU_T), (unsigned)((rows + RU_T - 1) / RU_T));
   cudaEvent_t t0 = timing_mark(h);
   k_rank_update<<<g, 256, 0, h->stream>>>(q.M64, h->ldm, rows, n + 1, h->d_A, rows, h->d_W, h->ldm, k);
@@ -753,16 +814,9 @@ cudaError_t launch_accept_raw(double2 *M, long ldm, long n, int E, const double2
                               double2 *W, int *status, cudaStream_t stream) {
   const long rows = n + E;
   if (k <= 0) return cudaSuccess;
-  const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
-  cudaError_t e = cudaFuncSetAttribute(k_acc_factor<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+  const SV<double2> v{M, ldm, M + n, ldm, M + (size_t)n * ldm, ldm};
+  cudaError_t e = accept_prologue<double2>(v, n, E, ldm, Einc, d_s, d_d, k, LU, piv, z, A, W, status, stream);
   if (e != cudaSuccess) return e;
-  k_acc_factor<double2><<<1, 256, smf, stream>>>(M, ldm, n, Einc, d_s, d_d, k, LU, piv, z, status);
-  const int wc = k <= 64 ? 64 : 32;
-  const size_t smw = sizeof(double2) * ((size_t)k * k + (size_t)k * wc);
-  e = cudaFuncSetAttribute(k_acc_W<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
-  if (e != cudaSuccess) return e;
-  k_acc_W<double2><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(M, ldm, n, d_s, d_d, k, LU, piv, z, W, ldm);
-  k_acc_gather<double2><<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(M, ldm, rows, d_s, k, A, rows);
   dim3 g((unsigned)((n + 1 + RU_T - 1) / RU_T), (unsigned)((rows + RU_T - 1) / RU_T));
   k_rank_update<<<g, 256, 0, stream>>>(M, ldm, rows, n + 1, A, rows, W, ldm, k);
   return cudaGetLastError();

@@ -27,8 +27,10 @@ struct Freq {
   double2 *G = nullptr;      // N x N column-major, as loaded (kept for refresh / drift check)
   double2 *gobj = nullptr;   // (E-1) x N row-major objective rows from the file
   double2 *Einc = nullptr;   // N
-  double2 *M64 = nullptr;    // (N+E) x ldm row-major, FP64 mode (or FP64 staging)
-  float2 *M32 = nullptr;     // (N+E) x ldm row-major, C64 mode
+  double2 *M64 = nullptr;    // (N+E) x ldm row-major: the FP64 state (C64 mode: build staging)
+  float2 *T32 = nullptr;     // C64 mode: T (N x ldm row-major, complex64)
+  double2 *y64 = nullptr;    // C64 mode: y (N) in FP64
+  double2 *R64 = nullptr;    // C64 mode: R and Eobj (E x ldm row-major, Eobj at column N) in FP64
   bool loaded = false;
 };
 
@@ -45,9 +47,14 @@ struct Handle {
   cudaStream_t own_stream = nullptr;
   std::vector<Freq> f;
   FreqConst *d_fconst = nullptr;
-  void **d_M64s = nullptr;     // device array of per-frequency M64 pointers
-  void **d_M32s = nullptr;     // device array of per-frequency M32 pointers
+  void *d_views = nullptr;     // device array of per-frequency state views (kernels_fp64.cu)
   void **d_Eincs = nullptr;    // device array of per-frequency Einc pointers
+  // C64 tensor-core update operands (kernels_c64.cu)
+  float *d_Aop = nullptr;      // rows_pad x kt_cap fp32, K-major
+  float *d_Bop = nullptr;      // cols_pad x kt_cap fp32, K-major
+  int kt_cap = 0;
+  long aop_rows = 0, bop_rows = 0;
+  int *d_tc_err = nullptr;     // set by bounded waits in the tensor-core kernel
   std::vector<FreqConst> h_fconst;
 
   // design
@@ -142,8 +149,20 @@ cudaError_t launch_eval(Handle *h, int ncand, double F_best);
 // Objective of the current design (from M's Eobj entries) into d_F[0].
 cudaError_t launch_current_objective(Handle *h);
 // Rank-k accept of an explicit edge list (device arrays s, d of length k) at
-// frequency f.
-cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k);
+// frequency f, on the FP64 layout (M64) or the complex64 layout (layout =
+// PNGF_PREC_C64: T32 on tensor cores, y64 / R64 in FP64).
+cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k, int layout);
+// Uploads the per-frequency state views for the handle's precision.
+cudaError_t setup_views(Handle *h);
+size_t view_bytes();
+// ---- complex64 form (kernels_c64.cu) ----
+// Splits the FP64 M of frequency f into T32 (complex64), y64 and R64.
+cudaError_t launch_split_M(Handle *h, int f);
+// After the accept prologue (h->d_A, h->d_W in FP64): updates y64 and R64 in
+// FP64 and T32 -= A W on the tensor cores (3xTF32 split products).
+cudaError_t launch_c64_update(Handle *h, int f, int k);
+// Reassembles frequency f's M in FP64 (into M64) from T32, y64, R64.
+cudaError_t launch_merge_M(Handle *h, int f);
 // Commits P and the tile map on the device for candidate c of the batch.
 cudaError_t launch_commit(Handle *h, int c);
 // The accept kernels on caller-supplied buffers (no handle): scratch LU (k^2),

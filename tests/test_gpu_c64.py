@@ -1,0 +1,86 @@
+"""Complex64 form (T in complex64, rank-k accept update on tcgen05 tensor
+cores with 3xTF32 split products; capacitance LU, y, R, Eobj, objective and
+accept test in FP64) against the plain FP64 form on the same G and design.
+
+Tolerances: the prepared state differs only by the complex64 rounding of T
+(relative 2^-24); one tensor-core accept keeps T within 1e-6 of max|T|;
+newEobj within 1e-5 relative, F within 1e-7 relative; a DBS run's objective
+within 1e-3 relative of the FP64 run's."""
+import numpy as np
+import pytest
+
+from conftest import case_G
+
+pytestmark = pytest.mark.gpu
+
+
+def handles(c, Gs, gobj, tm, max_flips):
+    from pngf_gb300 import lib
+    a = c["tiles"]
+    mid = (a - 1) // 2
+    out = []
+    for prec in (lib.PREC_FP64, lib.PREC_C64):
+        h = lib.Handle(a, a, c["freqs"], precision=prec, max_flips=max_flips)
+        for f, G in enumerate(Gs):
+            h.load_G(f, G, gobj[f])
+        h.set_tile_map(tm)
+        h.set_source_port(mid, mid, 1, 2)
+        h.prepare()
+        out.append(h)
+    return out
+
+
+@pytest.mark.parametrize("max_flips", [1, 4])
+def test_c64_eval_and_tensor_core_accept_match_fp64(max_flips, cases, built_lib):
+    c = cases["sym_9x9_f2_seed3"]
+    Gs, gobj = case_G(c, built_lib)
+    a = c["tiles"]
+    rng = np.random.default_rng(7)
+    tm = [int(v) for v in rng.integers(0, 2, a * a)]
+    h64, h32 = handles(c, Gs, gobj, tm, max_flips)
+    n = h64.n
+    for f in range(len(Gs)):
+        M64, _ = h64.get_M(f)
+        M32, _ = h32.get_M(f)
+        scale = np.abs(M64[:n, :n]).max()
+        assert np.abs(M32[:n, :n] - M64[:n, :n]).max() <= 2e-7 * scale
+        np.testing.assert_allclose(M32[n:], M64[n:], rtol=0, atol=1e-14 * np.abs(M64[n:]).max())
+    # DBS never flips the source tile (main.cpp:358-359): metal on the port
+    # edges shorts the port (|S11| = 1), an ill-conditioned case.
+    mid = (a - 1) // 2
+    pool = [t for t in range(a * a) if t != mid * a + mid]
+    cands = [[int(t) for t in rng.choice(pool, size=max_flips, replace=False)] for _ in range(40)]
+    eo64, F64 = h64.eval_candidates(cands)
+    eo32, F32 = h32.eval_candidates(cands)
+    np.testing.assert_allclose(eo32, eo64, rtol=1e-5, atol=1e-5 * np.abs(eo64).max())
+    np.testing.assert_allclose(F32, F64, rtol=1e-7)
+    for pick in (3, 11):  # two tensor-core accepts in a row
+        h64.accept(pick)
+        h32.accept(pick)
+        for f in range(len(Gs)):
+            M64, _ = h64.get_M(f)
+            M32, _ = h32.get_M(f)
+            scale = np.abs(M64[:n, :n]).max()
+            err = np.abs(M32[:n, :n] - M64[:n, :n]).max()
+            assert err <= 1e-6 * scale, (pick, f, err / scale)
+            e64, _ = h64.eobj(f)
+            e32, _ = h32.eobj(f)
+            np.testing.assert_allclose(e32, e64, rtol=1e-5, atol=1e-5 * np.abs(e64).max())
+        eo64, F64 = h64.eval_candidates(cands)
+        eo32, F32 = h32.eval_candidates(cands)
+        np.testing.assert_allclose(F32, F64, rtol=1e-7)
+
+
+def test_c64_dbs_reaches_fp64_objective(cases, built_lib):
+    from pngf_gb300 import lib
+    c = cases["single_11x11_f3_seed2"]
+    Gs, gobj = case_G(c, built_lib)
+    res = {}
+    for prec in (lib.PREC_FP64, lib.PREC_C64):
+        h = lib.Handle(11, 11, c["freqs"], precision=prec, max_flips=1)
+        for f, G in enumerate(Gs):
+            h.load_G(f, G, gobj[f])
+        d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=c["seed"], max_evals=600)
+        res[prec] = d.run()
+    F64, F32 = res[lib.PREC_FP64].F_best, res[lib.PREC_C64].F_best
+    assert abs(F32 - F64) <= 1e-3 * abs(F64)
