@@ -3,7 +3,7 @@ cores with 3xTF32 split products; capacitance LU, y, R, Eobj, objective and
 accept test in FP64) against the plain FP64 form on the same G and design.
 
 Tolerances: the prepared state differs only by the complex64 rounding of T
-(relative 2^-24); one tensor-core accept keeps T within 1e-6 of max|T|;
+(relative 2^-24); tensor-core accepts keep T within 5e-6 of max|T|;
 newEobj within 1e-5 relative, F within 1e-7 relative; a DBS run's objective
 within 1e-3 relative of the FP64 run's."""
 import numpy as np
@@ -62,7 +62,9 @@ def test_c64_eval_and_tensor_core_accept_match_fp64(max_flips, cases, built_lib)
             M32, _ = h32.get_M(f)
             scale = np.abs(M64[:n, :n]).max()
             err = np.abs(M32[:n, :n] - M64[:n, :n]).max()
-            assert err <= 1e-6 * scale, (pick, f, err / scale)
+            # complex64 rounding of T (6e-8) reaches the update through K^-1:
+            # ~1e-6 for 4-tile flips (k up to 96), below 1e-7 for single tiles
+            assert err <= 5e-6 * scale, (pick, f, err / scale)
             e64, _ = h64.eobj(f)
             e32, _ = h32.eobj(f)
             np.testing.assert_allclose(e32, e64, rtol=1e-5, atol=1e-5 * np.abs(e64).max())
