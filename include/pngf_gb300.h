@@ -68,7 +68,16 @@ typedef struct pngf_config {
   int precision;         /* PNGF_PREC_FP64 or PNGF_PREC_C64 */
   int defer_rank;        /* C64: flush the deferred low-rank correction at this rank (0 = every accept) */
   int device;            /* CUDA device ordinal */
+  int fp64_update;       /* PNGF_PREC_FP64: PNGF_F64_TENSOR (default) or PNGF_F64_SIMT */
 } pngf_config;
+
+/* How a PNGF_PREC_FP64 handle runs its rank-k accept update:
+ * PNGF_F64_TENSOR - exact integer slices on the BF16 tensor cores, recombined
+ *                   to FP64 accuracy (flip sets of up to 32 edges; larger ones
+ *                   use the FP64 units);
+ * PNGF_F64_SIMT   - FP64 fused multiply-adds on the FP64 units. */
+#define PNGF_F64_TENSOR 0
+#define PNGF_F64_SIMT 1
 
 /* Fills a config with the reference's defaults (main.cpp:142-160):
  * 3x3 cells per tile, E = 3, dx = dy = 0.01/60 m, dz = 0.01/180 m, FP64. */

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpngf_gb300.so")
 
-SOURCES = ["kernels_fp64.cu", "kernels_c64.cu", "capi.cu", "dbs.cpp", "gfile.cpp", "noalloc.cu"]
+SOURCES = ["kernels_fp64.cu", "kernels_c64.cu", "kernels_f64tc.cu", "capi.cu", "dbs.cpp", "gfile.cpp", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "-I" + os.path.join(ROOT, "include")]
 
@@ -35,7 +35,7 @@ def _compile(src: str) -> str:
     path = os.path.join(CSRC, src)
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(
             os.path.getmtime(path), *[os.path.getmtime(os.path.join(CSRC, h)) for h in os.listdir(CSRC)
-                                      if h.endswith(".h")],
+                                      if h.endswith(".h") or h.endswith(".cuh")],
             os.path.getmtime(os.path.join(ROOT, "include", "pngf_gb300.h"))):
         return obj
     cmd = [nvcc()] + ARCH + COMMON + ["-c", path, "-o", obj]

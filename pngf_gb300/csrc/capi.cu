@@ -243,7 +243,7 @@ int accept_cand(Handle *h, int c, int k) {
     timing_close(h, t0, T_ACCEPT, 0.0, 0.0, 0.0);
   }
   PNGF_CUDA(h, launch_commit(h, c));
-  if (h->cfg.precision == PNGF_PREC_C64) {  // the tensor-core kernel's bounded waits report here
+  if (h->d_tc_err) {  // the tensor-core kernels' bounded waits report here
     int tc = 0;
     PNGF_CUDA(h, cudaMemcpyAsync(&tc, h->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -310,6 +310,10 @@ int pngf_destroy(pngf_handle *ph) {
   dfree(h->d_Aop);
   dfree(h->d_Bop);
   dfree(h->d_tc_err);
+  dfree(h->d_A16);
+  dfree(h->d_B16);
+  dfree(h->d_eA);
+  dfree(h->d_fB);
   dfree(h->d_tile_map);
   dfree(h->d_P);
   dfree(h->d_tiles);
@@ -407,6 +411,21 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
       return fail(rc);
     if (cudaMemset(h->d_Aop, 0, sizeof(float) * h->aop_rows * h->kt_cap) != cudaSuccess ||
         cudaMemset(h->d_Bop, 0, sizeof(float) * h->bop_rows * h->kt_cap) != cudaSuccess ||
+        cudaMemset(h->d_tc_err, 0, sizeof(int)) != cudaSuccess)
+      return fail(PNGF_ERR_CUDA);
+  }
+  if (!c64 && c.fp64_update != PNGF_F64_SIMT) {  // FP64 updates on the tensor cores
+    h->f64tc = true;
+    h->init_chunk = f64tc_max_k();
+    h->a16_rows = (rows + 127) / 128 * 128;
+    h->b16_rows = (2 * (n + 1) + 127) / 128 * 128;
+    const size_t ca = (size_t)h->a16_rows * f64tc_op_cols(), cb = (size_t)h->b16_rows * f64tc_op_cols();
+    if (cudaMalloc(&h->d_A16, 2 * ca) != cudaSuccess || cudaMalloc(&h->d_B16, 2 * cb) != cudaSuccess)
+      return fail(PNGF_ERR_NOMEM);
+    if ((rc = dalloc(h, &h->d_eA, (size_t)h->a16_rows)) || (rc = dalloc(h, &h->d_fB, (size_t)h->b16_rows)) ||
+        (rc = dalloc(h, &h->d_tc_err, 1)))
+      return fail(rc);
+    if (cudaMemset(h->d_A16, 0, 2 * ca) != cudaSuccess || cudaMemset(h->d_B16, 0, 2 * cb) != cudaSuccess ||
         cudaMemset(h->d_tc_err, 0, sizeof(int)) != cudaSuccess)
       return fail(PNGF_ERR_CUDA);
   }
@@ -544,18 +563,23 @@ int pngf_prepare(pngf_handle *ph) {
   PNGF_CUDA(h, cudaMemsetAsync(h->d_acc_status, 0, sizeof(int), h->stream));
   for (int f = 0; f < h->cfg.num_freq; ++f) {
     PNGF_CUDA(h, launch_init_M(h, f));
-    for (size_t c0 = 0; c0 < on.size(); c0 += kInitChunk) {
-      const int k = (int)std::min<size_t>(kInitChunk, on.size() - c0);
+    for (size_t c0 = 0; c0 < on.size(); c0 += h->init_chunk) {
+      const int k = (int)std::min<size_t>(h->init_chunk, on.size() - c0);
       PNGF_CUDA(h, launch_accept_edges(h, f, h->d_acc_s + c0, h->d_acc_d + c0, k, PNGF_PREC_FP64));
     }
     if (h->cfg.precision == PNGF_PREC_C64) PNGF_CUDA(h, launch_split_M(h, f));
   }
-  int st = 0;
+  int st = 0, tc = 0;
   PNGF_CUDA(h, cudaMemcpyAsync(&st, h->d_acc_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  if (h->d_tc_err) PNGF_CUDA(h, cudaMemcpyAsync(&tc, h->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   PNGF_CUDA(h, cudaMemcpyAsync(h->h_fconst.data(), h->d_fconst, sizeof(FreqConst) * h->cfg.num_freq,
                                cudaMemcpyDeviceToHost, h->stream));
   PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
   if (st != PNGF_OK) return set_error(h, st, "singular capacitance matrix while building M for the design");
+  if (tc != 0) {
+    cudaMemset(h->d_tc_err, 0, sizeof(int));
+    return set_error(h, PNGF_ERR_TIMEOUT, "tensor-core update gave up waiting (code " + std::to_string(tc) + ")");
+  }
   h->prepared = true;
   h->batch_valid = false;
   return PNGF_OK;

@@ -12,7 +12,7 @@
 //
 // Kernel k_tc_update: one CTA per 128 x 128 output tile, 6 warps:
 //   warp 0  TMA producer: 128B-swizzled K-major tiles of A_op and B_op into a
-//           3-stage shared-memory ring (mbarrier complete_tx);
+//           2-stage shared-memory ring (mbarrier complete_tx), 3 CTAs per SM;
 //   warp 1  TMEM allocation and a single elected thread issuing
 //           tcgen05.mma.cta_group::1.kind::tf32 (M=128, N=128, K=8) into a
 //           128-column FP32 accumulator in TMEM, tcgen05.commit per stage;
@@ -27,6 +27,7 @@
 #include <mutex>
 
 #include "pngf_internal.h"
+#include "tc_common.cuh"
 
 namespace pngf {
 
@@ -35,12 +36,12 @@ namespace {
 constexpr int TC_BM = 128;       // rows per tile (MMA M)
 constexpr int TC_BN = 128;       // fp32 columns per tile (MMA N)
 constexpr int TC_BK = 32;        // fp32 K elements per stage = one 128-byte swizzle row
-constexpr int TC_ST = 3;         // pipeline stages
+constexpr int TC_ST = 2;         // pipeline stages (3 CTAs per SM fit in shared memory and TMEM)
 constexpr uint32_t A_BYTES = TC_BM * TC_BK * 4;
 constexpr uint32_t B_BYTES = TC_BN * TC_BK * 4;
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr size_t TC_SMEM = TC_ST * STAGE_BYTES + 1024 + 256;
-constexpr uint32_t kSpinLimit = 1u << 24;
+using namespace tc;
 
 // Instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
 // (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits
@@ -48,84 +49,10 @@ constexpr uint32_t kSpinLimit = 1u << 24;
 constexpr uint32_t kIdescTF32 =
     (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait for the phase with the given parity; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
-      : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor for a K-major tile with 128-byte swizzle:
-// start address >> 4 (bits 0-13), leading byte offset 16 B (unused for this
-// layout, bits 16-29), stride byte offset 1024 B between 8-row groups (bits
-// 32-45), descriptor version 1 (bits 46-47), layout SWIZZLE_128B = 2 (bits 61-63).
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
-  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
-         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
-}
-
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-      : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int q = 0; q < 16; ++q) v[q] = __uint_as_float(r[q]);
-}
-
-__device__ __forceinline__ float to_tf32(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
-}
-
 // D[i, j] -= sum_k Aop[i, k] Bop[j, k] for i < rows, j < cols (fp32, D row-major
 // with leading dimension ldd). Aop / Bop come through TMA maps (K-major, 128B
 // swizzle). nkb = K / 32.
-__global__ void __launch_bounds__(192, 1) k_tc_update(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(192, 3) k_tc_update(const __grid_constant__ CUtensorMap tmA,
                                                       const __grid_constant__ CUtensorMap tmB, float *__restrict__ D,
                                                       long ldd, int rows, int cols, int nkb, int *err) {
   extern __shared__ unsigned char smem_raw[];
@@ -199,35 +126,57 @@ __global__ void __launch_bounds__(192, 1) k_tc_update(const __grid_constant__ CU
     }
     __syncwarp();
   } else {
+    const int q = warp & 3;  // this warp may access TMEM lanes 32q .. 32q+31
+    const int row = m0 + q * 32 + lane;
+    const bool rin = row < rows;
+    float *drow = D + (size_t)row * ldd;
+    // The first half of this thread's row segment is read while the MMAs run;
+    // the second half is read while the first half is written back.
+    constexpr int HALF = TC_BN / 2;
+    float4 pre[HALF / 4];
+#pragma unroll
+    for (int u = 0; u < HALF / 4; ++u) {
+      const int col = n0 + 4 * u;
+      pre[u] = (rin && col + 4 <= cols) ? *reinterpret_cast<const float4 *>(drow + col) : make_float4(0, 0, 0, 0);
+    }
     // warp-uniform outcome: tcgen05.ld below is .sync.aligned
     const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
     tc_fence_after();
     if (!ok) {
       if (lane == 0) atomicExch(err, 3);
     } else {
-      const int q = warp & 3;  // this warp may access TMEM lanes 32q .. 32q+31
-      const int row = m0 + q * 32 + lane;
-      float *drow = D + (size_t)row * ldd;
-#pragma unroll 1
-      for (int c = 0; c < TC_BN / 16; ++c) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 16), v);
-        const int col0 = n0 + c * 16;
-        if (row < rows) {
-          if (col0 + 16 <= cols) {
-            float4 *p = reinterpret_cast<float4 *>(drow + col0);
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+#pragma unroll
+        for (int c = 0; c < HALF / 16; ++c) {
+          float v[16];
+          const int cc = half * (HALF / 16) + c;
+          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cc * 16), v);
+          const int col0 = n0 + cc * 16;
+          if (rin) {
+            if (col0 + 16 <= cols) {
+              float4 *p = reinterpret_cast<float4 *>(drow + col0);
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                float4 x = pre[c * 4 + u];
+                x.x -= v[4 * u];
+                x.y -= v[4 * u + 1];
+                x.z -= v[4 * u + 2];
+                x.w -= v[4 * u + 3];
+                p[u] = x;
+              }
+            } else {
+              for (int u = 0; u < 16; ++u)
+                if (col0 + u < cols) drow[col0 + u] -= v[u];
+            }
+          }
+          if (half == 0) {  // refill this slot with the matching chunk of the second half
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
-              float4 x = p[u];
-              x.x -= v[4 * u];
-              x.y -= v[4 * u + 1];
-              x.z -= v[4 * u + 2];
-              x.w -= v[4 * u + 3];
-              p[u] = x;
+              const int col = n0 + HALF + c * 16 + 4 * u;
+              pre[c * 4 + u] =
+                  (rin && col + 4 <= cols) ? *reinterpret_cast<const float4 *>(drow + col) : make_float4(0, 0, 0, 0);
             }
-          } else {
-            for (int u = 0; u < 16; ++u)
-              if (col0 + u < cols) drow[col0 + u] -= v[u];
           }
         }
       }

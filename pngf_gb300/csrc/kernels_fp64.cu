@@ -800,6 +800,10 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   e = accept_prologue<double2>(view64(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, h->d_LU, h->d_piv, h->d_z,
                                h->d_A, h->d_W, h->d_acc_status, h->stream);
   if (e != cudaSuccess) return e;
+  if (h->f64tc && k <= f64tc_max_k()) {
+    h->nlaunch += 3;
+    return launch_f64tc_update(h, f, k, q.M64, h->d_A, h->d_W);
+  }
   dim3 g((unsigned)((n + 1 + RU_T - 1) / RU_T), (unsigned)((rows + RU_T - 1) / RU_T));
   cudaEvent_t t0 = timing_mark(h);
   k_rank_update<<<g, 256, 0, h->stream>>>(q.M64, h->ldm, rows, n + 1, h->d_A, rows, h->d_W, h->ldm, k);

@@ -54,7 +54,13 @@ struct Handle {
   float *d_Bop = nullptr;      // cols_pad x kt_cap fp32, K-major
   int kt_cap = 0;
   long aop_rows = 0, bop_rows = 0;
-  int *d_tc_err = nullptr;     // set by bounded waits in the tensor-core kernel
+  int *d_tc_err = nullptr;     // set by bounded waits in the tensor-core kernels
+  // FP64 tensor-core update operands (kernels_f64tc.cu)
+  void *d_A16 = nullptr, *d_B16 = nullptr;  // bf16 slices, a16_rows / b16_rows x f64tc_op_cols()
+  int *d_eA = nullptr, *d_fB = nullptr;     // per-row / per-column power-of-two scales
+  long a16_rows = 0, b16_rows = 0;
+  bool f64tc = false;                       // FP64 updates of up to f64tc_max_k() edges on tensor cores
+  int init_chunk = kInitChunk;
   std::vector<FreqConst> h_fconst;
 
   // design
@@ -163,6 +169,11 @@ cudaError_t launch_split_M(Handle *h, int f);
 cudaError_t launch_c64_update(Handle *h, int f, int k);
 // Reassembles frequency f's M in FP64 (into M64) from T32, y64, R64.
 cudaError_t launch_merge_M(Handle *h, int f);
+// ---- FP64-accurate update on the tensor cores (kernels_f64tc.cu) ----
+int f64tc_max_k();
+size_t f64tc_op_cols();
+// M -= A W for M ((N+E) x ldm complex128), A ((N+E) x k column-major), W (k x ldm).
+cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W);
 // Commits P and the tile map on the device for candidate c of the batch.
 cudaError_t launch_commit(Handle *h, int c);
 // The accept kernels on caller-supplied buffers (no handle): scratch LU (k^2),

@@ -21,6 +21,7 @@ ERRORS = {1: "PNGF_ERR_ARG", 2: "PNGF_ERR_CUDA", 3: "PNGF_ERR_NOMEM", 4: "PNGF_E
           6: "PNGF_ERR_STATE", 7: "PNGF_ERR_TIMEOUT", 8: "PNGF_ERR_UNSUPPORTED", 9: "PNGF_ERR_NO_DEVICE",
           10: "PNGF_ERR_SCRATCH"}
 PREC_FP64, PREC_C64 = 0, 1
+F64_TENSOR, F64_SIMT = 0, 1
 DBS_SYMMETRIC, DBS_SINGLE = 0, 1
 INIT_EMPTY, INIT_RANDOM = 0, 1
 MAX_FREQ = 16
@@ -36,7 +37,7 @@ class Config(C.Structure):
     _fields_ = [("tiles_x", C.c_int), ("tiles_y", C.c_int), ("cells_x", C.c_int), ("cells_y", C.c_int),
                 ("num_eobj", C.c_int), ("max_flips", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
                 ("dz", C.c_double), ("num_freq", C.c_int), ("freq_hz", C.c_double * MAX_FREQ),
-                ("precision", C.c_int), ("defer_rank", C.c_int), ("device", C.c_int)]
+                ("precision", C.c_int), ("defer_rank", C.c_int), ("device", C.c_int), ("fp64_update", C.c_int)]
 
 
 class DbsParams(C.Structure):
@@ -153,7 +154,7 @@ class Handle:
     """Owns one pngf_handle (all frequencies of one DBS instance)."""
 
     def __init__(self, tiles_x, tiles_y, freqs, precision=PREC_FP64, max_flips=4, num_eobj=3, defer_rank=0,
-                 device=0):
+                 device=0, fp64_update=0):
         L = load()
         self.L = L
         cfg = Config()
@@ -164,6 +165,7 @@ class Handle:
         cfg.precision = precision
         cfg.defer_rank = defer_rank
         cfg.device = device
+        cfg.fp64_update = fp64_update
         self.cfg = cfg
         self.nf = len(freqs)
         self.E = num_eobj

@@ -4,7 +4,8 @@ accept test in FP64) against the plain FP64 form on the same G and design.
 
 Tolerances: the prepared state differs only by the complex64 rounding of T
 (relative 2^-24); tensor-core accepts keep T within 5e-6 of max|T|;
-newEobj within 1e-5 relative, F within 1e-7 relative; a DBS run's objective
+newEobj within 1e-5 relative, F within 1e-7 relative (1e-6 after accepted
+4-tile flips); a DBS run's objective
 within 1e-3 relative of the FP64 run's."""
 import numpy as np
 import pytest
@@ -70,7 +71,7 @@ def test_c64_eval_and_tensor_core_accept_match_fp64(max_flips, cases, built_lib)
             np.testing.assert_allclose(e32, e64, rtol=1e-5, atol=1e-5 * np.abs(e64).max())
         eo64, F64 = h64.eval_candidates(cands)
         eo32, F32 = h32.eval_candidates(cands)
-        np.testing.assert_allclose(F32, F64, rtol=1e-7)
+        np.testing.assert_allclose(F32, F64, rtol=1e-6)  # accepted 4-tile flips carry ~1e-7 of c64 rounding
 
 
 def test_c64_dbs_reaches_fp64_objective(cases, built_lib):
