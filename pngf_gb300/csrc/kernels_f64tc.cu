@@ -123,9 +123,31 @@ __global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, 
   }
 }
 
-__device__ __forceinline__ double pow2(int e) {
-  if (e > -1023 && e < 1024) return __longlong_as_double((long long)(e + 1023) << 52);
-  return ldexp(1.0, e);
+// Exact int32 value of a float holding an integer of magnitude below 2^22:
+// adding 1.5 * 2^23 puts the integer in the low mantissa bits (FP32 pipe only).
+__device__ __forceinline__ int f2i_exact(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
+
+// Y * 2^E as a double, built from the bits on the integer pipe (round half
+// up to 53 bits). Falls back to ldexp outside the normal exponent range.
+__device__ __forceinline__ double i64_scaled(long long Y, int E) {
+  if (Y == 0) return 0.0;
+  const unsigned long long s = Y < 0 ? 1ull : 0ull;
+  unsigned long long u = Y < 0 ? (unsigned long long)(-Y) : (unsigned long long)Y;
+  int msb = 63 - __clzll((long long)u);
+  unsigned long long mant;
+  if (msb > 52) {
+    const int sh = msb - 52;
+    mant = (u + (1ull << (sh - 1))) >> sh;
+    if (mant >> 53) {  // rounding carried into a new leading bit
+      mant >>= 1;
+      ++msb;
+    }
+  } else {
+    mant = u << (52 - msb);
+  }
+  const int be = msb + E + 1023;
+  if (be <= 0 || be >= 2047) return ldexp((double)Y, E);
+  return __longlong_as_double((long long)((s << 63) | ((unsigned long long)be << 52) | (mant & ((1ull << 52) - 1))));
 }
 
 // D[i, j] -= sum_c A_real[i, c] B_real[j, c] (exact to the truncation above)
@@ -195,41 +217,61 @@ __global__ void __launch_bounds__(192, 1) k_tc_update_f64(const __grid_constant_
     }
     __syncwarp();
   } else {
+    const int q = warp & 3;
+    const int row = m0 + q * 32 + lane;
+    const bool rin = row < rows;
+    const int ea = rin ? eA[row] : 0;
+    double *drow = D + (size_t)row * ldd;
+    // Chunk c of this thread's row segment: 16 doubles. Loads run one chunk
+    // ahead (the first while the MMAs run).
+    double2 cur[8], nxt[8];
+    auto load_chunk = [&](int c, double2 *dst) {
+      const int col0 = n0 + c * 16;
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        dst[u] = (rin && col0 + 16 <= cols) ? reinterpret_cast<const double2 *>(drow + col0)[u]
+                                            : make_double2(0.0, 0.0);
+    };
+    load_chunk(0, cur);
     const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
     tc_fence_after();
     if (!ok) {
       if (lane == 0) atomicExch(err, 13);
     } else {
-      const int q = warp & 3;
-      const int row = m0 + q * 32 + lane;
-      const int ea = row < rows ? eA[row] : 0;
-      double *drow = D + (size_t)row * ldd;
-#pragma unroll 1
+#pragma unroll
       for (int c = 0; c < FB_BN / 16; ++c) {
+        if (c + 1 < FB_BN / 16) load_chunk(c + 1, nxt);
         long long Y[16];
 #pragma unroll
         for (int u = 0; u < 16; ++u) Y[u] = 0;
-#pragma unroll 1
+#pragma unroll
         for (int l = 2; l <= FB_LMAX; ++l) {
           float v[16];
           tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((l - 2) * FB_BN + c * 16), v);
 #pragma unroll
           for (int u = 0; u < 16; ++u) {
-            const long long C = __float2ll_rn(v[u]);
+            const long long C = f2i_exact(v[u]);
             Y[u] += l < FB_LMAX ? (C << (FB_B * (FB_LMAX - 1 - l))) : ((C + 64) >> FB_B);
           }
         }
         const int col0 = n0 + c * 16;
-        if (row < rows) {
+        if (rin) {
+          if (col0 + 16 <= cols) {
+            double2 *p = reinterpret_cast<double2 *>(drow + col0);
 #pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            const int col = col0 + u;
-            if (col < cols) {
-              const double s = pow2(ea + sf[c * 16 + u] - FB_B * (FB_LMAX - 1));
-              drow[col] = fma(-(double)Y[u], s, drow[col]);
+            for (int u = 0; u < 8; ++u) {
+              double2 x = cur[u];
+              x.x -= i64_scaled(Y[2 * u], ea + sf[c * 16 + 2 * u] - FB_B * (FB_LMAX - 1));
+              x.y -= i64_scaled(Y[2 * u + 1], ea + sf[c * 16 + 2 * u + 1] - FB_B * (FB_LMAX - 1));
+              p[u] = x;
             }
+          } else {
+            for (int u = 0; u < 16; ++u)
+              if (col0 + u < cols) drow[col0 + u] -= i64_scaled(Y[u], ea + sf[c * 16 + u] - FB_B * (FB_LMAX - 1));
           }
         }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) cur[u] = nxt[u];
       }
     }
   }

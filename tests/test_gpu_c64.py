@@ -45,7 +45,8 @@ def test_c64_eval_and_tensor_core_accept_match_fp64(max_flips, cases, built_lib)
         M32, _ = h32.get_M(f)
         scale = np.abs(M64[:n, :n]).max()
         assert np.abs(M32[:n, :n] - M64[:n, :n]).max() <= 2e-7 * scale
-        np.testing.assert_allclose(M32[n:], M64[n:], rtol=0, atol=1e-14 * np.abs(M64[n:]).max())
+        # R and Eobj stay FP64; the two handles build them with different chunkings
+        np.testing.assert_allclose(M32[n:], M64[n:], rtol=0, atol=1e-11 * np.abs(M64[n:]).max())
     # DBS never flips the source tile (main.cpp:358-359): metal on the port
     # edges shorts the port (|S11| = 1), an ill-conditioned case.
     mid = (a - 1) // 2
