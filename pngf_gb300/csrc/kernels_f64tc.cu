@@ -14,19 +14,23 @@
 //    r, |r| < 2^-49, with integer a_p (|a_1| <= 128, |a_p| <= 64), exact in
 //    BF16; likewise every row of B_real with 2^-f;
 //  * products of slice pairs are exact in the tensor core and their sums over
-//    K stay integers below 2^24 (k <= 128), so the FP32 accumulation in TMEM is
+//    K stay integers below 2^22 (k <= 32), so the FP32 accumulation in TMEM is
 //    exact. Pairs with p + q = l share one accumulator per level l = 2..8 (28
 //    pairs in 7 TMEM accumulators); pairs with p + q > 8 are dropped, an error
 //    below 2^-50 of the row/column scales -- finer than FP64 GEMM rounding;
-//  * the epilogue recombines the levels exactly in 64-bit integers,
-//    Y = sum_l C_l 2^(7(7-l)), converts once and applies M -= Y 2^(e+f-49)
-//    with one FP64 fused multiply-add per element.
+//  * the epilogue recombines the levels exactly in integers,
+//    Y = sum_l C_l 2^(7(7-l)), builds Y 2^(e+f-49) as a double from its bits
+//    and subtracts it from M: one FP64 add per element.
 //
-// Kernel k_tc_update_f64: one CTA per 128-row x 64-column tile of M (as
-// doubles), the whole K extent of both operands in shared memory (TMA,
-// 128B swizzle), 28 pairs x 2k/16 tcgen05.mma.kind::f16 (M=128, N=64, K=16)
-// issued by one thread into a 512-column TMEM allocation, 4 epilogue warps.
-// Waits are bounded as in the complex64 kernel.
+// Kernel k_tc_update_f64 is persistent: one CTA per SM walks a contiguous
+// range of 128-row x 32-double-column tiles of M (row-block major). Warp 0
+// issues TMA loads (the A row-block stays in shared memory across its column
+// tiles; B tiles are double-buffered), warp 1 issues the tcgen05.mma.kind::f16
+// (M=128, N=32, K=16) chains into one of two TMEM accumulator sets (7 levels x
+// 32 columns each), and 8 epilogue warps (two warpgroups, 16 columns each)
+// drain one accumulator set while the MMAs fill the other. Every wait is
+// bounded; on timeout the kernel records an error code, drains its own TMA
+// copies, frees its TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -44,18 +48,21 @@ namespace {
 
 using namespace tc;
 
-constexpr int FB_BM = 128;   // rows of M per tile
-constexpr int FB_BN = 64;    // double columns of M per tile (MMA N)
-constexpr int FB_S = 7;      // slices per operand
-constexpr int FB_B = 7;      // bits per slice
-constexpr int FB_LMAX = 8;   // highest level kept (p + q <= 8)
+constexpr int FB_BM = 128;            // rows of M per tile (MMA M)
+constexpr int FB_BN = 32;             // double columns of M per tile (MMA N)
+constexpr int FB_S = 7;               // slices per operand
+constexpr int FB_B = 7;               // bits per slice
+constexpr int FB_LMAX = 8;            // highest level kept (p + q <= 8)
 constexpr int FB_NLEV = FB_LMAX - 1;  // levels 2..8
+constexpr int FB_ACC = FB_NLEV * FB_BN;  // TMEM columns of one accumulator set (224)
 constexpr uint32_t FB_ATOM_A = FB_BM * 128;  // one 64-element K atom of the A tile
 constexpr uint32_t FB_ATOM_B = FB_BN * 128;
-constexpr int FB_MAX_ATOMS = 7;             // K extent up to 448 (k <= 32)
-constexpr size_t FB_SMEM = FB_MAX_ATOMS * (FB_ATOM_A + FB_ATOM_B) + 1024 + 512;
+constexpr int FB_MAX_ATOMS = 7;              // K extent up to 448 (k <= 32)
+constexpr int FB_EPI_WARPS = 8;
+constexpr int FB_THREADS = 64 + 32 * FB_EPI_WARPS;
+constexpr size_t FB_SMEM = FB_MAX_ATOMS * (FB_ATOM_A + 2 * FB_ATOM_B) + 1024 + 256;
 
-// kind::f16 instruction descriptor: D f32, A and B bf16, K-major, N = 64, M = 128.
+// kind::f16 instruction descriptor: D f32, A and B bf16, K-major, N = 32, M = 128.
 constexpr uint32_t kIdescBF16 =
     (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(FB_BN >> 3) << 17) | ((uint32_t)(FB_BM >> 4) << 24);
 
@@ -77,8 +84,8 @@ __device__ __forceinline__ void write_slices(double x, int e, __nv_bfloat16 *dst
 }
 
 // A_op row i (i < rows): slices of the interleaved real row of A[i, :].
-// Row layout: slice p at columns [p*k2p, p*k2p + 2k), zeros elsewhere up to kop.
-__global__ void k_slice_A(const double2 *__restrict__ A, long lda, long rows, int k, int k2p, int kop,
+// Row pitch ld; slice p at columns [p*k2p, p*k2p + 2k), zeros elsewhere.
+__global__ void k_slice_A(const double2 *__restrict__ A, long lda, long rows, int k, int k2p, int ld,
                           __nv_bfloat16 *__restrict__ Aop, int *__restrict__ eA) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= rows) return;
@@ -89,8 +96,8 @@ __global__ void k_slice_A(const double2 *__restrict__ A, long lda, long rows, in
   }
   const int e = scale_exp(m);
   eA[i] = e;
-  __nv_bfloat16 *row = Aop + (size_t)i * kop;
-  for (int c = 0; c < kop; ++c) row[c] = __float2bfloat16_rn(0.f);
+  __nv_bfloat16 *row = Aop + (size_t)i * ld;
+  for (int c = 0; c < ld; ++c) row[c] = __float2bfloat16_rn(0.f);
   for (int r = 0; r < k; ++r) {
     const double2 a = A[(size_t)r * lda + i];
     write_slices(a.x, e, row + 2 * r, k2p);
@@ -100,7 +107,7 @@ __global__ void k_slice_A(const double2 *__restrict__ A, long lda, long rows, in
 
 // B_op row j' < 2(N+1): output column j' = 2j (real part) or 2j+1 (imaginary)
 // of M[:, j]; W is k x ldw (row-major, complex).
-__global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, int k, int k2p, int kop,
+__global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, int k, int k2p, int ld,
                           __nv_bfloat16 *__restrict__ Bop, int *__restrict__ fB) {
   const long jp = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (jp >= ncols2) return;
@@ -113,8 +120,8 @@ __global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, 
   }
   const int f = scale_exp(m);
   fB[jp] = f;
-  __nv_bfloat16 *row = Bop + (size_t)jp * kop;
-  for (int c = 0; c < kop; ++c) row[c] = __float2bfloat16_rn(0.f);
+  __nv_bfloat16 *row = Bop + (size_t)jp * ld;
+  for (int c = 0; c < ld; ++c) row[c] = __float2bfloat16_rn(0.f);
   for (int r = 0; r < k; ++r) {
     const double2 w = W[(size_t)r * ldw + j];
     // Re out: Re A Re W - Im A Im W; Im out: Re A Im W + Im A Re W
@@ -123,9 +130,10 @@ __global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, 
   }
 }
 
-// Exact int32 value of a float holding an integer of magnitude below 2^22:
-// adding 1.5 * 2^23 puts the integer in the low mantissa bits (FP32 pipe only).
-__device__ __forceinline__ int f2i_exact(float v) { return __float_as_int(v + 12582912.0f) - 0x4B400000; }
+// Exact bit pattern offset of a float holding an integer of magnitude below
+// 2^22 after adding 1.5 * 2^23 (the integer lands in the low mantissa bits).
+constexpr int kMagicBits = 0x4B400000;
+__device__ __forceinline__ int fbits(float v) { return __float_as_int(v + 12582912.0f); }
 
 // Y * 2^E as a double, built from the bits on the integer pipe (round half
 // up to 53 bits). Falls back to ldexp outside the normal exponent range.
@@ -150,53 +158,97 @@ __device__ __forceinline__ double i64_scaled(long long Y, int E) {
   return __longlong_as_double((long long)((s << 63) | ((unsigned long long)be << 52) | (mant & ((1ull << 52) - 1))));
 }
 
-// D[i, j] -= sum_c A_real[i, c] B_real[j, c] (exact to the truncation above)
-// for i < rows, j < cols; D row-major doubles, leading dimension ldd.
-__global__ void __launch_bounds__(192, 1) k_tc_update_f64(const __grid_constant__ CUtensorMap tmA,
-                                                          const __grid_constant__ CUtensorMap tmB,
-                                                          double *__restrict__ D, long ldd, int rows, int cols,
-                                                          int natoms, int k2p, const int *__restrict__ eA,
-                                                          const int *__restrict__ fB, int *err) {
+// D[i, j] -= sum_c A_real[i, c] B_real[j, c] for i < rows, j < cols; D
+// row-major doubles with leading dimension ldd. ncb = column tiles per row
+// block, ntiles = total tiles, natoms = 64-element K atoms of the operands.
+__global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_constant__ CUtensorMap tmA,
+                                                                 const __grid_constant__ CUtensorMap tmB,
+                                                                 double *__restrict__ D, long ldd, int rows, int cols,
+                                                                 int ncb, int ntiles, int natoms, int k2p,
+                                                                 const int *__restrict__ eA,
+                                                                 const int *__restrict__ fB, int *err) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                           ~static_cast<uintptr_t>(1023));
   const uint32_t sA = smem_u32(base);
-  const uint32_t sB = sA + FB_MAX_ATOMS * FB_ATOM_A;
-  uint64_t *bars = reinterpret_cast<uint64_t *>(base + FB_MAX_ATOMS * (FB_ATOM_A + FB_ATOM_B));
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
-  int *sf = reinterpret_cast<int *>(bars + 4);  // FB_BN column exponents
-  const uint32_t full = smem_u32(bars), done = full + 8;
+  const uint32_t sB0 = sA + FB_MAX_ATOMS * FB_ATOM_A;  // B buffer b at sB0 + b * FB_MAX_ATOMS * FB_ATOM_B
+  uint64_t *bars = reinterpret_cast<uint64_t *>(base + FB_MAX_ATOMS * (FB_ATOM_A + 2 * FB_ATOM_B));
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 12);
+  const uint32_t bar0 = smem_u32(bars);
+  const uint32_t a_full = bar0, a_empty = bar0 + 8;
+  auto b_full = [&](int b) { return bar0 + 16 + 8 * b; };
+  auto b_empty = [&](int b) { return bar0 + 32 + 8 * b; };
+  auto acc_full = [&](int b) { return bar0 + 48 + 8 * b; };
+  auto acc_empty = [&](int b) { return bar0 + 64 + 8 * b; };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * FB_BM, n0 = blockIdx.x * FB_BN;
+
+  // this CTA's contiguous tile range
+  const int t_begin = (int)(((long long)ntiles * blockIdx.x) / gridDim.x);
+  const int t_end = (int)(((long long)ntiles * (blockIdx.x + 1)) / gridDim.x);
 
   if (threadIdx.x == 0) {
-    mbar_init(full, 1);
-    mbar_init(done, 1);
+    mbar_init(a_full, 1);
+    mbar_init(a_empty, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(b_full(b), 1);
+      mbar_init(b_empty(b), 1);
+      mbar_init(acc_full(b), 1);
+      mbar_init(acc_empty(b), FB_EPI_WARPS);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (threadIdx.x < FB_BN) sf[threadIdx.x] = (n0 + (int)threadIdx.x < cols) ? fB[n0 + threadIdx.x] : 0;
   if (warp == 1) tmem_alloc(smem_u32(tslot), 512);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
+  const uint32_t a_bytes = (uint32_t)natoms * FB_ATOM_A, b_bytes = (uint32_t)natoms * FB_ATOM_B;
 
   if (warp == 0) {
     if (lane == 0) {
-      mbar_expect_tx(full, (uint32_t)natoms * (FB_ATOM_A + FB_ATOM_B));
-      for (int a = 0; a < natoms; ++a) {
-        tma_load_2d(sA + a * FB_ATOM_A, &tmA, a * 64, m0, full);
-        tma_load_2d(sB + a * FB_ATOM_B, &tmB, a * 64, n0, full);
+      bool ok = true;
+      int nA = 0, rb_loaded = -1, issuedB = 0;
+      for (int t = t_begin; t < t_end && ok; ++t) {
+        const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb;
+        if (rb != rb_loaded) {
+          if (nA > 0 && !mbar_wait(a_empty, (nA - 1) & 1)) { ok = false; break; }
+          mbar_expect_tx(a_full, a_bytes);
+          for (int a = 0; a < natoms; ++a) tma_load_2d(sA + a * FB_ATOM_A, &tmA, a * 64, rb * FB_BM, a_full);
+          rb_loaded = rb;
+          ++nA;
+        }
+        const int b = li & 1;
+        if (li >= 2 && !mbar_wait(b_empty(b), ((li >> 1) - 1) & 1)) { ok = false; break; }
+        const uint32_t sB = sB0 + b * FB_MAX_ATOMS * FB_ATOM_B;
+        mbar_expect_tx(b_full(b), b_bytes);
+        for (int a = 0; a < natoms; ++a) tma_load_2d(sB + a * FB_ATOM_B, &tmB, a * 64, cb * FB_BN, b_full(b));
+        ++issuedB;
       }
-      // Drain: the copies have landed before the CTA can exit.
-      if (!mbar_wait(full, 0)) atomicExch(err, 11);
+      if (!ok) atomicExch(err, 21);
+      // Drain the copies in flight before the CTA can exit.
+      if (nA > 0 && !mbar_wait(a_full, (nA - 1) & 1)) atomicExch(err, 24);
+      for (int li = issuedB > 2 ? issuedB - 2 : 0; li < issuedB; ++li)
+        if (!mbar_wait(b_full(li & 1), (li >> 1) & 1)) atomicExch(err, 24);
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      if (mbar_wait(full, 0)) {
+      bool ok = true;
+      int nA = 0, rb_have = -1;
+      for (int t = t_begin; t < t_end; ++t) {
+        const int li = t - t_begin, rb = t / ncb;
+        if (rb != rb_have) {
+          if (!mbar_wait(a_full, nA & 1)) { ok = false; break; }
+          rb_have = rb;
+          ++nA;
+        }
+        const int b = li & 1;
+        if (!mbar_wait(b_full(b), (li >> 1) & 1)) { ok = false; break; }
+        if (li >= 2 && !mbar_wait(acc_empty(b), ((li >> 1) - 1) & 1)) { ok = false; break; }
         tc_fence_after();
+        const uint32_t sB = sB0 + b * FB_MAX_ATOMS * FB_ATOM_B;
+        const uint32_t acc = tmem + (uint32_t)(b * 256);
         for (int l = 2; l <= FB_LMAX; ++l) {
-          const uint32_t dcol = tmem + (uint32_t)((l - 2) * FB_BN);
+          const uint32_t dcol = acc + (uint32_t)((l - 2) * FB_BN);
           bool first = true;
           for (int p = 1; p <= FB_S; ++p) {
             const int q = l - p;
@@ -210,70 +262,79 @@ __global__ void __launch_bounds__(192, 1) k_tc_update_f64(const __grid_constant_
             }
           }
         }
-      } else {
-        atomicExch(err, 12);
+        mma_commit(b_empty(b));
+        mma_commit(acc_full(b));
+        const bool last_of_rb = (t + 1 == t_end) || ((t + 1) / ncb != rb);
+        if (last_of_rb) mma_commit(a_empty);
       }
-      mma_commit(done);
+      if (!ok) atomicExch(err, 22);
     }
     __syncwarp();
   } else {
-    const int q = warp & 3;
-    const int row = m0 + q * 32 + lane;
-    const bool rin = row < rows;
-    const int ea = rin ? eA[row] : 0;
-    double *drow = D + (size_t)row * ldd;
-    // Chunk c of this thread's row segment: 16 doubles. Loads run one chunk
-    // ahead (the first while the MMAs run).
-    double2 cur[8], nxt[8];
-    auto load_chunk = [&](int c, double2 *dst) {
-      const int col0 = n0 + c * 16;
+    const int ew = warp - 2;          // 0..7
+    const int half = ew >> 2;         // which 16 columns of the tile
+    const int q = warp & 3;           // TMEM lanes 32q .. 32q+31
+    bool ok = true;
+    for (int t = t_begin; t < t_end; ++t) {
+      const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb;
+      const int b = li & 1;
+      const int row = rb * FB_BM + q * 32 + lane;
+      const bool rin = row < rows;
+      const int col0 = cb * FB_BN + half * 16;
+      double *drow = D + (size_t)row * ldd + col0;
+      const bool full16 = rin && col0 + 16 <= cols;
+      double2 cur[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u)
-        dst[u] = (rin && col0 + 16 <= cols) ? reinterpret_cast<const double2 *>(drow + col0)[u]
-                                            : make_double2(0.0, 0.0);
-    };
-    load_chunk(0, cur);
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
-    tc_fence_after();
-    if (!ok) {
-      if (lane == 0) atomicExch(err, 13);
-    } else {
+        cur[u] = full16 ? reinterpret_cast<const double2 *>(drow)[u] : make_double2(0.0, 0.0);
+      const int ea = rin ? eA[row] : 0;
+      ok = __all_sync(0xffffffffu, mbar_wait(acc_full(b), (li >> 1) & 1));
+      if (!ok) break;
+      tc_fence_after();
+      // Levels in pairs: P = C_l * 2^7 + C_{l+1} is an exact int32; Y = sum.
+      const uint32_t tbase = tmem + (uint32_t)(b * 256) + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 16);
+      float v0[16], v1[16];
+      long long Y[16];
+      tmem_ld16(tbase + 0 * FB_BN, v0);  // level 2
+      tmem_ld16(tbase + 1 * FB_BN, v1);  // level 3
 #pragma unroll
-      for (int c = 0; c < FB_BN / 16; ++c) {
-        if (c + 1 < FB_BN / 16) load_chunk(c + 1, nxt);
-        long long Y[16];
+      for (int u = 0; u < 16; ++u)
+        Y[u] = (long long)((fbits(v0[u]) - kMagicBits) * 128 + (fbits(v1[u]) - kMagicBits)) << 28;
+      tmem_ld16(tbase + 2 * FB_BN, v0);  // level 4
+      tmem_ld16(tbase + 3 * FB_BN, v1);  // level 5
 #pragma unroll
-        for (int u = 0; u < 16; ++u) Y[u] = 0;
+      for (int u = 0; u < 16; ++u)
+        Y[u] += (long long)((fbits(v0[u]) - kMagicBits) * 128 + (fbits(v1[u]) - kMagicBits)) << 14;
+      tmem_ld16(tbase + 4 * FB_BN, v0);  // level 6
+      tmem_ld16(tbase + 5 * FB_BN, v1);  // level 7
 #pragma unroll
-        for (int l = 2; l <= FB_LMAX; ++l) {
-          float v[16];
-          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)((l - 2) * FB_BN + c * 16), v);
+      for (int u = 0; u < 16; ++u)
+        Y[u] += (long long)((fbits(v0[u]) - kMagicBits) * 128 + (fbits(v1[u]) - kMagicBits));
+      tmem_ld16(tbase + 6 * FB_BN, v0);  // level 8, rounded to the level-7 grid
 #pragma unroll
-          for (int u = 0; u < 16; ++u) {
-            const long long C = f2i_exact(v[u]);
-            Y[u] += l < FB_LMAX ? (C << (FB_B * (FB_LMAX - 1 - l))) : ((C + 64) >> FB_B);
+      for (int u = 0; u < 16; ++u) Y[u] += (long long)((fbits(v0[u]) - kMagicBits + 64) >> 7);
+      // the accumulator set is free once every warp has read it
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acc_empty(b)) : "memory");
+      if (rin) {
+        const int E0 = ea - FB_B * (FB_LMAX - 1);
+        if (full16) {
+          double2 *p = reinterpret_cast<double2 *>(drow);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            double2 x = cur[u];
+            x.x -= i64_scaled(Y[2 * u], E0 + fB[col0 + 2 * u]);
+            x.y -= i64_scaled(Y[2 * u + 1], E0 + fB[col0 + 2 * u + 1]);
+            p[u] = x;
           }
+        } else {
+          for (int u = 0; u < 16; ++u)
+            if (col0 + u < cols) drow[u] -= i64_scaled(Y[u], E0 + fB[col0 + u]);
         }
-        const int col0 = n0 + c * 16;
-        if (rin) {
-          if (col0 + 16 <= cols) {
-            double2 *p = reinterpret_cast<double2 *>(drow + col0);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              double2 x = cur[u];
-              x.x -= i64_scaled(Y[2 * u], ea + sf[c * 16 + 2 * u] - FB_B * (FB_LMAX - 1));
-              x.y -= i64_scaled(Y[2 * u + 1], ea + sf[c * 16 + 2 * u + 1] - FB_B * (FB_LMAX - 1));
-              p[u] = x;
-            }
-          } else {
-            for (int u = 0; u < 16; ++u)
-              if (col0 + u < cols) drow[col0 + u] -= i64_scaled(Y[u], ea + sf[c * 16 + u] - FB_B * (FB_LMAX - 1));
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) cur[u] = nxt[u];
       }
     }
+    if (!ok && lane == 0) atomicExch(err, 23);
   }
   tc_fence_before();
   __syncthreads();
@@ -306,6 +367,8 @@ cudaError_t make_map_bf16(CUtensorMap *m, const void *base, long rows, int K, lo
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+int g_num_sms = 0;
+
 }  // namespace
 
 int f64tc_max_k() { return 32; }
@@ -332,10 +395,19 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
   if ((e = cudaFuncSetAttribute(k_tc_update_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FB_SMEM)) !=
       cudaSuccess)
     return e;
-  dim3 g((unsigned)((cols + FB_BN - 1) / FB_BN), (unsigned)((rows + FB_BM - 1) / FB_BM));
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 1;
+  }
+  const int nrb = (int)((rows + FB_BM - 1) / FB_BM), ncb = (int)((cols + FB_BN - 1) / FB_BN);
+  const int ntiles = nrb * ncb;
+  const int grid = ntiles < g_num_sms ? ntiles : g_num_sms;
   cudaEvent_t t0 = timing_mark(h);
-  k_tc_update_f64<<<g, 192, FB_SMEM, h->stream>>>(ma, mb, reinterpret_cast<double *>(M), 2 * h->ldm, (int)rows,
-                                                  (int)cols, natoms, k2p, h->d_eA, h->d_fB, h->d_tc_err);
+  k_tc_update_f64<<<grid, FB_THREADS, FB_SMEM, h->stream>>>(ma, mb, reinterpret_cast<double *>(M), 2 * h->ldm,
+                                                            (int)rows, (int)cols, ncb, ntiles, natoms, k2p, h->d_eA,
+                                                            h->d_fB, h->d_tc_err);
   const double cells = (double)rows * (double)(n + 1);
   timing_close(h, t0, T_UPDATE, 8.0 * k * cells, 2.0 * 16.0 * cells + 2.0 * kop * ((double)rows + (double)cols),
                0.0);
