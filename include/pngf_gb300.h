@@ -186,9 +186,11 @@ int pngf_accept(pngf_handle *h, int cand);
 int pngf_accept_edges_noalloc(double *M, long ldm, long n, int num_eobj, const double *Einc, const int *s,
                               const signed char *d, int k, int *status, void *stream);
 
-/* Largest relative deviation of the maintained M from one rebuilt from G in
- * FP64 on `ncols` sampled columns (drift check for PNGF_PREC_C64). */
-int pngf_drift_check(pngf_handle *h, int ncols, double *max_rel);
+/* Drift check of a PNGF_PREC_C64 handle: on `nrows` (1..8) sampled rows of T
+ * at every frequency, the exact FP64 rows for the current design are formed
+ * from G by iterative refinement (X <- X - (X C - H) C^-1 with
+ * C^-1 = I - P T, two sweeps) and *max_rel = max |T_c64 - T| / max |T|. */
+int pngf_drift_check(pngf_handle *h, int nrows, double *max_rel);
 /* Rebuilds M from G for the current design (drift refresh). */
 int pngf_refresh(pngf_handle *h);
 
@@ -234,6 +236,8 @@ typedef struct pngf_dbs_params {
   int run_index;
   long max_evals; /* stop after this many evaluations; 0 = run to convergence */
   int batch;      /* speculative candidates per launch (0 = whole remaining hat) */
+  int drift_every;   /* PNGF_PREC_C64: drift check every this many accepts (0 = never) */
+  double drift_tol;  /* ... and rebuild M from G in FP64 when the drift exceeds this */
 } pngf_dbs_params;
 
 typedef struct pngf_dbs pngf_dbs;
@@ -244,6 +248,9 @@ typedef struct pngf_dbs_stats {
   long launched;       /* candidates evaluated on the GPU, speculative included */
   int converged;       /* hat ran out with no improving flip */
   double F_init, F_best;
+  long drift_checks;   /* drift checks run */
+  long refreshes;      /* rebuilds of M from G after a drift check */
+  double drift_max;    /* largest drift seen, max |T_c64 - T| / max |T| */
 } pngf_dbs_stats;
 
 /* Draws the initial design (rand_binary per tile, main.cpp:187-208), forces

@@ -414,7 +414,7 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
         cudaMemset(h->d_tc_err, 0, sizeof(int)) != cudaSuccess)
       return fail(PNGF_ERR_CUDA);
   }
-  if (!c64 && c.fp64_update != PNGF_F64_SIMT) {  // FP64 updates on the tensor cores
+  if (c.fp64_update != PNGF_F64_SIMT) {  // FP64 updates (and the FP64 build of M) on the tensor cores
     h->f64tc = true;
     h->init_chunk = f64tc_max_k();
     h->a16_rows = (rows + 127) / 128 * 128;
@@ -699,12 +699,56 @@ int pngf_accept(pngf_handle *ph, int cand) {
   return accept_cand(h, cand, h->last_k[cand]);
 }
 
-int pngf_drift_check(pngf_handle *ph, int ncols, double *max_rel) {
+int pngf_drift_check(pngf_handle *ph, int nrows, double *max_rel) {
   Handle *h = H(ph);
-  if (!h) return PNGF_ERR_ARG;
-  (void)ncols;
-  (void)max_rel;
-  return set_error(h, PNGF_ERR_UNSUPPORTED, "drift check applies to PNGF_PREC_C64 handles");
+  if (!h || !max_rel) return PNGF_ERR_ARG;
+  if (h->cfg.precision != PNGF_PREC_C64)
+    return set_error(h, PNGF_ERR_UNSUPPORTED, "drift check applies to PNGF_PREC_C64 handles");
+  if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
+  if (nrows < 1 || nrows > 8) return set_error(h, PNGF_ERR_ARG, "drift check samples 1 to 8 rows");
+  const long n = h->n;
+  std::vector<int> on, rows(nrows);
+  for (long e = 0; e < n; ++e)
+    if (h->P[e]) on.push_back((int)e);
+  for (int r = 0; r < nrows; ++r) rows[r] = (int)(((2 * r + 1) * n) / (2 * nrows));
+  double2 *X = nullptr, *PH = nullptr, *Rk = nullptr;
+  int *d_rows = nullptr;
+  unsigned long long *d_out = nullptr;
+  int rc;
+  auto release = [&]() {
+    dfree(X);
+    dfree(PH);
+    dfree(Rk);
+    dfree(d_rows);
+    dfree(d_out);
+  };
+  if ((rc = dalloc(h, &X, (size_t)nrows * n)) || (rc = dalloc(h, &PH, (size_t)nrows * n)) ||
+      (rc = dalloc(h, &Rk, (size_t)nrows * n)) || (rc = dalloc(h, &d_rows, (size_t)nrows)) ||
+      (rc = dalloc(h, &d_out, 2 * (size_t)h->cfg.num_freq))) {
+    release();
+    return rc;
+  }
+  double worst = 0.0;
+  cudaError_t e = cudaMemcpyAsync(d_rows, rows.data(), sizeof(int) * nrows, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess && !on.empty())
+    e = cudaMemcpyAsync(h->d_acc_s, on.data(), sizeof(int) * on.size(), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, sizeof(unsigned long long) * 2 * h->cfg.num_freq, h->stream);
+  for (int f = 0; f < h->cfg.num_freq && e == cudaSuccess; ++f)
+    e = launch_drift_rows(h, f, d_rows, nrows, h->d_acc_s, (int)on.size(), X, PH, Rk, d_out + 2 * f);
+  std::vector<unsigned long long> out(2 * h->cfg.num_freq);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out.data(), d_out, sizeof(unsigned long long) * out.size(), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  release();
+  if (e != cudaSuccess) return cuda_check(h, e, "drift check");
+  for (int f = 0; f < h->cfg.num_freq; ++f) {
+    double dmax, xmax;
+    std::memcpy(&dmax, &out[2 * f], sizeof(double));
+    std::memcpy(&xmax, &out[2 * f + 1], sizeof(double));
+    if (xmax > 0) worst = std::max(worst, dmax / xmax);
+  }
+  *max_rel = worst;
+  return PNGF_OK;
 }
 
 int pngf_refresh(pngf_handle *ph) { return pngf_prepare(ph); }

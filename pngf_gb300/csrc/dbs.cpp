@@ -75,6 +75,8 @@ struct pngf_dbs {
   double F_init = 0.0, F_best = 0.0;
   std::vector<double> perf0;
   long evals = 0, accepts = 0, launched = 0;
+  long drift_checks = 0, refreshes = 0;
+  double drift_max = 0.0;
   std::vector<int> init_map;
   // log
   std::vector<int> lg_tile, lg_acc;
@@ -257,6 +259,18 @@ int pngf_dbs_step(pngf_dbs *d, int *accepted) {
       }
       d->hat.reset();
       if (accepted) *accepted = 1;
+      // Complex64 state: periodic FP64 drift check, rebuild from G when it drifted.
+      if (h->cfg.precision == PNGF_PREC_C64 && d->p.drift_every > 0 && d->accepts % d->p.drift_every == 0) {
+        double rel = 0.0;
+        pngf_handle *ph = reinterpret_cast<pngf_handle *>(h);
+        if ((rc = pngf_drift_check(ph, 4, &rel))) return rc;
+        ++d->drift_checks;
+        d->drift_max = std::max(d->drift_max, rel);
+        if (d->p.drift_tol > 0 && rel > d->p.drift_tol) {
+          if ((rc = pngf_refresh(ph)) || (rc = pngf_objective(ph, &d->F_best))) return rc;
+          ++d->refreshes;
+        }
+      }
       return PNGF_OK;
     }
     if (exhausted) {
@@ -275,6 +289,9 @@ int pngf_dbs_stats_get(const pngf_dbs *d, pngf_dbs_stats *out) {
   out->converged = d->converged ? 1 : 0;
   out->F_init = d->F_init;
   out->F_best = d->F_best;
+  out->drift_checks = d->drift_checks;
+  out->refreshes = d->refreshes;
+  out->drift_max = d->drift_max;
   return PNGF_OK;
 }
 

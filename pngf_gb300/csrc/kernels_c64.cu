@@ -293,6 +293,124 @@ __global__ void k_merge_M(const float2 *__restrict__ T32, const double2 *__restr
   M[(size_t)i * ldm + j] = v;
 }
 
+// ---------------------------------------------------------------------------
+// FP64 drift check of the complex64 T on sampled rows.
+//
+// The exact rows satisfy X C = H_rows with C = I + P H, H = G - I. Starting
+// from X = T32[rows], iterative refinement X <- X - (X C - H_rows) C^-1 uses
+// the identity C^-1 = I - P T with the complex64 T as the approximate
+// inverse; each sweep gains the digits complex64 has (two sweeps reach FP64).
+
+constexpr int DR_MAX_ROWS = 8;
+
+// out[r][j] = sum_{l in P} X[r][P_l] H[P_l][j], one warp per column j (lanes
+// walk P, so the reads of column j of G are contiguous).
+__global__ void k_rows_PH(const double2 *__restrict__ X, int nr, long n, const int *__restrict__ Pidx, int np,
+                          const double2 *__restrict__ G, double2 *__restrict__ out) {
+  const long j = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (j >= n) return;
+  double2 acc[DR_MAX_ROWS];
+#pragma unroll
+  for (int r = 0; r < DR_MAX_ROWS; ++r) acc[r] = make_double2(0.0, 0.0);
+  for (int q = lane; q < np; q += 32) {
+    const int l = Pidx[q];
+    double2 hv = G[(size_t)j * n + l];
+    if (l == j) hv.x -= 1.0;
+#pragma unroll
+    for (int r = 0; r < DR_MAX_ROWS; ++r)
+      if (r < nr) {
+        const double2 x = X[(size_t)r * n + l];
+        acc[r].x += x.x * hv.x - x.y * hv.y;
+        acc[r].y += x.x * hv.y + x.y * hv.x;
+      }
+  }
+#pragma unroll
+  for (int r = 0; r < DR_MAX_ROWS; ++r) {
+    for (int o = 16; o; o >>= 1) {
+      acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, o);
+      acc[r].y += __shfl_xor_sync(0xffffffffu, acc[r].y, o);
+    }
+    if (lane == 0 && r < nr) out[(size_t)r * n + j] = acc[r];
+  }
+}
+
+// Rk[r][j] = X[r][j] + PH[r][j] - H[rows_r][j].
+__global__ void k_rows_residual(const double2 *__restrict__ X, const double2 *__restrict__ PH,
+                                const double2 *__restrict__ G, const int *__restrict__ rows, int nr, long n,
+                                double2 *__restrict__ Rk) {
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  for (int r = 0; r < nr; ++r) {
+    const long i = rows[r];
+    double2 h = G[(size_t)j * n + i];
+    if (i == j) h.x -= 1.0;
+    const double2 x = X[(size_t)r * n + j], p = PH[(size_t)r * n + j];
+    Rk[(size_t)r * n + j] = make_double2(x.x + p.x - h.x, x.y + p.y - h.y);
+  }
+}
+
+// X[r][j] -= Rk[r][j] - sum_{l in P} Rk[r][P_l] T[P_l][j] (thread per column).
+__global__ void k_rows_refine(double2 *__restrict__ X, const double2 *__restrict__ Rk, int nr, long n,
+                              const int *__restrict__ Pidx, int np, const float2 *__restrict__ T32, long ldm) {
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  double2 acc[DR_MAX_ROWS];
+#pragma unroll
+  for (int r = 0; r < DR_MAX_ROWS; ++r) acc[r] = make_double2(0.0, 0.0);
+  for (int q = 0; q < np; ++q) {
+    const int l = Pidx[q];
+    const float2 tf = T32[(size_t)l * ldm + j];
+    const double2 t = make_double2(tf.x, tf.y);
+#pragma unroll
+    for (int r = 0; r < DR_MAX_ROWS; ++r)
+      if (r < nr) {
+        const double2 rv = Rk[(size_t)r * n + l];
+        acc[r].x += rv.x * t.x - rv.y * t.y;
+        acc[r].y += rv.x * t.y + rv.y * t.x;
+      }
+  }
+  for (int r = 0; r < nr; ++r) {
+    const double2 rv = Rk[(size_t)r * n + j];
+    double2 &x = X[(size_t)r * n + j];
+    x.x -= rv.x - acc[r].x;
+    x.y -= rv.y - acc[r].y;
+  }
+}
+
+__global__ void k_rows_load(const float2 *__restrict__ T32, long ldm, const int *__restrict__ rows, int nr, long n,
+                            double2 *__restrict__ X) {
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  for (int r = 0; r < nr; ++r) {
+    const float2 t = T32[(size_t)rows[r] * ldm + j];
+    X[(size_t)r * n + j] = make_double2(t.x, t.y);
+  }
+}
+
+// out[0] = max |T32[rows] - X|, out[1] = max |X| (non-negative doubles: their
+// bit patterns order like unsigned integers).
+__global__ void k_rows_compare(const float2 *__restrict__ T32, long ldm, const int *__restrict__ rows, int nr, long n,
+                               const double2 *__restrict__ X, unsigned long long *out) {
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  double dmax = 0.0, xmax = 0.0;
+  if (j < n)
+    for (int r = 0; r < nr; ++r) {
+      const float2 t = T32[(size_t)rows[r] * ldm + j];
+      const double2 x = X[(size_t)r * n + j];
+      dmax = fmax(dmax, hypot(t.x - x.x, t.y - x.y));
+      xmax = fmax(xmax, hypot(x.x, x.y));
+    }
+  for (int o = 16; o; o >>= 1) {
+    dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
+    xmax = fmax(xmax, __shfl_xor_sync(0xffffffffu, xmax, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(out, (unsigned long long)__double_as_longlong(dmax));
+    atomicMax(out + 1, (unsigned long long)__double_as_longlong(xmax));
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 std::once_flag g_encode_once;
 
@@ -328,6 +446,23 @@ cudaError_t launch_split_M(Handle *h, int f) {
   dim3 g((unsigned)((h->ldm + 255) / 256), (unsigned)(h->n + h->E));
   k_split_M<<<g, 256, 0, h->stream>>>(q.M64, h->n, h->E, h->ldm, q.T32, q.y64, q.R64);
   h->nlaunch += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_drift_rows(Handle *h, int f, const int *d_rows, int nr, const int *d_P, int np, double2 *X,
+                              double2 *PH, double2 *Rk, unsigned long long *d_out) {
+  Freq &q = h->f[f];
+  const long n = h->n;
+  if (nr < 1 || nr > DR_MAX_ROWS) return cudaErrorInvalidValue;
+  const unsigned g1 = (unsigned)((n + 255) / 256), gw = (unsigned)((n * 32 + 255) / 256);
+  k_rows_load<<<g1, 256, 0, h->stream>>>(q.T32, h->ldm, d_rows, nr, n, X);
+  for (int it = 0; it < 2; ++it) {
+    k_rows_PH<<<gw, 256, 0, h->stream>>>(X, nr, n, d_P, np, q.G, PH);
+    k_rows_residual<<<g1, 256, 0, h->stream>>>(X, PH, q.G, d_rows, nr, n, Rk);
+    k_rows_refine<<<g1, 256, 0, h->stream>>>(X, Rk, nr, n, d_P, np, q.T32, h->ldm);
+  }
+  k_rows_compare<<<g1, 256, 0, h->stream>>>(q.T32, h->ldm, d_rows, nr, n, X, d_out);
+  h->nlaunch += 8;
   return cudaGetLastError();
 }
 

@@ -275,6 +275,20 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
     const int half = ew >> 2;         // which 16 columns of the tile
     const int q = warp & 3;           // TMEM lanes 32q .. 32q+31
     bool ok = true;
+    // D and the column exponents of a tile are fetched one tile ahead.
+    double2 cur[8], nxt[8];
+    int cf[16], nf_[16];
+    auto fetch = [&](int t, double2 *dv, int *fv) {
+      const int rb = t / ncb, cb = t - rb * ncb;
+      const int row = rb * FB_BM + q * 32 + lane, col0 = cb * FB_BN + half * 16;
+      const bool full16 = row < rows && col0 + 16 <= cols;
+      const double2 *src = reinterpret_cast<const double2 *>(D + (size_t)row * ldd + col0);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) dv[u] = full16 ? src[u] : make_double2(0.0, 0.0);
+#pragma unroll
+      for (int u = 0; u < 16; ++u) fv[u] = col0 + u < cols ? fB[col0 + u] : 0;
+    };
+    if (t_begin < t_end) fetch(t_begin, cur, cf);
     for (int t = t_begin; t < t_end; ++t) {
       const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb;
       const int b = li & 1;
@@ -283,10 +297,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
       const int col0 = cb * FB_BN + half * 16;
       double *drow = D + (size_t)row * ldd + col0;
       const bool full16 = rin && col0 + 16 <= cols;
-      double2 cur[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-        cur[u] = full16 ? reinterpret_cast<const double2 *>(drow)[u] : make_double2(0.0, 0.0);
+      if (t + 1 < t_end) fetch(t + 1, nxt, nf_);
       const int ea = rin ? eA[row] : 0;
       ok = __all_sync(0xffffffffu, mbar_wait(acc_full(b), (li >> 1) & 1));
       if (!ok) break;
@@ -324,15 +335,19 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             double2 x = cur[u];
-            x.x -= i64_scaled(Y[2 * u], E0 + fB[col0 + 2 * u]);
-            x.y -= i64_scaled(Y[2 * u + 1], E0 + fB[col0 + 2 * u + 1]);
+            x.x -= i64_scaled(Y[2 * u], E0 + cf[2 * u]);
+            x.y -= i64_scaled(Y[2 * u + 1], E0 + cf[2 * u + 1]);
             p[u] = x;
           }
         } else {
           for (int u = 0; u < 16; ++u)
-            if (col0 + u < cols) drow[u] -= i64_scaled(Y[u], E0 + fB[col0 + u]);
+            if (col0 + u < cols) drow[u] -= i64_scaled(Y[u], E0 + cf[u]);
         }
       }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) cur[u] = nxt[u];
+#pragma unroll
+      for (int u = 0; u < 16; ++u) cf[u] = nf_[u];
     }
     if (!ok && lane == 0) atomicExch(err, 23);
   }

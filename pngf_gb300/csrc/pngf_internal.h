@@ -169,6 +169,11 @@ cudaError_t launch_split_M(Handle *h, int f);
 cudaError_t launch_c64_update(Handle *h, int f, int k);
 // Reassembles frequency f's M in FP64 (into M64) from T32, y64, R64.
 cudaError_t launch_merge_M(Handle *h, int f);
+// FP64 rows of T for the current design at rows d_rows (nr <= 8) by iterative
+// refinement from T32 against G; d_out[0..1] receive (as double bits, atomic
+// max) max |T32 - T| and max |T| over those rows. d_P: the set edges (np).
+cudaError_t launch_drift_rows(Handle *h, int f, const int *d_rows, int nr, const int *d_P, int np, double2 *X,
+                              double2 *PH, double2 *Rk, unsigned long long *d_out);
 // ---- FP64-accurate update on the tensor cores (kernels_f64tc.cu) ----
 int f64tc_max_k();
 size_t f64tc_op_cols();

@@ -42,12 +42,13 @@ class Config(C.Structure):
 
 class DbsParams(C.Structure):
     _fields_ = [("mode", C.c_int), ("init", C.c_int), ("seed", C.c_int), ("run_index", C.c_int),
-                ("max_evals", C.c_long), ("batch", C.c_int)]
+                ("max_evals", C.c_long), ("batch", C.c_int), ("drift_every", C.c_int), ("drift_tol", C.c_double)]
 
 
 class DbsStats(C.Structure):
     _fields_ = [("evals", C.c_long), ("accepts", C.c_long), ("launched", C.c_long), ("converged", C.c_int),
-                ("F_init", C.c_double), ("F_best", C.c_double)]
+                ("F_init", C.c_double), ("F_best", C.c_double), ("drift_checks", C.c_long),
+                ("refreshes", C.c_long), ("drift_max", C.c_double)]
 
 
 class Timing(C.Structure):
@@ -266,15 +267,20 @@ class Handle:
     def accept(self, c):
         self._chk(self.L.pngf_accept(self.h, c), "pngf_accept")
 
+    def drift_check(self, nrows=4):
+        r = C.c_double()
+        self._chk(self.L.pngf_drift_check(self.h, nrows, C.byref(r)), "pngf_drift_check")
+        return r.value
+
 
 class Dbs:
     """The native DBS driver over a prepared-able handle (G loaded)."""
 
     def __init__(self, handle: Handle, mode=DBS_SYMMETRIC, init=INIT_RANDOM, seed=1, max_evals=0, batch=0,
-                 run_index=0):
+                 run_index=0, drift_every=0, drift_tol=0.0):
         self.hd = handle
         self.max_evals = max_evals
-        p = DbsParams(mode, init, seed, run_index, max_evals, batch)
+        p = DbsParams(mode, init, seed, run_index, max_evals, batch, drift_every, drift_tol)
         d = C.c_void_p()
         handle._chk(handle.L.pngf_dbs_begin(handle.h, C.byref(p), C.byref(d)), "pngf_dbs_begin")
         self.d = d

@@ -75,6 +75,35 @@ def test_c64_eval_and_tensor_core_accept_match_fp64(max_flips, cases, built_lib)
         np.testing.assert_allclose(F32, F64, rtol=1e-6)  # accepted 4-tile flips carry ~1e-7 of c64 rounding
 
 
+def test_drift_check_measures_complex64_error(cases, built_lib):
+    """The drift check's FP64 rows (refined from G) reproduce the FP64 state's
+    rows, so the reported drift equals the true complex64 error on them."""
+    c = cases["sym_9x9_f2_seed3"]
+    Gs, gobj = case_G(c, built_lib)
+    a = c["tiles"]
+    rng = np.random.default_rng(4)
+    tm = [int(v) for v in rng.integers(0, 2, a * a)]
+    h64, h32 = handles(c, Gs, gobj, tm, 1)
+    n = h64.n
+    mid = (a - 1) // 2
+    pool = [t for t in range(a * a) if t != mid * a + mid]
+    for step in range(3):
+        cands = [[int(t)] for t in rng.choice(pool, size=8, replace=False)]
+        h64.eval_candidates(cands)
+        h32.eval_candidates(cands)
+        h64.accept(step)
+        h32.accept(step)
+    rows = [((2 * r + 1) * n) // 8 for r in range(4)]
+    true = 0.0
+    for f in range(len(Gs)):
+        T64 = h64.get_M(f)[0][rows, :n]
+        T32 = h32.get_M(f)[0][rows, :n]
+        true = max(true, np.abs(T32 - T64).max() / np.abs(T64).max())
+    drift = h32.drift_check(4)
+    assert 1e-9 < drift < 1e-5
+    assert abs(drift - true) <= 0.05 * true + 1e-12
+
+
 def test_c64_dbs_reaches_fp64_objective(cases, built_lib):
     from pngf_gb300 import lib
     c = cases["single_11x11_f3_seed2"]
@@ -84,7 +113,10 @@ def test_c64_dbs_reaches_fp64_objective(cases, built_lib):
         h = lib.Handle(11, 11, c["freqs"], precision=prec, max_flips=1)
         for f, G in enumerate(Gs):
             h.load_G(f, G, gobj[f])
-        d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=c["seed"], max_evals=600)
+        d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=c["seed"], max_evals=600,
+                    drift_every=16, drift_tol=1e-4)
         res[prec] = d.run()
     F64, F32 = res[lib.PREC_FP64].F_best, res[lib.PREC_C64].F_best
     assert abs(F32 - F64) <= 1e-3 * abs(F64)
+    s32 = res[lib.PREC_C64]
+    assert s32.drift_checks >= 1 and 0 < s32.drift_max < 1e-4
