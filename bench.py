@@ -255,6 +255,78 @@ def run_form(a, precision, Gs, rank, local, dist):
     return out
 
 
+def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_steps=600, topk=64):
+    """Wall time to the converged objective: plain FP64 DBS (reference order,
+    run until the hat is empty) against the proposal + complex64 form, whose
+    network is trained only on plain complex64 runs from other seeds. The
+    proposal run stops once its objective is within 1e-3 relative of the plain
+    run's final objective (or at its own convergence)."""
+    import torch
+    from pngf_gb300 import lib
+    out = {}
+    nfl = 1
+    h = lib.Handle(a.tiles, a.tiles, FREQS, precision=lib.PREC_FP64, max_flips=nfl, device=local)
+    for f, G in enumerate(Gs):
+        h.load_G(f, G, None)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0)
+    s = d.run()
+    torch.cuda.synchronize()
+    out["plain_fp64"] = {"wall_s": time.perf_counter() - t0, "F_final": s.F_best, "F_init": s.F_init,
+                         "evals": s.evals, "accepts": s.accepts, "converged": bool(s.converged)}
+    F_target = s.F_best * (1.0 + 1e-3)
+    d.close()
+    h.close()
+    torch.cuda.empty_cache()
+    h = lib.Handle(a.tiles, a.tiles, FREQS, precision=lib.PREC_C64, max_flips=nfl, device=local)
+    for f, G in enumerate(Gs):
+        h.load_G(f, G, None)
+    prop = lib.Proposal(h, channels=32, seed=1)
+    t0 = time.perf_counter()
+    for sd in train_seeds:  # training pairs from plain complex64 runs of other designs
+        d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=sd, max_evals=train_evals)
+        lib.dbs_set_proposal(d, prop, topk=0)
+        d.run()
+        d.close()
+    t_collect = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = prop.train(train_steps, batch=32, lr=2e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    samples = prop.num_samples()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0, drift_every=32, drift_tol=1e-4)
+    lib.dbs_set_proposal(d, prop, topk=topk, train_every=8, train_steps=20, train_batch=32, lr=1e-3)
+    t_reach = None
+    while True:
+        d.step()
+        s = d.stats()
+        if t_reach is None and s.F_best <= F_target:
+            torch.cuda.synchronize()
+            t_reach = time.perf_counter() - t0
+            break
+        if s.converged:
+            break
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    out["proposal_c64"] = {"wall_s_to_target": t_reach, "wall_s": wall, "F_final": s.F_best, "evals": s.evals,
+                           "accepts": s.accepts, "prop_hits": s.prop_hits, "full_passes": s.full_passes,
+                           "converged": bool(s.converged), "drift_max": s.drift_max,
+                           "reached_target": t_reach is not None,
+                           "training": {"seeds": list(train_seeds), "collect_s": t_collect, "train_s": t_train,
+                                        "samples": samples, "final_loss": loss, "steps": train_steps}}
+    out["F_target"] = F_target
+    if t_reach:
+        out["speedup_wall_to_objective"] = out["plain_fp64"]["wall_s"] / t_reach
+    d.close()
+    prop.close()
+    h.close()
+    torch.cuda.empty_cache()
+    return out
+
+
 def reduce_form(r, dist):
     """Whole-job figures: sums of work over ranks, max of times over ranks."""
     import torch

@@ -251,6 +251,8 @@ typedef struct pngf_dbs_stats {
   long drift_checks;   /* drift checks run */
   long refreshes;      /* rebuilds of M from G after a drift check */
   double drift_max;    /* largest drift seen, max |T_c64 - T| / max |T| */
+  long prop_hits;      /* proposal steps whose top-k batch held an improving flip */
+  long full_passes;    /* proposal steps that fell back to a full exact pass */
 } pngf_dbs_stats;
 
 /* Draws the initial design (rand_binary per tile, main.cpp:187-208), forces
@@ -270,6 +272,44 @@ int pngf_dbs_log(const pngf_dbs *d, long cap, int *tile, int *accept, double *F,
 /* Writes the log in Logger::save's text format (logger.hpp:75-106). */
 int pngf_dbs_save_log(const pngf_dbs *d, const char *path);
 int pngf_dbs_end(pngf_dbs *d);
+
+/* ---- learned proposals (no reference counterpart) ----
+ * A 4-layer 3x3 convolutional network over the tile map (3 input channels:
+ * tile state, per-tile Woodbury sensitivity log mean |T_ee|, last exact gain;
+ * C channels; BF16 weights, FP32 accumulation; hand-written forward, backward
+ * and Adam kernels) predicts each single-tile flip's objective change. The
+ * DBS driver uses it to order exact evaluations; every proposal is evaluated
+ * exactly, and a full exact pass is the fallback. */
+typedef struct pngf_prop pngf_prop;
+
+int pngf_prop_create(pngf_handle *h, int channels, unsigned long long seed, pngf_prop **out);
+int pngf_prop_destroy(pngf_prop *p);
+long pngf_prop_num_params(const pngf_prop *p);
+/* FP32 master parameters, layer by layer: weights (C_out x C_in x 3 x 3) then biases. */
+int pngf_prop_get_params(const pngf_prop *p, float *params);
+int pngf_prop_set_params(pngf_prop *p, const float *params);
+/* Features (3 x tiles_y x tiles_x) of the handle's current design. */
+int pngf_prop_features(pngf_prop *p, float *feat);
+/* Records exact objective changes of single-tile flips at the current design
+ * as one training sample (non-finite gains are skipped). */
+int pngf_prop_record(pngf_prop *p, const int *tiles, const double *gains, int count);
+long pngf_prop_num_samples(const pngf_prop *p);
+/* Adam on random minibatches of recorded samples (masked mean squared error). */
+int pngf_prop_train(pngf_prop *p, int steps, int batch, float lr, float *loss);
+/* Predicted change (in gain-scale units) per tile; non-candidate tiles +inf. */
+int pngf_prop_predict(pngf_prop *p, float *pred);
+/* Forward + backward on given inputs (B x 3 x H x W), targets and masks
+ * (B x H x W): output, mean masked squared error and parameter gradients. */
+int pngf_prop_forward_backward(pngf_prop *p, const float *x, int B, const float *target, const float *mask,
+                               float *out, float *grad, float *loss);
+const char *pngf_prop_last_error(const pngf_prop *p);
+/* Attaches a network to a single-tile DBS run. topk = 0: plain DBS that
+ * records every exact evaluation as training data. topk > 0: each step
+ * evaluates the top-k predicted flips exactly and accepts the best improving
+ * one, else runs a full exact pass; every train_every steps, train_steps Adam
+ * steps (batch train_batch, learning rate lr) on the recorded samples. */
+int pngf_dbs_set_proposal(pngf_dbs *d, pngf_prop *p, int topk, int train_every, int train_steps, int train_batch,
+                          float lr);
 
 #ifdef __cplusplus
 }

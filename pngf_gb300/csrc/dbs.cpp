@@ -81,7 +81,19 @@ struct pngf_dbs {
   // log
   std::vector<int> lg_tile, lg_acc;
   std::vector<double> lg_F, lg_Fb, lg_perf;
+  // learned proposals (optional)
+  pngf_prop *prop = nullptr;
+  int topk = 0, train_every = 0, train_steps = 0, train_batch = 32;
+  float train_lr = 1e-3f;
+  long prop_steps = 0, prop_hits = 0, full_passes = 0;
 };
+
+extern "C" {
+int pngf_prop_record(pngf_prop *p, const int *tiles, const double *gains, int count);
+int pngf_prop_predict(pngf_prop *p, float *pred);
+int pngf_prop_train(pngf_prop *p, int steps, int batch, float lr, float *loss);
+long pngf_prop_num_samples(const pngf_prop *p);
+}
 
 namespace {
 
@@ -136,9 +148,97 @@ void log_row(pngf_dbs *d, const Cand &c, int acc, double F, const double *perf, 
   d->lg_perf.insert(d->lg_perf.end(), perf, perf + 3 * nf);
 }
 
+// Proposal-driven decision (no reference counterpart): the network's top-k
+// single-tile flips are evaluated exactly and the best improving one is
+// accepted; if none improves, a full exact pass over every candidate tile
+// follows, and if that finds nothing either the design is a local minimum.
+int proposal_step(pngf_dbs *d, int *accepted) {
+  pngf::Handle *h = d->h;
+  const int map_sz = h->map_sz, nf = h->cfg.num_freq, mf = h->cfg.max_flips;
+  const int xsz = h->cfg.tiles_x;
+  std::vector<int> elig;
+  for (int t = 0; t < map_sz; ++t) {
+    const int ty = t / xsz, tx = t - ty * xsz;
+    if (ty == d->mid_y && (tx == d->mid_x || tx == d->mid_x - 1 || tx == d->mid_x + 1)) continue;
+    elig.push_back(t);
+  }
+  // Evaluates `list` exactly, records the gains, logs the rows and returns the
+  // index (into list) of the best improving flip, or -1.
+  auto run_batch = [&](const std::vector<int> &list, pngf::EvalOut &o, int *best) -> int {
+    const int n = (int)list.size();
+    std::vector<int> tiles((size_t)n * mf, 0), nflip(n, 1);
+    for (int i = 0; i < n; ++i) tiles[(size_t)i * mf] = list[i];
+    int rc = pngf::eval_batch(h, tiles.data(), nflip.data(), n, d->F_best, &o);
+    if (rc) return rc;
+    d->launched += n;
+    d->evals += n;
+    std::vector<double> gains(n);
+    for (int i = 0; i < n; ++i) gains[i] = o.F[i] - d->F_best;
+    if ((rc = pngf_prop_record(d->prop, list.data(), gains.data(), n))) return rc;
+    *best = -1;
+    for (int i = 0; i < n; ++i)
+      if (o.F[i] < d->F_best && (*best < 0 || o.F[i] < o.F[*best])) *best = i;
+    for (int i = 0; i < n; ++i) {
+      Cand c{list[i], 1, {list[i], 0, 0, 0}};
+      log_row(d, c, i == *best, o.F[i], o.perf.data() + (size_t)i * nf * 3, nf);
+    }
+    return PNGF_OK;
+  };
+  auto take = [&](const std::vector<int> &list, pngf::EvalOut &o, int best) -> int {
+    int rc = pngf::accept_cand(h, best, o.k[best]);
+    if (rc) return rc;
+    d->F_best = o.F[best];
+    ++d->accepts;
+    if (accepted) *accepted = 1;
+    (void)list;
+    return PNGF_OK;
+  };
+  int rc;
+  ++d->prop_steps;
+  if (d->train_every > 0 && d->prop_steps % d->train_every == 0 && pngf_prop_num_samples(d->prop) > 0) {
+    float loss = 0.f;
+    if ((rc = pngf_prop_train(d->prop, d->train_steps, d->train_batch, d->train_lr, &loss))) return rc;
+  }
+  pngf::EvalOut o;
+  int best = -1;
+  if (pngf_prop_num_samples(d->prop) > 0) {
+    std::vector<float> pred(map_sz);
+    if ((rc = pngf_prop_predict(d->prop, pred.data()))) return rc;
+    std::vector<int> order(elig);
+    const int k = std::min<int>(d->topk, (int)order.size());
+    std::partial_sort(order.begin(), order.begin() + k, order.end(),
+                      [&](int a, int b) { return pred[a] < pred[b]; });
+    order.resize(k);
+    if ((rc = run_batch(order, o, &best))) return rc;
+    if (best >= 0) {
+      ++d->prop_hits;
+      return take(order, o, best);
+    }
+  }
+  ++d->full_passes;
+  if ((rc = run_batch(elig, o, &best))) return rc;
+  if (best >= 0) return take(elig, o, best);
+  d->converged = d->done = true;
+  return PNGF_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int pngf_dbs_set_proposal(pngf_dbs *d, pngf_prop *p, int topk, int train_every, int train_steps, int train_batch,
+                          float lr) {
+  if (!d) return PNGF_ERR_ARG;
+  if (p && d->p.mode != PNGF_DBS_SINGLE)
+    return pngf::set_error(d->h, PNGF_ERR_UNSUPPORTED, "proposals apply to single-tile candidates");
+  d->prop = p;
+  d->topk = topk;
+  d->train_every = train_every;
+  d->train_steps = train_steps;
+  d->train_batch = train_batch > 0 ? train_batch : 32;
+  d->train_lr = lr > 0 ? lr : 1e-3f;
+  return PNGF_OK;
+}
 
 int pngf_dbs_begin(pngf_handle *ph, const pngf_dbs_params *p, pngf_dbs **out) {
   pngf::Handle *h = reinterpret_cast<pngf::Handle *>(ph);
@@ -201,6 +301,7 @@ int pngf_dbs_step(pngf_dbs *d, int *accepted) {
   if (accepted) *accepted = 0;
   pngf::Handle *h = d->h;
   const int nf = h->cfg.num_freq, mf = h->cfg.max_flips;
+  if (d->prop && d->topk > 0) return d->done ? PNGF_OK : proposal_step(d, accepted);
   while (!d->done) {
     long budget = d->p.max_evals > 0 ? d->p.max_evals - d->evals : std::numeric_limits<long>::max();
     if (budget <= 0) {
@@ -237,6 +338,15 @@ int pngf_dbs_step(pngf_dbs *d, int *accepted) {
     int rc = pngf::eval_batch(h, tiles.data(), nflip.data(), nc, d->F_best, &o);
     if (rc) return rc;
     d->launched += nc;
+    if (d->prop && d->p.mode == PNGF_DBS_SINGLE) {  // every exact evaluation is a training pair
+      std::vector<int> tl(nc);
+      std::vector<double> gains(nc);
+      for (int i = 0; i < nc; ++i) {
+        tl[i] = cands[i].tiles[0];
+        gains[i] = o.F[i] - d->F_best;
+      }
+      if ((rc = pngf_prop_record(d->prop, tl.data(), gains.data(), nc))) return rc;
+    }
     const int j = o.first;
     const int upto = j >= 0 ? j : nc - 1;
     for (int i = 0; i <= upto; ++i) {
@@ -292,6 +402,8 @@ int pngf_dbs_stats_get(const pngf_dbs *d, pngf_dbs_stats *out) {
   out->drift_checks = d->drift_checks;
   out->refreshes = d->refreshes;
   out->drift_max = d->drift_max;
+  out->prop_hits = d->prop_hits;
+  out->full_passes = d->full_passes;
   return PNGF_OK;
 }
 

@@ -27,7 +27,7 @@
 // issues TMA loads (the A row-block stays in shared memory across its column
 // tiles; B tiles are double-buffered), warp 1 issues the tcgen05.mma.kind::f16
 // (M=128, N=32, K=16) chains into one of two TMEM accumulator sets (7 levels x
-// 32 columns each), and 8 epilogue warps (two warpgroups, 16 columns each)
+// 32 columns each), and 16 epilogue warps (four warpgroups, 8 columns each)
 // drain one accumulator set while the MMAs fill the other. Every wait is
 // bounded; on timeout the kernel records an error code, drains its own TMA
 // copies, frees its TMEM and returns.
@@ -58,7 +58,7 @@ constexpr int FB_ACC = FB_NLEV * FB_BN;  // TMEM columns of one accumulator set 
 constexpr uint32_t FB_ATOM_A = FB_BM * 128;  // one 64-element K atom of the A tile
 constexpr uint32_t FB_ATOM_B = FB_BN * 128;
 constexpr int FB_MAX_ATOMS = 7;              // K extent up to 448 (k <= 32)
-constexpr int FB_EPI_WARPS = 8;
+constexpr int FB_EPI_WARPS = 16;
 constexpr int FB_THREADS = 64 + 32 * FB_EPI_WARPS;
 constexpr size_t FB_SMEM = FB_MAX_ATOMS * (FB_ATOM_A + 2 * FB_ATOM_B) + 1024 + 256;
 
@@ -271,83 +271,71 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
     }
     __syncwarp();
   } else {
-    const int ew = warp - 2;          // 0..7
-    const int half = ew >> 2;         // which 16 columns of the tile
+    const int ew = warp - 2;          // 0..15
+    const int part = ew >> 2;         // which 8 columns of the tile
     const int q = warp & 3;           // TMEM lanes 32q .. 32q+31
     bool ok = true;
-    // D and the column exponents of a tile are fetched one tile ahead.
-    double2 cur[8], nxt[8];
-    int cf[16], nf_[16];
-    auto fetch = [&](int t, double2 *dv, int *fv) {
+    // D of a tile is fetched one tile ahead.
+    double2 cur[4], nxt[4];
+    auto fetch = [&](int t, double2 *dv) {
       const int rb = t / ncb, cb = t - rb * ncb;
-      const int row = rb * FB_BM + q * 32 + lane, col0 = cb * FB_BN + half * 16;
-      const bool full16 = row < rows && col0 + 16 <= cols;
+      const int row = rb * FB_BM + q * 32 + lane, col0 = cb * FB_BN + part * 8;
+      const bool full8 = row < rows && col0 + 8 <= cols;
       const double2 *src = reinterpret_cast<const double2 *>(D + (size_t)row * ldd + col0);
 #pragma unroll
-      for (int u = 0; u < 8; ++u) dv[u] = full16 ? src[u] : make_double2(0.0, 0.0);
-#pragma unroll
-      for (int u = 0; u < 16; ++u) fv[u] = col0 + u < cols ? fB[col0 + u] : 0;
+      for (int u = 0; u < 4; ++u) dv[u] = full8 ? src[u] : make_double2(0.0, 0.0);
     };
-    if (t_begin < t_end) fetch(t_begin, cur, cf);
+    if (t_begin < t_end) fetch(t_begin, cur);
     for (int t = t_begin; t < t_end; ++t) {
       const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb;
       const int b = li & 1;
       const int row = rb * FB_BM + q * 32 + lane;
       const bool rin = row < rows;
-      const int col0 = cb * FB_BN + half * 16;
+      const int col0 = cb * FB_BN + part * 8;
       double *drow = D + (size_t)row * ldd + col0;
-      const bool full16 = rin && col0 + 16 <= cols;
-      if (t + 1 < t_end) fetch(t + 1, nxt, nf_);
+      const bool full8 = rin && col0 + 8 <= cols;
+      if (t + 1 < t_end) fetch(t + 1, nxt);
       const int ea = rin ? eA[row] : 0;
       ok = __all_sync(0xffffffffu, mbar_wait(acc_full(b), (li >> 1) & 1));
       if (!ok) break;
       tc_fence_after();
-      // Levels in pairs: P = C_l * 2^7 + C_{l+1} is an exact int32; Y = sum.
-      const uint32_t tbase = tmem + (uint32_t)(b * 256) + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 16);
-      float v0[16], v1[16];
-      long long Y[16];
-      tmem_ld16(tbase + 0 * FB_BN, v0);  // level 2
-      tmem_ld16(tbase + 1 * FB_BN, v1);  // level 3
+      // All seven level loads in flight at once, one wait.
+      const uint32_t tbase = tmem + (uint32_t)(b * 256) + ((uint32_t)(q * 32) << 16) + (uint32_t)(part * 8);
+      uint32_t v[FB_NLEV][8];
 #pragma unroll
-      for (int u = 0; u < 16; ++u)
-        Y[u] = (long long)((fbits(v0[u]) - kMagicBits) * 128 + (fbits(v1[u]) - kMagicBits)) << 28;
-      tmem_ld16(tbase + 2 * FB_BN, v0);  // level 4
-      tmem_ld16(tbase + 3 * FB_BN, v1);  // level 5
-#pragma unroll
-      for (int u = 0; u < 16; ++u)
-        Y[u] += (long long)((fbits(v0[u]) - kMagicBits) * 128 + (fbits(v1[u]) - kMagicBits)) << 14;
-      tmem_ld16(tbase + 4 * FB_BN, v0);  // level 6
-      tmem_ld16(tbase + 5 * FB_BN, v1);  // level 7
-#pragma unroll
-      for (int u = 0; u < 16; ++u)
-        Y[u] += (long long)((fbits(v0[u]) - kMagicBits) * 128 + (fbits(v1[u]) - kMagicBits));
-      tmem_ld16(tbase + 6 * FB_BN, v0);  // level 8, rounded to the level-7 grid
-#pragma unroll
-      for (int u = 0; u < 16; ++u) Y[u] += (long long)((fbits(v0[u]) - kMagicBits + 64) >> 7);
+      for (int l = 0; l < FB_NLEV; ++l) tmem_ld8_nowait(tbase + (uint32_t)(l * FB_BN), v[l]);
+      tmem_wait_ld();
       // the accumulator set is free once every warp has read it
       tc_fence_before();
       __syncwarp();
       if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acc_empty(b)) : "memory");
+      // Levels in pairs: P = C_l * 2^7 + C_{l+1} is an exact int32;
+      // Y = P23 2^28 + P45 2^14 + P67 + round(C8 / 2^7).
+      long long Y[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        auto C = [&](int l) { return fbits(__uint_as_float(v[l][u])) - kMagicBits; };
+        Y[u] = ((long long)(C(0) * 128 + C(1)) << 28) + ((long long)(C(2) * 128 + C(3)) << 14) +
+               (long long)(C(4) * 128 + C(5)) + (long long)((C(6) + 64) >> 7);
+      }
       if (rin) {
         const int E0 = ea - FB_B * (FB_LMAX - 1);
-        if (full16) {
+        if (full8) {
           double2 *p = reinterpret_cast<double2 *>(drow);
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
+          for (int u = 0; u < 4; ++u) {
             double2 x = cur[u];
-            x.x -= i64_scaled(Y[2 * u], E0 + cf[2 * u]);
-            x.y -= i64_scaled(Y[2 * u + 1], E0 + cf[2 * u + 1]);
+            x.x -= i64_scaled(Y[2 * u], E0 + fB[col0 + 2 * u]);
+            x.y -= i64_scaled(Y[2 * u + 1], E0 + fB[col0 + 2 * u + 1]);
             p[u] = x;
           }
         } else {
-          for (int u = 0; u < 16; ++u)
-            if (col0 + u < cols) drow[u] -= i64_scaled(Y[u], E0 + cf[u]);
+          for (int u = 0; u < 8; ++u)
+            if (col0 + u < cols) drow[u] -= i64_scaled(Y[u], E0 + fB[col0 + u]);
         }
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) cur[u] = nxt[u];
-#pragma unroll
-      for (int u = 0; u < 16; ++u) cf[u] = nf_[u];
+      for (int u = 0; u < 4; ++u) cur[u] = nxt[u];
     }
     if (!ok && lane == 0) atomicExch(err, 23);
   }

@@ -1,0 +1,584 @@
+// Learned flip proposals: a small convolutional network over the tile map.
+//
+// No reference counterpart. The network ranks single-tile flips by predicted
+// objective change so that the exact Woodbury evaluation runs on the most
+// promising tiles first; every proposal is still evaluated exactly, and a full
+// exact pass is the fallback, so the network only reorders work.
+//
+// Input (3 channels on the tiles_y x tiles_x grid):
+//   0  tile state, +-1;
+//   1  Woodbury sensitivity: log of the mean |T_ee| over the tile's edges
+//      (frequency 0), standardized over the map;
+//   2  the tile's last exact gain (F after flip - F at that time), divided by
+//      the running gain scale and clipped to [-4, 4], 0 if never evaluated.
+// Network: 4 layers of 3x3 convolutions (zero padding), 3 -> C -> C -> C -> 1
+// with ReLU between; weights stored in BF16 (FP32 master copy for Adam),
+// activations and accumulation in FP32. Output: predicted gain / gain scale.
+//
+// Kernels are plain SIMT: the whole network is ~20k parameters and ~70 MFLOP
+// per 41x41 map, far too small to be worth tensor-core tiles.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "pngf_internal.h"
+
+namespace pngf {
+namespace {
+
+constexpr int NL = 4;
+
+__global__ void k_conv_fwd(const float *__restrict__ x, const __nv_bfloat16 *__restrict__ w,
+                           const float *__restrict__ bias, float *__restrict__ z, float *__restrict__ a, int Cin,
+                           int Cout, int H, int W, int relu) {
+  extern __shared__ float sw[];  // Cin * 9 weights of this output channel
+  const int co = blockIdx.y, b = blockIdx.z;
+  for (int i = threadIdx.x; i < Cin * 9; i += blockDim.x) sw[i] = __bfloat162float(w[(size_t)co * Cin * 9 + i]);
+  __syncthreads();
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= H * W) return;
+  const int py = p / W, px = p - py * W;
+  float acc = bias[co];
+  const float *xb = x + (size_t)b * Cin * H * W;
+  for (int ci = 0; ci < Cin; ++ci) {
+    const float *xc = xb + (size_t)ci * H * W;
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky) {
+      const int yy = py + ky - 1;
+      if (yy < 0 || yy >= H) continue;
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        const int xx = px + kx - 1;
+        if (xx < 0 || xx >= W) continue;
+        acc = fmaf(xc[yy * W + xx], sw[ci * 9 + ky * 3 + kx], acc);
+      }
+    }
+  }
+  const size_t o = ((size_t)b * Cout + co) * H * W + p;
+  z[o] = acc;
+  if (a) a[o] = relu ? fmaxf(acc, 0.f) : acc;
+}
+
+// dx[b][ci][p] = sum_co sum_k dz[b][co][p - (k - 1)] w[co][ci][k]
+__global__ void k_conv_bwd_in(const float *__restrict__ dz, const __nv_bfloat16 *__restrict__ w,
+                              float *__restrict__ dx, int Cin, int Cout, int H, int W) {
+  extern __shared__ float sw[];  // Cout * 9 weights feeding input channel ci
+  const int ci = blockIdx.y, b = blockIdx.z;
+  for (int i = threadIdx.x; i < Cout * 9; i += blockDim.x) {
+    const int co = i / 9, k = i - co * 9;
+    sw[i] = __bfloat162float(w[((size_t)co * Cin + ci) * 9 + k]);
+  }
+  __syncthreads();
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= H * W) return;
+  const int py = p / W, px = p - py * W;
+  float acc = 0.f;
+  for (int co = 0; co < Cout; ++co) {
+    const float *dzc = dz + ((size_t)b * Cout + co) * H * W;
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky) {
+      const int yy = py - (ky - 1);
+      if (yy < 0 || yy >= H) continue;
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        const int xx = px - (kx - 1);
+        if (xx < 0 || xx >= W) continue;
+        acc = fmaf(dzc[yy * W + xx], sw[co * 9 + ky * 3 + kx], acc);
+      }
+    }
+  }
+  dx[((size_t)b * Cin + ci) * H * W + p] = acc;
+}
+
+// dw[co][ci][k] = sum_b sum_p dz[b][co][p] x[b][ci][p + k - 1]; db[co] from ci = 0.
+__global__ void k_conv_bwd_w(const float *__restrict__ x, const float *__restrict__ dz, float *__restrict__ dw,
+                             float *__restrict__ db, int B, int Cin, int Cout, int H, int W) {
+  const int ci = blockIdx.x, co = blockIdx.y;
+  float acc[10];
+#pragma unroll
+  for (int k = 0; k < 10; ++k) acc[k] = 0.f;
+  const int HW = H * W;
+  for (int idx = threadIdx.x; idx < B * HW; idx += blockDim.x) {
+    const int b = idx / HW, p = idx - b * HW;
+    const int py = p / W, px = p - py * W;
+    const float g = dz[((size_t)b * Cout + co) * HW + p];
+    const float *xc = x + ((size_t)b * Cin + ci) * HW;
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky) {
+      const int yy = py + ky - 1;
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        const int xx = px + kx - 1;
+        if (yy >= 0 && yy < H && xx >= 0 && xx < W) acc[ky * 3 + kx] = fmaf(g, xc[yy * W + xx], acc[ky * 3 + kx]);
+      }
+    }
+    acc[9] += g;
+  }
+  __shared__ float red[32][10];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 10; ++k) {
+    float v = acc[k];
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wid][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 10) {
+    float s = 0.f;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i][threadIdx.x];
+    if (threadIdx.x < 9) dw[((size_t)co * Cin + ci) * 9 + threadIdx.x] = s;
+    else if (ci == 0) db[co] = s;
+  }
+}
+
+__global__ void k_relu_bwd(const float *__restrict__ z, float *__restrict__ g, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && z[i] <= 0.f) g[i] = 0.f;
+}
+
+// Masked mean squared error; out[0] += loss, dout = d loss / d y.
+__global__ void k_mse(const float *__restrict__ y, const float *__restrict__ t, const float *__restrict__ m,
+                      float *__restrict__ dy, size_t n, float inv_count, float *loss) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float l = 0.f;
+  if (i < n) {
+    const float d = (y[i] - t[i]) * m[i];
+    dy[i] = 2.f * d * inv_count;
+    l = d * d * inv_count;
+  }
+  for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
+}
+
+__global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m, float *__restrict__ v,
+                       __nv_bfloat16 *__restrict__ wb, int n, float lr, float b1, float b2, float eps, float c1,
+                       float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi, vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  w[i] = wi;
+  wb[i] = __float2bfloat16_rn(wi);
+}
+
+__global__ void k_to_bf16(const float *__restrict__ w, __nv_bfloat16 *__restrict__ wb, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) wb[i] = __float2bfloat16_rn(w[i]);
+}
+
+// Channel 1 of the features: per tile, mean log |T_ee| over its edges (frequency 0).
+template <typename TM>
+__global__ void k_tile_sensitivity(const TM *__restrict__ T, long ldt, int tiles_x, int tiles_y, int cells_x,
+                                   int cells_y, int ex_xsz, int ey_xsz, long nx, float *__restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= tiles_x * tiles_y) return;
+  const int ty = t / tiles_x, tx = t - ty * tiles_x;
+  double s = 0.0;
+  int cnt = 0;
+  for (int jj = 0; jj <= cells_y; ++jj)
+    for (int ii = 0; ii < cells_x; ++ii) {
+      const long e = (long)(tx * cells_x + ii) + (long)(ty * cells_y + jj) * ex_xsz;
+      const TM v = T[(size_t)e * ldt + e];
+      s += log(hypot((double)v.x, (double)v.y) + 1e-300);
+      ++cnt;
+    }
+  for (int jj = 0; jj < cells_y; ++jj)
+    for (int ii = 0; ii <= cells_x; ++ii) {
+      const long e = nx + (long)(tx * cells_x + ii) + (long)(ty * cells_y + jj) * ey_xsz;
+      const TM v = T[(size_t)e * ldt + e];
+      s += log(hypot((double)v.x, (double)v.y) + 1e-300);
+      ++cnt;
+    }
+  out[t] = (float)(s / cnt);
+}
+
+}  // namespace
+}  // namespace pngf
+
+using namespace pngf;
+
+struct pngf_prop {
+  Handle *h = nullptr;
+  int C = 32, H = 0, W = 0, map_sz = 0;
+  int cin[NL], cout[NL];
+  size_t woff[NL], boff[NL], nparam = 0;
+  float *d_w = nullptr, *d_g = nullptr, *d_m = nullptr, *d_v = nullptr;  // fp32 params, grads, Adam moments
+  __nv_bfloat16 *d_wb = nullptr;                                         // bf16 weights used by the kernels
+  long adam_t = 0;
+  // activations for a batch of up to cap maps
+  int cap = 0;
+  float *d_x = nullptr;                     // cap x 3 x H x W
+  float *d_z[NL] = {}, *d_a[NL] = {};       // pre/post activations
+  float *d_g1 = nullptr, *d_g2 = nullptr;   // activation gradients (cap x C x H x W)
+  float *d_t = nullptr, *d_mask = nullptr;  // targets and masks (cap x H x W)
+  float *d_loss = nullptr, *d_sens = nullptr;
+  // training samples (host): features and (normalized) targets / masks
+  std::vector<float> feat, tgt, msk;
+  long samples = 0, max_samples = 4096;
+  std::vector<float> last_gain;  // per tile, raw objective change
+  double gain_scale = 0.0, gain_sq = 0.0;
+  long gain_n = 0;
+  std::mt19937 rng{1};
+  std::string err;
+};
+
+namespace {
+
+int prop_alloc_batch(pngf_prop *p, int B) {
+  if (B <= p->cap) return PNGF_OK;
+  auto fr = [](float *&q) {
+    if (q) cudaFree(q);
+    q = nullptr;
+  };
+  fr(p->d_x);
+  for (int l = 0; l < NL; ++l) {
+    fr(p->d_z[l]);
+    fr(p->d_a[l]);
+  }
+  fr(p->d_g1);
+  fr(p->d_g2);
+  fr(p->d_t);
+  fr(p->d_mask);
+  const size_t HW = (size_t)p->H * p->W;
+  bool ok = cudaMalloc(&p->d_x, sizeof(float) * B * 3 * HW) == cudaSuccess;
+  for (int l = 0; l < NL && ok; ++l)
+    ok = cudaMalloc(&p->d_z[l], sizeof(float) * B * p->cout[l] * HW) == cudaSuccess &&
+         cudaMalloc(&p->d_a[l], sizeof(float) * B * p->cout[l] * HW) == cudaSuccess;
+  ok = ok && cudaMalloc(&p->d_g1, sizeof(float) * B * p->C * HW) == cudaSuccess &&
+       cudaMalloc(&p->d_g2, sizeof(float) * B * p->C * HW) == cudaSuccess &&
+       cudaMalloc(&p->d_t, sizeof(float) * B * HW) == cudaSuccess &&
+       cudaMalloc(&p->d_mask, sizeof(float) * B * HW) == cudaSuccess;
+  if (!ok) return PNGF_ERR_NOMEM;
+  p->cap = B;
+  return PNGF_OK;
+}
+
+cudaError_t prop_forward(pngf_prop *p, int B) {
+  const int HW = p->H * p->W;
+  const float *in = p->d_x;
+  for (int l = 0; l < NL; ++l) {
+    dim3 g((HW + 127) / 128, p->cout[l], B);
+    k_conv_fwd<<<g, 128, sizeof(float) * p->cin[l] * 9, p->h->stream>>>(
+        in, p->d_wb + p->woff[l], p->d_w + p->boff[l], p->d_z[l], p->d_a[l], p->cin[l], p->cout[l], p->H, p->W,
+        l < NL - 1 ? 1 : 0);
+    in = p->d_a[l];
+  }
+  return cudaGetLastError();
+}
+
+// Backward from d(output) in d_g1 (B x 1 x H x W); fills d_g.
+cudaError_t prop_backward(pngf_prop *p, int B) {
+  const int HW = p->H * p->W;
+  float *gcur = p->d_g1, *gnext = p->d_g2;
+  for (int l = NL - 1; l >= 0; --l) {
+    if (l < NL - 1) {
+      const size_t n = (size_t)B * p->cout[l] * HW;
+      k_relu_bwd<<<(unsigned)((n + 255) / 256), 256, 0, p->h->stream>>>(p->d_z[l], gcur, n);
+    }
+    const float *xin = l == 0 ? p->d_x : p->d_a[l - 1];
+    k_conv_bwd_w<<<dim3(p->cin[l], p->cout[l]), 256, 0, p->h->stream>>>(xin, gcur, p->d_g + p->woff[l],
+                                                                        p->d_g + p->boff[l], B, p->cin[l],
+                                                                        p->cout[l], p->H, p->W);
+    if (l > 0) {
+      dim3 g((HW + 127) / 128, p->cin[l], B);
+      k_conv_bwd_in<<<g, 128, sizeof(float) * p->cout[l] * 9, p->h->stream>>>(gcur, p->d_wb + p->woff[l], gnext,
+                                                                               p->cin[l], p->cout[l], p->H, p->W);
+      std::swap(gcur, gnext);
+    }
+  }
+  return cudaGetLastError();
+}
+
+int prop_err(pngf_prop *p, int code, const std::string &m) {
+  p->err = m;
+  return code;
+}
+
+bool eligible(const Handle *h, int t) {
+  const int xsz = h->cfg.tiles_x, ysz = h->cfg.tiles_y;
+  const int mx = (int)((xsz - 1) * 0.5), my = (int)((ysz - 1) * 0.5);
+  const int ty = t / xsz, tx = t - ty * xsz;
+  if (ty == my && (tx == mx || tx == mx - 1 || tx == mx + 1)) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pngf_prop_create(pngf_handle *ph, int channels, unsigned long long seed, pngf_prop **out) {
+  Handle *h = reinterpret_cast<Handle *>(ph);
+  if (!h || !out || channels < 1 || channels > 128) return PNGF_ERR_ARG;
+  pngf_prop *p = new pngf_prop();
+  p->h = h;
+  p->C = channels;
+  p->H = h->cfg.tiles_y;
+  p->W = h->cfg.tiles_x;
+  p->map_sz = h->map_sz;
+  p->rng.seed((unsigned)seed);
+  const int cin[NL] = {3, channels, channels, channels}, cout[NL] = {channels, channels, channels, 1};
+  size_t off = 0;
+  for (int l = 0; l < NL; ++l) {
+    p->cin[l] = cin[l];
+    p->cout[l] = cout[l];
+    p->woff[l] = off;
+    off += (size_t)cout[l] * cin[l] * 9;
+    p->boff[l] = off;
+    off += cout[l];
+  }
+  p->nparam = off;
+  // He-normal initialisation, zero biases
+  std::vector<float> w(off, 0.f);
+  for (int l = 0; l < NL; ++l) {
+    std::normal_distribution<float> nd(0.f, std::sqrt(2.f / (cin[l] * 9)));
+    for (size_t i = 0; i < (size_t)cout[l] * cin[l] * 9; ++i) w[p->woff[l] + i] = nd(p->rng);
+  }
+  bool ok = cudaMalloc(&p->d_w, sizeof(float) * off) == cudaSuccess &&
+            cudaMalloc(&p->d_g, sizeof(float) * off) == cudaSuccess &&
+            cudaMalloc(&p->d_m, sizeof(float) * off) == cudaSuccess &&
+            cudaMalloc(&p->d_v, sizeof(float) * off) == cudaSuccess &&
+            cudaMalloc(&p->d_wb, sizeof(__nv_bfloat16) * off) == cudaSuccess &&
+            cudaMalloc(&p->d_loss, sizeof(float)) == cudaSuccess &&
+            cudaMalloc(&p->d_sens, sizeof(float) * p->map_sz) == cudaSuccess;
+  if (!ok || prop_alloc_batch(p, 64) != PNGF_OK) {
+    pngf_prop_destroy(p);
+    return PNGF_ERR_NOMEM;
+  }
+  cudaMemcpy(p->d_w, w.data(), sizeof(float) * off, cudaMemcpyHostToDevice);
+  cudaMemset(p->d_m, 0, sizeof(float) * off);
+  cudaMemset(p->d_v, 0, sizeof(float) * off);
+  k_to_bf16<<<(unsigned)((off + 255) / 256), 256>>>(p->d_w, p->d_wb, (int)off);
+  if (cudaDeviceSynchronize() != cudaSuccess) {
+    pngf_prop_destroy(p);
+    return PNGF_ERR_CUDA;
+  }
+  p->last_gain.assign(p->map_sz, 0.f);
+  *out = p;
+  return PNGF_OK;
+}
+
+int pngf_prop_destroy(pngf_prop *p) {
+  if (!p) return PNGF_OK;
+  auto fr = [](void *q) {
+    if (q) cudaFree(q);
+  };
+  fr(p->d_w);
+  fr(p->d_g);
+  fr(p->d_m);
+  fr(p->d_v);
+  fr(p->d_wb);
+  fr(p->d_loss);
+  fr(p->d_sens);
+  fr(p->d_x);
+  for (int l = 0; l < NL; ++l) {
+    fr(p->d_z[l]);
+    fr(p->d_a[l]);
+  }
+  fr(p->d_g1);
+  fr(p->d_g2);
+  fr(p->d_t);
+  fr(p->d_mask);
+  delete p;
+  return PNGF_OK;
+}
+
+long pngf_prop_num_params(const pngf_prop *p) { return p ? (long)p->nparam : 0; }
+
+int pngf_prop_get_params(const pngf_prop *p, float *w) {
+  if (!p || !w) return PNGF_ERR_ARG;
+  return cudaMemcpy(w, p->d_w, sizeof(float) * p->nparam, cudaMemcpyDeviceToHost) == cudaSuccess ? PNGF_OK
+                                                                                                 : PNGF_ERR_CUDA;
+}
+
+int pngf_prop_set_params(pngf_prop *p, const float *w) {
+  if (!p || !w) return PNGF_ERR_ARG;
+  if (cudaMemcpy(p->d_w, w, sizeof(float) * p->nparam, cudaMemcpyHostToDevice) != cudaSuccess) return PNGF_ERR_CUDA;
+  k_to_bf16<<<(unsigned)((p->nparam + 255) / 256), 256, 0, p->h->stream>>>(p->d_w, p->d_wb, (int)p->nparam);
+  return cudaStreamSynchronize(p->h->stream) == cudaSuccess ? PNGF_OK : PNGF_ERR_CUDA;
+}
+
+// Forward and backward on caller-given inputs (B x 3 x H x W), targets and
+// masks (B x H x W): output (B x H x W), loss and gradients (nparam), all host
+// memory. For gradient checks.
+int pngf_prop_forward_backward(pngf_prop *p, const float *x, int B, const float *target, const float *mask,
+                               float *out, float *grad, float *loss) {
+  if (!p || !x || B < 1) return PNGF_ERR_ARG;
+  int rc = prop_alloc_batch(p, B);
+  if (rc) return rc;
+  cudaStream_t s = p->h->stream;
+  const size_t HW = (size_t)p->H * p->W;
+  cudaMemcpyAsync(p->d_x, x, sizeof(float) * B * 3 * HW, cudaMemcpyHostToDevice, s);
+  if (prop_forward(p, B) != cudaSuccess) return PNGF_ERR_CUDA;
+  if (out) cudaMemcpyAsync(out, p->d_z[NL - 1], sizeof(float) * B * HW, cudaMemcpyDeviceToHost, s);
+  if (target && mask) {
+    cudaMemcpyAsync(p->d_t, target, sizeof(float) * B * HW, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(p->d_mask, mask, sizeof(float) * B * HW, cudaMemcpyHostToDevice, s);
+    double msum = 0.0;
+    for (size_t i = 0; i < B * HW; ++i) msum += mask[i];
+    cudaMemsetAsync(p->d_loss, 0, sizeof(float), s);
+    const size_t n = B * HW;
+    k_mse<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p->d_z[NL - 1], p->d_t, p->d_mask, p->d_g1, n,
+                                                       (float)(1.0 / std::max(1.0, msum)), p->d_loss);
+    if (prop_backward(p, B) != cudaSuccess) return PNGF_ERR_CUDA;
+    if (grad) cudaMemcpyAsync(grad, p->d_g, sizeof(float) * p->nparam, cudaMemcpyDeviceToHost, s);
+    if (loss) cudaMemcpyAsync(loss, p->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s);
+  }
+  return cudaStreamSynchronize(s) == cudaSuccess ? PNGF_OK : PNGF_ERR_CUDA;
+}
+
+// Features of the handle's current design (3 x H x W), written to the device
+// input slot `slot` and, if feat is not NULL, to host memory.
+static int prop_features(pngf_prop *p, int slot, float *feat) {
+  Handle *h = p->h;
+  if (!h->prepared) return prop_err(p, PNGF_ERR_STATE, "handle not prepared");
+  const int HW = p->map_sz;
+  if (h->cfg.precision == PNGF_PREC_FP64)
+    k_tile_sensitivity<double2><<<(HW + 127) / 128, 128, 0, h->stream>>>(
+        h->f[0].M64, h->ldm, h->cfg.tiles_x, h->cfg.tiles_y, h->cfg.cells_x, h->cfg.cells_y, h->ex_xsz, h->ey_xsz,
+        h->nx, p->d_sens);
+  else
+    k_tile_sensitivity<float2><<<(HW + 127) / 128, 128, 0, h->stream>>>(
+        h->f[0].T32, h->ldm, h->cfg.tiles_x, h->cfg.tiles_y, h->cfg.cells_x, h->cfg.cells_y, h->ex_xsz, h->ey_xsz,
+        h->nx, p->d_sens);
+  std::vector<float> sens(HW), f(3 * HW);
+  if (cudaMemcpyAsync(sens.data(), p->d_sens, sizeof(float) * HW, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return prop_err(p, PNGF_ERR_CUDA, "feature extraction");
+  double mu = 0.0, sd = 0.0;
+  for (float v : sens) mu += v;
+  mu /= HW;
+  for (float v : sens) sd += (v - mu) * (v - mu);
+  sd = std::sqrt(sd / HW) + 1e-12;
+  const double gs = p->gain_scale > 0 ? p->gain_scale : 1.0;
+  for (int t = 0; t < HW; ++t) {
+    f[t] = h->tile_map[t] ? 1.f : -1.f;
+    f[HW + t] = (float)((sens[t] - mu) / sd);
+    f[2 * HW + t] = (float)std::max(-4.0, std::min(4.0, p->last_gain[t] / gs));
+  }
+  if (feat) std::memcpy(feat, f.data(), sizeof(float) * 3 * HW);
+  if (slot >= 0 &&
+      cudaMemcpyAsync(p->d_x + (size_t)slot * 3 * HW, f.data(), sizeof(float) * 3 * HW, cudaMemcpyHostToDevice,
+                      h->stream) != cudaSuccess)
+    return prop_err(p, PNGF_ERR_CUDA, "feature upload");
+  return PNGF_OK;
+}
+
+int pngf_prop_features(pngf_prop *p, float *feat) {
+  if (!p) return PNGF_ERR_ARG;
+  return prop_features(p, -1, feat);
+}
+
+// Records exact gains (F after flip - F now) of single-tile flips at the
+// handle's current design: updates each tile's last gain and stores one
+// training sample (features, normalized gains, mask).
+int pngf_prop_record(pngf_prop *p, const int *tiles, const double *gains, int count) {
+  if (!p || (count > 0 && (!tiles || !gains))) return PNGF_ERR_ARG;
+  const int HW = p->map_sz;
+  std::vector<float> f(3 * HW);
+  int rc = prop_features(p, -1, f.data());
+  if (rc) return rc;
+  for (int i = 0; i < count; ++i) {
+    if (tiles[i] < 0 || tiles[i] >= HW) return prop_err(p, PNGF_ERR_ARG, "tile index out of range");
+    if (!std::isfinite(gains[i])) continue;  // singular capacitance: no label
+    p->gain_sq += gains[i] * gains[i];
+    ++p->gain_n;
+  }
+  if (p->gain_n > 0) p->gain_scale = std::sqrt(p->gain_sq / p->gain_n);
+  std::vector<float> t(HW, 0.f), m(HW, 0.f);
+  const double gs = p->gain_scale > 0 ? p->gain_scale : 1.0;
+  for (int i = 0; i < count; ++i) {
+    if (!std::isfinite(gains[i])) continue;
+    const int tile = tiles[i];
+    t[tile] = (float)std::max(-8.0, std::min(8.0, gains[i] / gs));
+    m[tile] = 1.f;
+  }
+  // Ring buffer of samples.
+  const long slot = p->samples % p->max_samples;
+  if ((long)p->feat.size() < (slot + 1) * 3 * HW) {
+    p->feat.resize((slot + 1) * 3 * HW);
+    p->tgt.resize((slot + 1) * HW);
+    p->msk.resize((slot + 1) * HW);
+  }
+  std::memcpy(&p->feat[slot * 3 * HW], f.data(), sizeof(float) * 3 * HW);
+  std::memcpy(&p->tgt[slot * HW], t.data(), sizeof(float) * HW);
+  std::memcpy(&p->msk[slot * HW], m.data(), sizeof(float) * HW);
+  ++p->samples;
+  for (int i = 0; i < count; ++i)
+    if (std::isfinite(gains[i])) p->last_gain[tiles[i]] = (float)gains[i];
+  return PNGF_OK;
+}
+
+long pngf_prop_num_samples(const pngf_prop *p) { return p ? std::min(p->samples, p->max_samples) : 0; }
+
+// Adam steps on random minibatches of the stored samples; *loss = mean loss.
+int pngf_prop_train(pngf_prop *p, int steps, int batch, float lr, float *loss) {
+  if (!p || steps < 0 || batch < 1) return PNGF_ERR_ARG;
+  const long have = std::min(p->samples, p->max_samples);
+  if (have == 0) return prop_err(p, PNGF_ERR_STATE, "no training samples");
+  int rc = prop_alloc_batch(p, batch);
+  if (rc) return rc;
+  cudaStream_t s = p->h->stream;
+  const int HW = p->map_sz;
+  std::vector<float> x((size_t)batch * 3 * HW), t((size_t)batch * HW), m((size_t)batch * HW);
+  double lsum = 0.0;
+  std::uniform_int_distribution<long> pick(0, have - 1);
+  for (int it = 0; it < steps; ++it) {
+    double msum = 0.0;
+    for (int b = 0; b < batch; ++b) {
+      const long i = pick(p->rng);
+      std::memcpy(&x[(size_t)b * 3 * HW], &p->feat[i * 3 * HW], sizeof(float) * 3 * HW);
+      std::memcpy(&t[(size_t)b * HW], &p->tgt[i * HW], sizeof(float) * HW);
+      std::memcpy(&m[(size_t)b * HW], &p->msk[i * HW], sizeof(float) * HW);
+      for (int q = 0; q < HW; ++q) msum += p->msk[i * HW + q];
+    }
+    cudaMemcpyAsync(p->d_x, x.data(), sizeof(float) * x.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(p->d_t, t.data(), sizeof(float) * t.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(p->d_mask, m.data(), sizeof(float) * m.size(), cudaMemcpyHostToDevice, s);
+    if (prop_forward(p, batch) != cudaSuccess) return prop_err(p, PNGF_ERR_CUDA, "forward");
+    cudaMemsetAsync(p->d_loss, 0, sizeof(float), s);
+    const size_t n = (size_t)batch * HW;
+    k_mse<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p->d_z[NL - 1], p->d_t, p->d_mask, p->d_g1, n,
+                                                       (float)(1.0 / std::max(1.0, msum)), p->d_loss);
+    if (prop_backward(p, batch) != cudaSuccess) return prop_err(p, PNGF_ERR_CUDA, "backward");
+    ++p->adam_t;
+    const float b1 = 0.9f, b2 = 0.999f;
+    k_adam<<<(unsigned)((p->nparam + 255) / 256), 256, 0, s>>>(
+        p->d_w, p->d_g, p->d_m, p->d_v, p->d_wb, (int)p->nparam, lr, b1, b2, 1e-8f,
+        1.f - std::pow(b1, (float)p->adam_t), 1.f - std::pow(b2, (float)p->adam_t));
+    float l = 0.f;
+    cudaMemcpyAsync(&l, p->d_loss, sizeof(float), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return prop_err(p, PNGF_ERR_CUDA, "training step");
+    lsum += l;
+  }
+  if (loss) *loss = steps > 0 ? (float)(lsum / steps) : 0.f;
+  return PNGF_OK;
+}
+
+// Predicted gain (in units of the gain scale) of flipping each tile of the
+// handle's current design; tiles that are never candidates get +inf.
+int pngf_prop_predict(pngf_prop *p, float *pred) {
+  if (!p || !pred) return PNGF_ERR_ARG;
+  int rc = prop_features(p, 0, nullptr);
+  if (rc) return rc;
+  if (prop_forward(p, 1) != cudaSuccess) return prop_err(p, PNGF_ERR_CUDA, "forward");
+  if (cudaMemcpyAsync(pred, p->d_z[NL - 1], sizeof(float) * p->map_sz, cudaMemcpyDeviceToHost, p->h->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(p->h->stream) != cudaSuccess)
+    return prop_err(p, PNGF_ERR_CUDA, "prediction");
+  for (int t = 0; t < p->map_sz; ++t)
+    if (!eligible(p->h, t)) pred[t] = INFINITY;
+  return PNGF_OK;
+}
+
+const char *pngf_prop_last_error(const pngf_prop *p) { return p ? p->err.c_str() : "null"; }
+
+}  // extern "C"

@@ -48,7 +48,8 @@ class DbsParams(C.Structure):
 class DbsStats(C.Structure):
     _fields_ = [("evals", C.c_long), ("accepts", C.c_long), ("launched", C.c_long), ("converged", C.c_int),
                 ("F_init", C.c_double), ("F_best", C.c_double), ("drift_checks", C.c_long),
-                ("refreshes", C.c_long), ("drift_max", C.c_double)]
+                ("refreshes", C.c_long), ("drift_max", C.c_double), ("prop_hits", C.c_long),
+                ("full_passes", C.c_long)]
 
 
 class Timing(C.Structure):
@@ -108,6 +109,19 @@ def load():
         "pngf_dbs_log": (I, [P, L_, P, P, P, P, P, P]),
         "pngf_dbs_save_log": (I, [P, C.c_char_p]),
         "pngf_dbs_end": (I, [P]),
+        "pngf_prop_create": (I, [P, I, C.c_ulonglong, P]),
+        "pngf_prop_destroy": (I, [P]),
+        "pngf_prop_num_params": (L_, [P]),
+        "pngf_prop_get_params": (I, [P, P]),
+        "pngf_prop_set_params": (I, [P, P]),
+        "pngf_prop_features": (I, [P, P]),
+        "pngf_prop_record": (I, [P, P, P, I]),
+        "pngf_prop_num_samples": (L_, [P]),
+        "pngf_prop_train": (I, [P, I, I, C.c_float, P]),
+        "pngf_prop_predict": (I, [P, P]),
+        "pngf_prop_forward_backward": (I, [P, P, I, P, P, P, P, P]),
+        "pngf_prop_last_error": (C.c_char_p, [P]),
+        "pngf_dbs_set_proposal": (I, [P, P, I, I, I, I, C.c_float]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -329,3 +343,85 @@ class Dbs:
             self.close()
         except Exception:
             pass
+
+
+class Proposal:
+    """The learned flip-proposal network attached to a handle."""
+
+    def __init__(self, handle: Handle, channels=32, seed=1):
+        self.hd = handle
+        self.L = handle.L
+        p = C.c_void_p()
+        rc = self.L.pngf_prop_create(handle.h, channels, seed, C.byref(p))
+        if rc:
+            raise PngfError(rc, "pngf_prop_create")
+        self.p = p
+        self.H = handle.cfg.tiles_y
+        self.W = handle.cfg.tiles_x
+
+    def _chk(self, rc, what):
+        if rc:
+            raise PngfError(rc, "%s: %s" % (what, self.L.pngf_prop_last_error(self.p).decode()))
+
+    def num_params(self):
+        return self.L.pngf_prop_num_params(self.p)
+
+    def params(self):
+        w = np.zeros(self.num_params(), dtype=np.float32)
+        self._chk(self.L.pngf_prop_get_params(self.p, _ptr(w)), "get_params")
+        return w
+
+    def set_params(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._chk(self.L.pngf_prop_set_params(self.p, _ptr(w)), "set_params")
+
+    def features(self):
+        f = np.zeros((3, self.H, self.W), dtype=np.float32)
+        self._chk(self.L.pngf_prop_features(self.p, _ptr(f)), "features")
+        return f
+
+    def record(self, tiles, gains):
+        t = np.ascontiguousarray(tiles, dtype=np.int32)
+        g = np.ascontiguousarray(gains, dtype=np.float64)
+        self._chk(self.L.pngf_prop_record(self.p, _ptr(t), _ptr(g), len(t)), "record")
+
+    def num_samples(self):
+        return self.L.pngf_prop_num_samples(self.p)
+
+    def train(self, steps, batch=32, lr=1e-3):
+        loss = C.c_float()
+        self._chk(self.L.pngf_prop_train(self.p, steps, batch, lr, C.byref(loss)), "train")
+        return loss.value
+
+    def predict(self):
+        out = np.zeros(self.H * self.W, dtype=np.float32)
+        self._chk(self.L.pngf_prop_predict(self.p, _ptr(out)), "predict")
+        return out
+
+    def forward_backward(self, x, target=None, mask=None):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        B = x.shape[0]
+        out = np.zeros((B, self.H, self.W), dtype=np.float32)
+        grad = np.zeros(self.num_params(), dtype=np.float32)
+        loss = np.zeros(1, dtype=np.float32)
+        t = None if target is None else np.ascontiguousarray(target, dtype=np.float32)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.float32)
+        self._chk(self.L.pngf_prop_forward_backward(self.p, _ptr(x), B, _ptr(t), _ptr(m), _ptr(out), _ptr(grad),
+                                                    _ptr(loss)), "forward_backward")
+        return out, grad, float(loss[0])
+
+    def close(self):
+        if getattr(self, "p", None):
+            self.L.pngf_prop_destroy(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def dbs_set_proposal(dbs: Dbs, prop, topk=64, train_every=0, train_steps=0, train_batch=32, lr=1e-3):
+    dbs.hd._chk(dbs.hd.L.pngf_dbs_set_proposal(dbs.d, prop.p if prop else None, topk, train_every, train_steps,
+                                              train_batch, lr), "pngf_dbs_set_proposal")
