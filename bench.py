@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", default="fp64,c64", help="precision forms to run; the first is the headline")
     ap.add_argument("--nfreq", type=int, default=5, help="use the first NFREQ of the five frequencies")
+    ap.add_argument("--converge", action="store_true",
+                    help="also time plain FP64 DBS to convergence against proposal + complex64 DBS")
     return ap.parse_args()
 
 
@@ -360,6 +362,7 @@ def gpu_arm(a, world, rank, local):
     if "c64" in forms:
         r32 = run_form(a, lib.PREC_C64, Gs, rank, local, dist)
         c64_red = reduce_form(r32, dist)
+    conv = converge_compare(a, Gs, local) if (a.converge and rank == 0) else None
     del Gs
     if rank != 0:
         if dist:
@@ -459,6 +462,8 @@ def gpu_arm(a, world, rank, local):
             },
             "clocks": r32["clocks"], "gpu_launches": t32["kernel_launches"], "setup_s": r32["setup_s"],
         }
+    if conv is not None:
+        line["converge"] = conv
     if world == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(a.tiles, a.mode, a.seed, FREQS[0], r64["evals"],
                                                    r64["accepts"], nf)
