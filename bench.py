@@ -329,13 +329,14 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
     return out
 
 
-def reduce_form(r, dist):
-    """Whole-job figures: sums of work over ranks, max of times over ranks."""
+def reduce_form(r, dist, device="cuda"):
+    """Whole-job figures: sums of work over ranks, max of times over ranks
+    (each rank runs its own DBS instance; the job ends with the slowest)."""
     import torch
-    vec = torch.tensor([r["wall"], r["dev_s"], r["evals"], r["accepts"], r["launched"]], dtype=torch.float64,
-                       device="cuda")
     if not dist:
         return r["wall"], r["dev_s"], r["evals"], r["accepts"], r["launched"]
+    vec = torch.tensor([r["wall"], r["dev_s"], r["evals"], r["accepts"], r["launched"]], dtype=torch.float64,
+                       device=device)
     mx, sm = vec.clone(), vec.clone()
     dist.all_reduce(mx, op=dist.ReduceOp.MAX)
     dist.all_reduce(sm, op=dist.ReduceOp.SUM)

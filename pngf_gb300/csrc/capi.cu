@@ -181,7 +181,7 @@ static int eval_resident(Handle *h, int ncand, double F_best) {
   return PNGF_OK;
 }
 
-int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best, EvalOut *out) {
+int eval_launch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best) {
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "pngf_prepare has not been called for this design");
   if (ncand <= 0) return set_error(h, PNGF_ERR_ARG, "ncand must be positive");
   int rc;
@@ -197,10 +197,10 @@ int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double 
   if ((rc = eval_resident(h, ncand, F_best))) return rc;
   h->batch_tiles.assign(tiles, tiles + (size_t)ncand * mf);
   h->batch_nflip.assign(nflip, nflip + ncand);
-  if (!out) return PNGF_OK;
-  // One pinned block: F, perf, new_eobj (as doubles), then ints first, ek, status.
+  // One pinned block: F, perf, new_eobj (as doubles), then ints: first, ek,
+  // status, and the tensor-core error flag (set by an earlier accept).
   const size_t nF = ncand, nperf = (size_t)ncand * nf * 3, neo = (size_t)ncand * nf * h->E * 2;
-  const size_t nint = 1 + (size_t)ncand + (size_t)ncand * nf;
+  const size_t nint = 2 + (size_t)ncand + (size_t)ncand * nf;
   if ((rc = ensure_host_out(h, nF + nperf + neo + nint))) return rc;
   double *hF = h->h_out, *hperf = hF + nF, *heo = hperf + nperf;
   int *hint = reinterpret_cast<int *>(heo + neo);
@@ -211,7 +211,30 @@ int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double 
   PNGF_CUDA(h, cudaMemcpyAsync(hint + 1, h->d_ek, sizeof(int) * ncand, cudaMemcpyDeviceToHost, h->stream));
   PNGF_CUDA(h, cudaMemcpyAsync(hint + 1 + ncand, h->d_status, sizeof(int) * ncand * nf, cudaMemcpyDeviceToHost,
                                h->stream));
+  hint[1 + ncand + (size_t)ncand * nf] = 0;
+  if (h->d_tc_err)
+    PNGF_CUDA(h, cudaMemcpyAsync(hint + 1 + ncand + (size_t)ncand * nf, h->d_tc_err, sizeof(int),
+                                 cudaMemcpyDeviceToHost, h->stream));
+  h->launched_n = ncand;
+  return PNGF_OK;
+}
+
+int eval_collect(Handle *h, EvalOut *out) {
+  const int ncand = h->launched_n, mf = h->cfg.max_flips, nf = h->cfg.num_freq;
+  if (ncand <= 0) return set_error(h, PNGF_ERR_STATE, "no batch in flight");
+  h->launched_n = 0;
+  const size_t nF = ncand, nperf = (size_t)ncand * nf * 3, neo = (size_t)ncand * nf * h->E * 2;
+  const size_t nint = 2 + (size_t)ncand + (size_t)ncand * nf;
+  double *hF = h->h_out, *hperf = hF + nF, *heo = hperf + nperf;
+  int *hint = reinterpret_cast<int *>(heo + neo);
   PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  const int tc = hint[1 + ncand + (size_t)ncand * nf];
+  if (tc != 0) {
+    cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->stream);
+    h->batch_valid = false;
+    return set_error(h, PNGF_ERR_TIMEOUT, "tensor-core update gave up waiting (code " + std::to_string(tc) + ")");
+  }
+  if (!out) return PNGF_OK;
   out->F.assign(hF, hF + nF);
   out->perf.assign(hperf, hperf + nperf);
   out->new_eobj.assign(heo, heo + neo);
@@ -231,7 +254,15 @@ int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double 
   return PNGF_OK;
 }
 
-int accept_cand(Handle *h, int c, int k) {
+int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best, EvalOut *out) {
+  int rc = eval_launch(h, tiles, nflip, ncand, F_best);
+  if (rc) return rc;
+  return eval_collect(h, out);
+}
+
+int accept_cand(Handle *h, int c, int k) { return accept_cand_async(h, c, k, true); }
+
+int accept_cand_async(Handle *h, int c, int k, bool check_now) {
   if (!h->batch_valid) return set_error(h, PNGF_ERR_STATE, "no evaluated batch to accept from");
   if (c < 0 || c >= h->batch_n) return set_error(h, PNGF_ERR_ARG, "candidate index outside the last batch");
   if (k < 0 || k > h->kmax) return set_error(h, PNGF_ERR_ARG, "invalid flipped-edge count");
@@ -243,7 +274,7 @@ int accept_cand(Handle *h, int c, int k) {
     timing_close(h, t0, T_ACCEPT, 0.0, 0.0, 0.0);
   }
   PNGF_CUDA(h, launch_commit(h, c));
-  if (h->d_tc_err) {  // the tensor-core kernels' bounded waits report here
+  if (h->d_tc_err && check_now) {  // the tensor-core kernels' bounded waits report here (else at the next collect)
     int tc = 0;
     PNGF_CUDA(h, cudaMemcpyAsync(&tc, h->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     PNGF_CUDA(h, cudaStreamSynchronize(h->stream));

@@ -84,6 +84,7 @@ struct Handle {
   int *d_first = nullptr;
   int *d_status = nullptr;                      // per-candidate LU status
   int batch_n = 0;
+  int launched_n = 0;      // batch enqueued by eval_launch, not yet collected
   bool batch_valid = false;
   std::vector<int> batch_tiles, batch_nflip;
   std::vector<int> last_k, last_status;   // per-candidate edge count / status of the host-API batch
@@ -141,8 +142,15 @@ struct EvalOut {
 };
 // Evaluates a batch of host tile lists (validated) and reads the results back.
 int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best, EvalOut *out);
+// The same in two phases: enqueue the batch and its result copies on the
+// handle's stream, then wait for them and parse.
+int eval_launch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best);
+int eval_collect(Handle *h, EvalOut *out);
 // Applies candidate c (k flipped edges) of the last batch at every frequency.
 int accept_cand(Handle *h, int c, int k);
+// Same; with check_now = false nothing waits for the GPU (the tensor-core
+// error flag is then reported by the next eval_collect).
+int accept_cand_async(Handle *h, int c, int k, bool check_now);
 
 // ---- kernels (kernels_fp64.cu) ----
 // Builds M for P = 0 from G and the objective rows; computes Einc and the
