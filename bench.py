@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import re
 import os
 import statistics
 import subprocess
@@ -48,7 +49,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 FREQS = [27.0e9, 28.5e9, 30.0e9, 31.5e9, 33.0e9]
-PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "rank_update_fp64_21x21.json")
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "tc_update_f64_21x21.md")
 
 
 def parse():
@@ -227,6 +228,7 @@ def run_form(a, precision, Gs, rank, local, dist):
         h.load_G(f, G, None)
     d = lib.Dbs(h, mode=lib.DBS_SINGLE if a.mode == "single" else lib.DBS_SYMMETRIC, init=lib.INIT_RANDOM,
                 seed=a.seed + rank, batch=0)
+    tune = h.autotune()  # kernel forms for this instance; the state is left unchanged
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t_setup
     for _ in range(a.warmup):
@@ -250,11 +252,22 @@ def run_form(a, precision, Gs, rank, local, dist):
     s1 = d.stats()
     out = dict(evals=s1.evals - s0.evals, accepts=s1.accepts - s0.accepts, launched=s1.launched - s0.launched,
                wall=wall, dev_s=(tm["eval_ms"] + tm["accept_ms"]) * 1e-3, tm=tm, clocks=clocks, setup_s=setup_s,
-               F_init=s1.F_init, F_best=s1.F_best, n=h.n, ldm=h.ldm)
+               F_init=s1.F_init, F_best=s1.F_best, n=h.n, ldm=h.ldm, tune=tune)
     d.close()
     h.close()
     torch.cuda.empty_cache()
     return out
+
+
+def autotune_on(h, mode_single=True):
+    """Autotunes a handle's kernel forms on a throwaway random design (seed
+    99), outside any timed region; the forms stay with the handle."""
+    from pngf_gb300 import lib
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE if mode_single else lib.DBS_SYMMETRIC, init=lib.INIT_RANDOM, seed=99,
+                max_evals=1)
+    t = h.autotune()
+    d.close()
+    return t
 
 
 def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_steps=600, topk=64):
@@ -270,18 +283,22 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
     h = lib.Handle(a.tiles, a.tiles, FREQS, precision=lib.PREC_FP64, max_flips=nfl, device=local)
     for f, G in enumerate(Gs):
         h.load_G(f, G, None)
+    tune64 = autotune_on(h)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0)
     s = d.run()
     torch.cuda.synchronize()
     out["plain_fp64"] = {"wall_s": time.perf_counter() - t0, "F_final": s.F_best, "F_init": s.F_init,
-                         "evals": s.evals, "accepts": s.accepts, "converged": bool(s.converged)}
+                         "evals": s.evals, "accepts": s.accepts, "converged": bool(s.converged),
+                         "eval_form": tune64["eval_form"]}
     F_target = s.F_best * (1.0 + 1e-3)
     d.close()
     h.close()
     torch.cuda.empty_cache()
-    h = lib.Handle(a.tiles, a.tiles, FREQS, precision=lib.PREC_C64, max_flips=nfl, device=local)
+    # complex64 state built directly in complex64 on the tensor cores
+    h = lib.Handle(a.tiles, a.tiles, FREQS, precision=lib.PREC_C64, max_flips=nfl, device=local,
+                   c64_build=lib.BUILD_C64)
     for f, G in enumerate(Gs):
         h.load_G(f, G, None)
     prop = lib.Proposal(h, channels=32, seed=1)
@@ -297,6 +314,7 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     samples = prop.num_samples()
+    tune32 = autotune_on(h)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0, drift_every=32, drift_tol=1e-4)
@@ -316,6 +334,8 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
     out["proposal_c64"] = {"wall_s_to_target": t_reach, "wall_s": wall, "F_final": s.F_best, "evals": s.evals,
                            "accepts": s.accepts, "prop_hits": s.prop_hits, "full_passes": s.full_passes,
                            "converged": bool(s.converged), "drift_max": s.drift_max,
+                           "drift_checks": s.drift_checks, "refreshes": s.refreshes,
+                           "eval_form": tune32["eval_form"], "update_cols": tune32["update"][tune32["update_form"]]["cols"],
                            "reached_target": t_reach is not None,
                            "training": {"seeds": list(train_seeds), "collect_s": t_collect, "train_s": t_train,
                                         "samples": samples, "final_loss": loss, "steps": train_steps}}
@@ -377,24 +397,31 @@ def gpu_arm(a, world, rank, local):
     upd_s = tm["update_ms"] * 1e-3
     achieved = tm["update_flop"] / upd_s / 1e12 if upd_s > 0 else None
     traffic = None
-    if os.path.exists(PROFILE_SUMMARY):
+    if os.path.exists(PROFILE_SUMMARY):  # ncu capture summary: "dram_bytes_per_launch: <bytes>"
         with open(PROFILE_SUMMARY) as fh:
-            traffic = json.load(fh).get("dram_bytes_per_launch")
+            m = re.search(r"dram_bytes_per_launch:\s*([0-9.eE+]+)", fh.read())
+        traffic = float(m.group(1)) if m else None
+    # Dominant kernel of the FP64 form: the accept update on the tensor cores
+    # (k_tc_update_f64: exact 7-bit integer slices of A and W, BF16 MMAs into
+    # FP32 TMEM accumulators, FP64 recombination). It streams M once in and
+    # once out, so its bound is HBM; its FP64-equivalent rate is reported
+    # against the measured DGEMM rate.
+    upd_gbs = tm["update_bytes"] / upd_s / 1e9 if upd_s > 0 else None
     roofline = {
-        "kernel": "k_rank_update (FP64 complex rank-k update of M, accept step)",
-        "bound": "fp64",
-        "achieved": achieved,
-        "peak": fp64_peak,
-        "unit": "TFLOP/s",
-        "frac": achieved / fp64_peak if achieved else None,
-        "peak_source": "measured on this GPU in this run: cuBLAS DGEMM 4096^3 via torch, best of 5 "
-                       "(MEASURED_PEAKS.json has no FP64 figure)",
+        "kernel": "k_tc_update_f64 (FP64-accurate complex rank-k update of M on tcgen05, accept step)",
+        "bound": "hbm",
+        "achieved": upd_gbs,
+        "peak": peaks["hbm_gbs"],
+        "unit": "GB/s",
+        "frac": upd_gbs / peaks["hbm_gbs"] if upd_gbs else None,
+        "peak_source": peak_src,
         "traffic": traffic,
-        "algorithmic_flop_per_launch": tm["update_flop"] / max(1, tm["update_launches"]),
         "algorithmic_bytes_per_launch": tm["update_bytes"] / max(1, tm["update_launches"]),
         "launch_ms": tm["update_ms"] / max(1, tm["update_launches"]),
-        "hbm_view": {"achieved_gbs": tm["update_bytes"] / upd_s / 1e9 if upd_s > 0 else None,
-                     "peak_gbs": peaks["hbm_gbs"], "peak_source": peak_src},
+        "fp64_view": {"achieved_tflops": achieved, "dgemm_peak_tflops": fp64_peak,
+                      "frac": achieved / fp64_peak if achieved else None,
+                      "algorithmic_flop_per_launch": tm["update_flop"] / max(1, tm["update_launches"]),
+                      "peak_source": "cuBLAS DGEMM 4096^3 via torch on this GPU in this run, best of 5"},
         "share_of_device_time": tm["update_ms"] / max(1e-9, tm["eval_ms"] + tm["accept_ms"]),
     }
     eval_s = tm["eval_ms"] * 1e-3
@@ -435,7 +462,7 @@ def gpu_arm(a, world, rank, local):
             "eval_kernel_fp64_tflops": tm["eval_flop"] / eval_s / 1e12 if eval_s > 0 else None,
             "eval_ms": tm["eval_ms"], "accept_ms": tm["accept_ms"], "update_ms": tm["update_ms"],
             "setup_s": r64["setup_s"], "F_init": r64["F_init"], "F_best": r64["F_best"],
-            "fp64_gemm_tflops": fp64_peak,
+            "fp64_gemm_tflops": fp64_peak, "autotune": r64["tune"],
         },
     }
     if r32 is not None:
@@ -462,6 +489,7 @@ def gpu_arm(a, world, rank, local):
                 "algorithmic_bytes_per_launch": t32["update_bytes"] / max(1, t32["update_launches"]),
             },
             "clocks": r32["clocks"], "gpu_launches": t32["kernel_launches"], "setup_s": r32["setup_s"],
+            "autotune": r32["tune"],
         }
     if conv is not None:
         line["converge"] = conv

@@ -69,7 +69,19 @@ typedef struct pngf_config {
   int defer_rank;        /* C64: flush the deferred low-rank correction at this rank (0 = every accept) */
   int device;            /* CUDA device ordinal */
   int fp64_update;       /* PNGF_PREC_FP64: PNGF_F64_TENSOR (default) or PNGF_F64_SIMT */
+  int c64_build;         /* PNGF_PREC_C64: PNGF_BUILD_FP64 (default) or PNGF_BUILD_C64, see below */
 } pngf_config;
+
+/* How pngf_prepare builds the state of a PNGF_PREC_C64 handle for a design:
+ * PNGF_BUILD_FP64 - in FP64 (as a PNGF_PREC_FP64 handle does), then T is
+ *                   rounded to complex64;
+ * PNGF_BUILD_C64  - directly in complex64: the design's edges are accepted in
+ *                   chunks through the complex64 accept step (FP64 factor and
+ *                   solves, 3xTF32 tensor-core update). Several times faster
+ *                   and about as accurate as a run of complex64 accepts.
+ * pngf_refresh always rebuilds in FP64. */
+#define PNGF_BUILD_FP64 0
+#define PNGF_BUILD_C64 1
 
 /* How a PNGF_PREC_FP64 handle runs its rank-k accept update:
  * PNGF_F64_TENSOR - exact integer slices on the BF16 tensor cores, recombined
@@ -191,6 +203,8 @@ int pngf_accept_edges_noalloc(double *M, long ldm, long n, int num_eobj, const d
  * from G by iterative refinement (X <- X - (X C - H) C^-1 with
  * C^-1 = I - P T, two sweeps) and *max_rel = max |T_c64 - T| / max |T|. */
 int pngf_drift_check(pngf_handle *h, int nrows, double *max_rel);
+/* The same at frequency f only. */
+int pngf_drift_check_freq(pngf_handle *h, int f, int nrows, double *max_rel);
 /* Rebuilds M from G for the current design (drift refresh). */
 int pngf_refresh(pngf_handle *h);
 
@@ -221,6 +235,33 @@ typedef struct pngf_timing {
 int pngf_timing_enable(pngf_handle *h, int on);
 /* Synchronizes the handle's stream and returns the accumulated counters. */
 int pngf_timing_get(pngf_handle *h, pngf_timing *out);
+
+/* ---- autotuning (no reference counterpart) ---- */
+
+#define PNGF_TUNE_MAX 8
+/* Forms of the candidate kernel: warps that work on one (candidate, frequency)
+ * and candidates per CTA. Warp-per-candidate forms (1 warp) apply when a
+ * candidate flips at most 32 edges. All forms return bit-identical results. */
+typedef struct pngf_tune {
+  int eval_form;                     /* chosen form */
+  int eval_forms;                    /* forms listed below */
+  int warps_per_cand[PNGF_TUNE_MAX];
+  int cands_per_cta[PNGF_TUNE_MAX];
+  double eval_us[PNGF_TUNE_MAX];     /* device time of one batch; -1 = form does not apply */
+  int batch;                         /* candidates in the timed batch (every tile once) */
+  int update_form;                   /* chosen complex64 update tile form */
+  int update_forms;
+  int update_cols[PNGF_TUNE_MAX];    /* FP32 output columns per update tile */
+  double update_us[PNGF_TUNE_MAX];   /* device time of one rank-update; -1 = not timed */
+} pngf_tune;
+/* Times every applicable form of the candidate kernel (and, for
+ * PNGF_PREC_C64, of the update tile) at the current design, keeps the fastest
+ * for this handle and reports the times. Call after pngf_prepare; the last
+ * evaluated batch is discarded and M is left unchanged. */
+int pngf_autotune(pngf_handle *h, pngf_tune *out);
+/* Selects a candidate-kernel form by index (PNGF_ERR_UNSUPPORTED if it does
+ * not apply to this handle). */
+int pngf_set_eval_form(pngf_handle *h, int form);
 
 /* ---- DBS driver (host, native): pngf-opt/main.cpp:181-459 ---- */
 

@@ -383,6 +383,7 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
       c.max_flips > 8 || !(c.dx > 0) || !(c.dy > 0) || !(c.dz > 0))
     return PNGF_ERR_ARG;
   if (c.precision != PNGF_PREC_FP64 && c.precision != PNGF_PREC_C64) return PNGF_ERR_ARG;
+  if (c.c64_build != PNGF_BUILD_FP64 && c.c64_build != PNGF_BUILD_C64) return PNGF_ERR_ARG;
   const int kmax = c.max_flips * edges_per_tile(c);
   if (kmax > kMaxEvalK) return PNGF_ERR_UNSUPPORTED;
   int ndev = 0;
@@ -434,7 +435,7 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
     einc[f] = q.Einc;
   }
   if (c64) {  // tensor-core operands: rows padded to the 128-row tile, zero outside what each update writes
-    h->kt_cap = (6 * kmax + 31) / 32 * 32;
+    h->kt_cap = (6 * std::max(kmax, kInitChunk) + 31) / 32 * 32;  // accepts and complex64 build chunks
     h->aop_rows = (n + 127) / 128 * 128;
     h->bop_rows = (2 * n + 127) / 128 * 128;
     if ((rc = dalloc(h, &h->d_Aop, (size_t)h->aop_rows * h->kt_cap)) ||
@@ -574,9 +575,9 @@ int pngf_set_source_port(pngf_handle *ph, int tile_x, int tile_y, int y_offset, 
   return PNGF_OK;
 }
 
-int pngf_prepare(pngf_handle *ph) {
-  Handle *h = H(ph);
-  if (!h) return PNGF_ERR_ARG;
+// Builds the state for the current design from G. fp64: in FP64 (then T is
+// rounded for a complex64 handle); else directly in complex64.
+static int prepare_impl(Handle *h, bool fp64) {
   for (int f = 0; f < h->cfg.num_freq; ++f)
     if (!h->f[f].loaded) return set_error(h, PNGF_ERR_STATE, "G not loaded for frequency " + std::to_string(f));
   if (!h->have_map) return set_error(h, PNGF_ERR_STATE, "tile map not set");
@@ -592,13 +593,17 @@ int pngf_prepare(pngf_handle *ph) {
     PNGF_CUDA(h, cudaMemcpyAsync(h->d_acc_d, ones.data(), on.size(), cudaMemcpyHostToDevice, h->stream));
   }
   PNGF_CUDA(h, cudaMemsetAsync(h->d_acc_status, 0, sizeof(int), h->stream));
+  const bool c64 = h->cfg.precision == PNGF_PREC_C64;
   for (int f = 0; f < h->cfg.num_freq; ++f) {
     PNGF_CUDA(h, launch_init_M(h, f));
-    for (size_t c0 = 0; c0 < on.size(); c0 += h->init_chunk) {
-      const int k = (int)std::min<size_t>(h->init_chunk, on.size() - c0);
-      PNGF_CUDA(h, launch_accept_edges(h, f, h->d_acc_s + c0, h->d_acc_d + c0, k, PNGF_PREC_FP64));
+    if (c64 && !fp64) PNGF_CUDA(h, launch_split_M(h, f));
+    const int chunk = fp64 ? h->init_chunk : kInitChunk;
+    for (size_t c0 = 0; c0 < on.size(); c0 += chunk) {
+      const int k = (int)std::min<size_t>(chunk, on.size() - c0);
+      PNGF_CUDA(h, launch_accept_edges(h, f, h->d_acc_s + c0, h->d_acc_d + c0, k,
+                                       fp64 ? PNGF_PREC_FP64 : PNGF_PREC_C64));
     }
-    if (h->cfg.precision == PNGF_PREC_C64) PNGF_CUDA(h, launch_split_M(h, f));
+    if (c64 && fp64) PNGF_CUDA(h, launch_split_M(h, f));
   }
   int st = 0, tc = 0;
   PNGF_CUDA(h, cudaMemcpyAsync(&st, h->d_acc_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -614,6 +619,12 @@ int pngf_prepare(pngf_handle *ph) {
   h->prepared = true;
   h->batch_valid = false;
   return PNGF_OK;
+}
+
+int pngf_prepare(pngf_handle *ph) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  return prepare_impl(h, !(h->cfg.precision == PNGF_PREC_C64 && h->cfg.c64_build == PNGF_BUILD_C64));
 }
 
 int pngf_get_eobj(pngf_handle *ph, int f, double *eobj, double *vinc_ln) {
@@ -730,9 +741,10 @@ int pngf_accept(pngf_handle *ph, int cand) {
   return accept_cand(h, cand, h->last_k[cand]);
 }
 
-int pngf_drift_check(pngf_handle *ph, int nrows, double *max_rel) {
-  Handle *h = H(ph);
-  if (!h || !max_rel) return PNGF_ERR_ARG;
+}  // extern "C"
+
+// Drift check over frequencies f0 .. f1-1.
+static int drift_impl(Handle *h, int f0, int f1, int nrows, double *max_rel) {
   if (h->cfg.precision != PNGF_PREC_C64)
     return set_error(h, PNGF_ERR_UNSUPPORTED, "drift check applies to PNGF_PREC_C64 handles");
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
@@ -764,7 +776,7 @@ int pngf_drift_check(pngf_handle *ph, int nrows, double *max_rel) {
   if (e == cudaSuccess && !on.empty())
     e = cudaMemcpyAsync(h->d_acc_s, on.data(), sizeof(int) * on.size(), cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, sizeof(unsigned long long) * 2 * h->cfg.num_freq, h->stream);
-  for (int f = 0; f < h->cfg.num_freq && e == cudaSuccess; ++f)
+  for (int f = f0; f < f1 && e == cudaSuccess; ++f)
     e = launch_drift_rows(h, f, d_rows, nrows, h->d_acc_s, (int)on.size(), X, PH, Rk, d_out + 2 * f);
   std::vector<unsigned long long> out(2 * h->cfg.num_freq);
   if (e == cudaSuccess)
@@ -772,7 +784,7 @@ int pngf_drift_check(pngf_handle *ph, int nrows, double *max_rel) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   release();
   if (e != cudaSuccess) return cuda_check(h, e, "drift check");
-  for (int f = 0; f < h->cfg.num_freq; ++f) {
+  for (int f = f0; f < f1; ++f) {
     double dmax, xmax;
     std::memcpy(&dmax, &out[2 * f], sizeof(double));
     std::memcpy(&xmax, &out[2 * f + 1], sizeof(double));
@@ -782,7 +794,26 @@ int pngf_drift_check(pngf_handle *ph, int nrows, double *max_rel) {
   return PNGF_OK;
 }
 
-int pngf_refresh(pngf_handle *ph) { return pngf_prepare(ph); }
+extern "C" {
+
+int pngf_drift_check(pngf_handle *ph, int nrows, double *max_rel) {
+  Handle *h = H(ph);
+  if (!h || !max_rel) return PNGF_ERR_ARG;
+  return drift_impl(h, 0, h->cfg.num_freq, nrows, max_rel);
+}
+
+int pngf_drift_check_freq(pngf_handle *ph, int f, int nrows, double *max_rel) {
+  Handle *h = H(ph);
+  if (!h || !max_rel) return PNGF_ERR_ARG;
+  if (f < 0 || f >= h->cfg.num_freq) return set_error(h, PNGF_ERR_ARG, "frequency index out of range");
+  return drift_impl(h, f, f + 1, nrows, max_rel);
+}
+
+int pngf_refresh(pngf_handle *ph) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  return prepare_impl(h, true);
+}
 
 int pngf_timing_enable(pngf_handle *ph, int on) {
   Handle *h = H(ph);
@@ -803,6 +834,125 @@ int pngf_timing_get(pngf_handle *ph, pngf_timing *out) {
   *out = h->tacc;
   out->kernel_launches = h->nlaunch;
   return PNGF_OK;
+}
+
+}  // extern "C"
+
+// Times the complex64 update at each output tile width with zero operands
+// (T, y and R are then left unchanged) and keeps the fastest.
+static int tune_update(Handle *h, pngf_tune *out) {
+  if (h->cfg.precision != PNGF_PREC_C64) return PNGF_OK;
+  const int widths[2] = {128, 64};
+  const int k = std::min(h->kmax, 24);
+  const long rows = h->n + h->E;
+  PNGF_CUDA(h, cudaMemsetAsync(h->d_A, 0, sizeof(double2) * rows * k, h->stream));
+  PNGF_CUDA(h, cudaMemsetAsync(h->d_W, 0, sizeof(double2) * k * h->ldm, h->stream));
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+    if (a) cudaEventDestroy(a);
+    return set_error(h, PNGF_ERR_CUDA, "event creation failed");
+  }
+  const long nl0 = h->nlaunch;
+  const bool timing = h->timing;
+  h->timing = false;
+  const int reps = 3;
+  double best = 1e300;
+  int bi = 0;
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+    h->c64_cols = widths[i];
+    out->update_cols[i] = widths[i];
+    out->update_us[i] = -1.0;
+    if ((e = launch_c64_update(h, 0, k)) != cudaSuccess) break;  // warm-up
+    cudaEventRecord(a, h->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_c64_update(h, 0, k);
+    cudaEventRecord(b, h->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    out->update_us[i] = 1e3 * ms / reps;
+    if (out->update_us[i] < best) {
+      best = out->update_us[i];
+      bi = i;
+    }
+  }
+  h->timing = timing;
+  h->nlaunch = nl0;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  h->c64_cols = widths[bi];
+  out->update_form = bi;
+  out->update_forms = 2;
+  if (e != cudaSuccess) return cuda_check(h, e, "autotune (update)");
+  int tc = 0;
+  PNGF_CUDA(h, cudaMemcpy(&tc, h->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (tc != 0) {
+    cudaMemset(h->d_tc_err, 0, sizeof(int));
+    return set_error(h, PNGF_ERR_TIMEOUT, "tensor-core update gave up waiting (code " + std::to_string(tc) + ")");
+  }
+  return PNGF_OK;
+}
+
+extern "C" {
+
+int pngf_set_eval_form(pngf_handle *ph, int form) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  if (!eval_variant_ok(h, form)) return set_error(h, PNGF_ERR_UNSUPPORTED, "candidate-kernel form does not apply");
+  h->eval_variant = form;
+  return PNGF_OK;
+}
+
+int pngf_autotune(pngf_handle *ph, pngf_tune *out) {
+  Handle *h = H(ph);
+  if (!h || !out) return PNGF_ERR_ARG;
+  if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "pngf_prepare has not been called for this design");
+  std::memset(out, 0, sizeof(*out));
+  // Every tile once as a single-tile candidate: the shape of a DBS pass.
+  const int mf = h->cfg.max_flips, nc = h->map_sz;
+  std::vector<int> tiles((size_t)nc * mf, 0), nfl(nc, 1);
+  for (int i = 0; i < nc; ++i) tiles[(size_t)i * mf] = i;
+  int rc = eval_batch(h, tiles.data(), nfl.data(), nc, 0.0, nullptr);
+  if (rc) return rc;
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+    if (a) cudaEventDestroy(a);
+    return set_error(h, PNGF_ERR_CUDA, "event creation failed");
+  }
+  const int reps = 5;
+  double best = 1e300;
+  int bestv = 0;
+  out->eval_forms = kEvalVariants;
+  out->batch = nc;
+  const long nl0 = h->nlaunch;
+  cudaError_t e = cudaSuccess;
+  for (int v = 0; v < kEvalVariants && e == cudaSuccess; ++v) {
+    out->warps_per_cand[v] = kEvalForms[v].warps_per_cand;
+    out->cands_per_cta[v] = kEvalForms[v].cands_per_cta;
+    out->eval_us[v] = -1.0;
+    if (!eval_variant_ok(h, v)) continue;
+    h->eval_variant = v;
+    if ((e = launch_eval(h, nc, 0.0)) != cudaSuccess) break;  // warm-up
+    cudaEventRecord(a, h->stream);
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_eval(h, nc, 0.0);
+    cudaEventRecord(b, h->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    out->eval_us[v] = 1e3 * ms / reps;
+    if (out->eval_us[v] < best) {
+      best = out->eval_us[v];
+      bestv = v;
+    }
+  }
+  h->nlaunch = nl0;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  h->eval_variant = bestv;
+  out->eval_form = bestv;
+  h->batch_valid = false;
+  if (e != cudaSuccess) return cuda_check(h, e, "autotune");
+  return tune_update(h, out);
 }
 
 }  // extern "C"

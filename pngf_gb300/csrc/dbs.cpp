@@ -140,6 +140,26 @@ bool next_candidate(pngf_dbs *d, Cand *c) {
   }
 }
 
+// Complex64 state: every drift_every accepts, an FP64 drift check of 4 sampled
+// rows of T at one frequency (frequencies in turn); the state is rebuilt from
+// G in FP64 when the drift exceeds drift_tol.
+int drift_after_accept(pngf_dbs *d) {
+  pngf::Handle *h = d->h;
+  if (h->cfg.precision != PNGF_PREC_C64 || d->p.drift_every <= 0 || d->accepts % d->p.drift_every != 0)
+    return PNGF_OK;
+  double rel = 0.0;
+  pngf_handle *ph = reinterpret_cast<pngf_handle *>(h);
+  int rc = pngf_drift_check_freq(ph, (int)(d->drift_checks % h->cfg.num_freq), 4, &rel);
+  if (rc) return rc;
+  ++d->drift_checks;
+  d->drift_max = std::max(d->drift_max, rel);
+  if (d->p.drift_tol > 0 && rel > d->p.drift_tol) {
+    if ((rc = pngf_refresh(ph)) || (rc = pngf_objective(ph, &d->F_best))) return rc;
+    ++d->refreshes;
+  }
+  return PNGF_OK;
+}
+
 void log_row(pngf_dbs *d, const Cand &c, int acc, double F, const double *perf, int nf) {
   d->lg_tile.push_back(c.log_index);
   d->lg_acc.push_back(acc);
@@ -191,7 +211,7 @@ int proposal_step(pngf_dbs *d, int *accepted) {
     ++d->accepts;
     if (accepted) *accepted = 1;
     (void)list;
-    return PNGF_OK;
+    return drift_after_accept(d);
   };
   int rc;
   ++d->prop_steps;
@@ -369,19 +389,7 @@ int pngf_dbs_step(pngf_dbs *d, int *accepted) {
       }
       d->hat.reset();
       if (accepted) *accepted = 1;
-      // Complex64 state: periodic FP64 drift check, rebuild from G when it drifted.
-      if (h->cfg.precision == PNGF_PREC_C64 && d->p.drift_every > 0 && d->accepts % d->p.drift_every == 0) {
-        double rel = 0.0;
-        pngf_handle *ph = reinterpret_cast<pngf_handle *>(h);
-        if ((rc = pngf_drift_check(ph, 4, &rel))) return rc;
-        ++d->drift_checks;
-        d->drift_max = std::max(d->drift_max, rel);
-        if (d->p.drift_tol > 0 && rel > d->p.drift_tol) {
-          if ((rc = pngf_refresh(ph)) || (rc = pngf_objective(ph, &d->F_best))) return rc;
-          ++d->refreshes;
-        }
-      }
-      return PNGF_OK;
+      return drift_after_accept(d);
     }
     if (exhausted) {
       d->converged = d->done = true;

@@ -34,27 +34,30 @@ namespace pngf {
 namespace {
 
 constexpr int TC_BM = 128;       // rows per tile (MMA M)
-constexpr int TC_BN = 128;       // fp32 columns per tile (MMA N)
 constexpr int TC_BK = 32;        // fp32 K elements per stage = one 128-byte swizzle row
 constexpr int TC_ST = 2;         // pipeline stages (3 CTAs per SM fit in shared memory and TMEM)
 constexpr uint32_t A_BYTES = TC_BM * TC_BK * 4;
-constexpr uint32_t B_BYTES = TC_BN * TC_BK * 4;
-constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr size_t TC_SMEM = TC_ST * STAGE_BYTES + 1024 + 256;
+// Per output-tile width BN (fp32 columns, the MMA N; 64 or 128, picked by the autotuner):
+template <int BN> __host__ __device__ constexpr uint32_t b_bytes() { return BN * TC_BK * 4; }
+template <int BN> __host__ __device__ constexpr uint32_t stage_bytes() { return A_BYTES + b_bytes<BN>(); }
+template <int BN> __host__ __device__ constexpr size_t tc_smem() { return TC_ST * stage_bytes<BN>() + 1024 + 256; }
 using namespace tc;
 
 // Instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
 // (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits
 // 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t kIdescTF32 =
-    (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+template <int BN> __host__ __device__ constexpr uint32_t idesc_tf32() {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+}
 
 // D[i, j] -= sum_k Aop[i, k] Bop[j, k] for i < rows, j < cols (fp32, D row-major
 // with leading dimension ldd). Aop / Bop come through TMA maps (K-major, 128B
 // swizzle). nkb = K / 32.
+template <int BN>
 __global__ void __launch_bounds__(192, 3) k_tc_update(const __grid_constant__ CUtensorMap tmA,
                                                       const __grid_constant__ CUtensorMap tmB, float *__restrict__ D,
                                                       long ldd, int rows, int cols, int nkb, int *err) {
+  constexpr uint32_t B_BYTES = b_bytes<BN>(), STAGE_BYTES = stage_bytes<BN>();
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                           ~static_cast<uintptr_t>(1023));
@@ -74,7 +77,7 @@ __global__ void __launch_bounds__(192, 3) k_tc_update(const __grid_constant__ CU
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
-                 "r"((uint32_t)TC_BN)
+                 "r"((uint32_t)BN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -82,7 +85,7 @@ __global__ void __launch_bounds__(192, 3) k_tc_update(const __grid_constant__ CU
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -118,7 +121,7 @@ __global__ void __launch_bounds__(192, 3) k_tc_update(const __grid_constant__ CU
         const uint64_t bd = sw128_desc(sbase + s * STAGE_BYTES + A_BYTES);
 #pragma unroll
         for (int kk = 0; kk < TC_BK / 8; ++kk)  // K = 8 tf32 = 32 bytes per MMA: +2 in 16-byte units
-          mma_tf32(tmem, ad + 2 * kk, bd + 2 * kk, kIdescTF32, (kb | kk) != 0);
+          mma_tf32(tmem, ad + 2 * kk, bd + 2 * kk, idesc_tf32<BN>(), (kb | kk) != 0);
         mma_commit(empty0 + 8 * s);
       }
       mma_commit(done);
@@ -132,7 +135,7 @@ __global__ void __launch_bounds__(192, 3) k_tc_update(const __grid_constant__ CU
     float *drow = D + (size_t)row * ldd;
     // The first half of this thread's row segment is read while the MMAs run;
     // the second half is read while the first half is written back.
-    constexpr int HALF = TC_BN / 2;
+    constexpr int HALF = BN / 2;
     float4 pre[HALF / 4];
 #pragma unroll
     for (int u = 0; u < HALF / 4; ++u) {
@@ -186,7 +189,7 @@ __global__ void __launch_bounds__(192, 3) k_tc_update(const __grid_constant__ CU
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)TC_BN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
   }
 }
 
@@ -350,32 +353,46 @@ __global__ void k_rows_residual(const double2 *__restrict__ X, const double2 *__
   }
 }
 
-// X[r][j] -= Rk[r][j] - sum_{l in P} Rk[r][P_l] T[P_l][j] (thread per column).
-__global__ void k_rows_refine(double2 *__restrict__ X, const double2 *__restrict__ Rk, int nr, long n,
-                              const int *__restrict__ Pidx, int np, const float2 *__restrict__ T32, long ldm) {
-  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= n) return;
+// X[r][j] -= Rk[r][j] - sum_{l in P} Rk[r][P_l] T[P_l][j]: 32 columns per CTA
+// (lane = column, so each warp reads 256 contiguous bytes of a row of T), the
+// sum over P split across the CTA's 8 warps and reduced in shared memory.
+__global__ void __launch_bounds__(256) k_rows_refine(double2 *__restrict__ X, const double2 *__restrict__ Rk, int nr,
+                                                     long n, const int *__restrict__ Pidx, int np,
+                                                     const float2 *__restrict__ T32, long ldm) {
+  __shared__ double2 part[8][DR_MAX_ROWS][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long j = (long)blockIdx.x * 32 + lane;
   double2 acc[DR_MAX_ROWS];
 #pragma unroll
   for (int r = 0; r < DR_MAX_ROWS; ++r) acc[r] = make_double2(0.0, 0.0);
-  for (int q = 0; q < np; ++q) {
-    const int l = Pidx[q];
-    const float2 tf = T32[(size_t)l * ldm + j];
-    const double2 t = make_double2(tf.x, tf.y);
+  if (j < n)
+    for (int q = w; q < np; q += 8) {
+      const int l = Pidx[q];
+      const float2 tf = T32[(size_t)l * ldm + j];
+      const double2 t = make_double2(tf.x, tf.y);
 #pragma unroll
-    for (int r = 0; r < DR_MAX_ROWS; ++r)
-      if (r < nr) {
-        const double2 rv = Rk[(size_t)r * n + l];
-        acc[r].x += rv.x * t.x - rv.y * t.y;
-        acc[r].y += rv.x * t.y + rv.y * t.x;
+      for (int r = 0; r < DR_MAX_ROWS; ++r)
+        if (r < nr) {
+          const double2 rv = Rk[(size_t)r * n + l];
+          acc[r].x += rv.x * t.x - rv.y * t.y;
+          acc[r].y += rv.x * t.y + rv.y * t.x;
+        }
+    }
+#pragma unroll
+  for (int r = 0; r < DR_MAX_ROWS; ++r) part[w][r][lane] = acc[r];
+  __syncthreads();
+  if (w == 0 && j < n)
+    for (int r = 0; r < nr; ++r) {
+      double2 sum = part[0][r][lane];
+      for (int u = 1; u < 8; ++u) {
+        sum.x += part[u][r][lane].x;
+        sum.y += part[u][r][lane].y;
       }
-  }
-  for (int r = 0; r < nr; ++r) {
-    const double2 rv = Rk[(size_t)r * n + j];
-    double2 &x = X[(size_t)r * n + j];
-    x.x -= rv.x - acc[r].x;
-    x.y -= rv.y - acc[r].y;
-  }
+      const double2 rv = Rk[(size_t)r * n + j];
+      double2 &x = X[(size_t)r * n + j];
+      x.x -= rv.x - sum.x;
+      x.y -= rv.y - sum.y;
+    }
 }
 
 __global__ void k_rows_load(const float2 *__restrict__ T32, long ldm, const int *__restrict__ rows, int nr, long n,
@@ -427,11 +444,11 @@ cudaError_t get_encoder() {
 }
 
 // 2-D fp32 tensor map over rows x K (K contiguous, row pitch ldk floats),
-// box 32 x 128, 128-byte swizzle.
-cudaError_t make_map(CUtensorMap *m, const float *base, long rows, int K, long ldk) {
+// box 32 x box_rows, 128-byte swizzle.
+cudaError_t make_map(CUtensorMap *m, const float *base, long rows, int K, long ldk, int box_rows) {
   const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)ldk * sizeof(float)};
-  const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)TC_BM};
+  const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box,
                               estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -459,7 +476,7 @@ cudaError_t launch_drift_rows(Handle *h, int f, const int *d_rows, int nr, const
   for (int it = 0; it < 2; ++it) {
     k_rows_PH<<<gw, 256, 0, h->stream>>>(X, nr, n, d_P, np, q.G, PH);
     k_rows_residual<<<g1, 256, 0, h->stream>>>(X, PH, q.G, d_rows, nr, n, Rk);
-    k_rows_refine<<<g1, 256, 0, h->stream>>>(X, Rk, nr, n, d_P, np, q.T32, h->ldm);
+    k_rows_refine<<<(unsigned)((n + 31) / 32), 256, 0, h->stream>>>(X, Rk, nr, n, d_P, np, q.T32, h->ldm);
   }
   k_rows_compare<<<g1, 256, 0, h->stream>>>(q.T32, h->ldm, d_rows, nr, n, X, d_out);
   h->nlaunch += 8;
@@ -489,17 +506,26 @@ cudaError_t launch_c64_update(Handle *h, int f, int k) {
   const dim3 ga((unsigned)((Kt + 127) / 128), (unsigned)n), gb((unsigned)((Kt + 127) / 128), (unsigned)(2 * n));
   k_build_Aop<<<ga, 128, 0, h->stream>>>(h->d_A, rows, n, k, Kt, h->kt_cap, h->d_Aop);
   k_build_Bop<<<gb, 128, 0, h->stream>>>(h->d_W, h->ldm, n, k, Kt, h->kt_cap, h->d_Bop);
+  const int bn = h->c64_cols == 64 ? 64 : 128;
   CUtensorMap ma, mb;
-  if ((e = make_map(&ma, h->d_Aop, h->aop_rows, Kt, h->kt_cap)) != cudaSuccess) return e;
-  if ((e = make_map(&mb, h->d_Bop, h->bop_rows, Kt, h->kt_cap)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM)) !=
-      cudaSuccess)
-    return e;
+  if ((e = make_map(&ma, h->d_Aop, h->aop_rows, Kt, h->kt_cap, TC_BM)) != cudaSuccess) return e;
+  if ((e = make_map(&mb, h->d_Bop, h->bop_rows, Kt, h->kt_cap, bn)) != cudaSuccess) return e;
   const int dcols = (int)(2 * n);
-  dim3 g((unsigned)((dcols + TC_BN - 1) / TC_BN), (unsigned)((n + TC_BM - 1) / TC_BM));
+  dim3 g((unsigned)((dcols + bn - 1) / bn), (unsigned)((n + TC_BM - 1) / TC_BM));
   cudaEvent_t t0 = timing_mark(h);
-  k_tc_update<<<g, 192, TC_SMEM, h->stream>>>(ma, mb, reinterpret_cast<float *>(q.T32), 2 * h->ldm, (int)n, dcols,
-                                               Kt / TC_BK, h->d_tc_err);
+  if (bn == 64) {
+    if ((e = cudaFuncSetAttribute(k_tc_update<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tc_smem<64>())) != cudaSuccess)
+      return e;
+    k_tc_update<64><<<g, 192, tc_smem<64>(), h->stream>>>(ma, mb, reinterpret_cast<float *>(q.T32), 2 * h->ldm,
+                                                          (int)n, dcols, Kt / TC_BK, h->d_tc_err);
+  } else {
+    if ((e = cudaFuncSetAttribute(k_tc_update<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tc_smem<128>())) != cudaSuccess)
+      return e;
+    k_tc_update<128><<<g, 192, tc_smem<128>(), h->stream>>>(ma, mb, reinterpret_cast<float *>(q.T32), 2 * h->ldm,
+                                                            (int)n, dcols, Kt / TC_BK, h->d_tc_err);
+  }
   const double cells = (double)n * (double)n;  // complex entries of T updated
   timing_close(h, t0, T_UPDATE, 8.0 * k * cells,
                2.0 * 8.0 * cells + 4.0 * Kt * ((double)h->aop_rows + (double)h->bop_rows), 0.0);

@@ -30,20 +30,33 @@
 
 namespace pngf {
 
+// Complex arithmetic with every fused multiply-add written out, so that the
+// rounding does not depend on how the compiler contracts an expression in a
+// given kernel: the CTA- and warp-per-candidate evaluation kernels (and the
+// accept prologue) then produce bit-identical results.
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_double2(__fma_rn(a.x, b.x, __dmul_rn(-a.y, b.y)), __fma_rn(a.x, b.y, __dmul_rn(a.y, b.x)));
 }
 // a - b*c
 __device__ __forceinline__ double2 cfnma(double2 a, double2 b, double2 c) {
-  return make_double2(a.x - b.x * c.x + b.y * c.y, a.y - b.x * c.y - b.y * c.x);
+  return make_double2(__fma_rn(b.y, c.y, __fma_rn(-b.x, c.x, a.x)), __fma_rn(-b.y, c.x, __fma_rn(-b.x, c.y, a.y)));
 }
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
 __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
-  const double den = b.x * b.x + b.y * b.y;
-  return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+  const double den = __fma_rn(b.x, b.x, __dmul_rn(b.y, b.y));
+  return make_double2(__ddiv_rn(__fma_rn(a.x, b.x, __dmul_rn(a.y, b.y)), den),
+                      __ddiv_rn(__fma_rn(a.y, b.x, __dmul_rn(-a.x, b.y)), den));
+}
+// 1 / p, as the LU's column scaling uses it.
+__device__ __forceinline__ double2 crecip(double2 p) {
+  const double den = __fma_rn(p.x, p.x, __dmul_rn(p.y, p.y));
+  return make_double2(__ddiv_rn(p.x, den), __ddiv_rn(-p.y, den));
+}
+__device__ __forceinline__ double2 shfl2(double2 v, int src) {
+  return make_double2(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
 }
 
 template <typename T> __device__ __forceinline__ double2 ldM(const T *M, size_t i);
@@ -99,7 +112,8 @@ __host__ Geo make_geo(const Handle *h) {
 }
 
 // One frequency's objective term (main.cpp:407-413). perf = (Re S11, Im S11, D).
-__device__ double objective_term(const double2 *eo, int E, const FreqConst &fc, const ObjConst &oc,
+// Not inlined, so every kernel that calls it rounds it the same way.
+__device__ __noinline__ double objective_term(const double2 *eo, int E, const FreqConst &fc, const ObjConst &oc,
                                  double *perf) {
   const double2 v = cadd(eo[0], fc.vinc);
   double2 zin = make_double2(-v.x * oc.dx * 0.5 / (2.0 * oc.dy * oc.dz),
@@ -303,9 +317,7 @@ __device__ int cta_lu(double2 *K, int ld, int k, int *piv, double *red_v, int *r
       }
     __syncthreads();
     if (red_v[0] != 0.0) {
-      const double2 pv = K[j + j * ld];
-      const double den = pv.x * pv.x + pv.y * pv.y;
-      const double2 r = make_double2(pv.x / den, -pv.y / den);
+      const double2 r = crecip(K[j + j * ld]);
       for (int i = j + 1 + tid; i < k; i += nt) K[i + j * ld] = cmul(K[i + j * ld], r);
     }
     __syncthreads();
@@ -387,8 +399,8 @@ __device__ int cta_capacitance(const SV<TM> &M, long n, const double2 *__restric
 // ---------------------------------------------------------------------------
 // evaluation
 
-template <typename TM>
-__global__ void __launch_bounds__(128) k_eval(const SV<TM> *__restrict__ Ms, const double2 *const *__restrict__ Eincs,
+template <typename TM, int NT>
+__global__ void __launch_bounds__(NT) k_eval(const SV<TM> *__restrict__ Ms, const double2 *const *__restrict__ Eincs,
                                               long n, int E, int kmax, const int *__restrict__ es,
                                               const signed char *__restrict__ ed, const int *__restrict__ ek,
                                               const FreqConst *__restrict__ fconst, ObjConst oc, int nf,
@@ -435,6 +447,150 @@ __global__ void __launch_bounds__(128) k_eval(const SV<TM> *__restrict__ Ms, con
   __syncthreads();
   if (tid == 0) {
     const size_t cf = (size_t)c * nf + f;
+    for (int e = 0; e < E; ++e) new_eobj[cf * E + e] = eo[e];
+    double pf[3];
+    double F = objective_term(eo, E, fconst[f], oc, pf);
+    if (info != 0) F = nan("");
+    Ff[cf] = F;
+    perf[cf * 3 + 0] = pf[0];
+    perf[cf * 3 + 1] = pf[1];
+    perf[cf * 3 + 2] = pf[2];
+    status[cf] = info != 0 ? PNGF_ERR_SINGULAR : PNGF_OK;
+  }
+}
+
+// Warp-per-candidate evaluation for candidates of at most 32 edges: WPC warps
+// per CTA, one (candidate, frequency) per warp, no CTA-wide barrier. Lane r
+// owns row r of K (shared memory, column-major, odd leading dimension) and
+// entry r of the edge list, Einc_s and the right-hand side; the pivot search
+// is a warp argmax and the triangular solves run in registers with shuffles.
+// Every operation, and its order, is the one k_eval performs, so both kernels
+// return bit-identical results.
+template <typename TM, int WPC>
+__global__ void __launch_bounds__(32 * WPC)
+    k_eval_warp(const SV<TM> *__restrict__ Ms, const double2 *const *__restrict__ Eincs, long n, int E, int kmax,
+                int ncand, const int *__restrict__ es, const signed char *__restrict__ ed,
+                const int *__restrict__ ek, const FreqConst *__restrict__ fconst, ObjConst oc, int nf,
+                double2 *__restrict__ new_eobj, double *__restrict__ Ff, double *__restrict__ perf,
+                int *__restrict__ status) {
+  extern __shared__ double2 smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * WPC + warp, f = blockIdx.y;
+  if (c >= ncand) return;
+  const int ld = kmax | 1;
+  double2 *K = smem + (size_t)warp * ld * kmax;
+  const SV<TM> M = Ms[f];
+  const int k = ek[c];
+  const size_t cf = (size_t)c * nf + f;
+  if (k < 0) {
+    if (lane == 0) {
+      Ff[cf] = nan("");
+      status[cf] = PNGF_ERR_ARG;
+    }
+    return;
+  }
+  int s_l = 0;
+  signed char d_l = 1;
+  double2 einc_l = make_double2(0.0, 0.0);
+  if (lane < k) {
+    s_l = es[(size_t)c * kmax + lane];
+    d_l = ed[(size_t)c * kmax + lane];
+    einc_l = Eincs[f][s_l];
+  }
+  // K = T[s,s] D, one row per step with the lanes along the row.
+  for (int r = 0; r < k; ++r) {
+    const int sr = __shfl_sync(0xffffffffu, s_l, r);
+    if (lane < k) {
+      double2 v = M.t(sr, s_l);
+      if (d_l < 0) v = make_double2(-v.x, -v.y);
+      K[r + lane * ld] = v;
+    }
+  }
+  __syncwarp();
+  // w = y_s - T[s,s] D Einc_s, then K += I.
+  double2 w = make_double2(0.0, 0.0);
+  if (lane < k) w = M.yv(s_l);
+  for (int q = 0; q < k; ++q) {
+    const double2 eq = shfl2(einc_l, q);
+    if (lane < k) w = cfnma(w, K[lane + q * ld], eq);
+  }
+  if (lane < k) K[lane + lane * ld].x += 1.0;
+  __syncwarp();
+  // LU with partial pivoting (izamax: largest |re|+|im|, first on ties).
+  int info = 0, piv_l = lane;
+  for (int j = 0; j < k; ++j) {
+    double bv = -1.0;
+    int bi = j;
+    if (lane >= j && lane < k) {
+      const double v = cabs1(K[lane + j * ld]);
+      if (v > bv) {
+        bv = v;
+        bi = lane;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > bv || (ov == bv && oi < bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    const int p = bi;
+    if (lane == j) piv_l = p;
+    if (bv == 0.0 && info == 0) info = j + 1;
+    if (p != j) {
+      if (lane < k) {
+        const double2 t = K[j + lane * ld];
+        K[j + lane * ld] = K[p + lane * ld];
+        K[p + lane * ld] = t;
+      }
+      __syncwarp();
+    }
+    if (bv != 0.0) {
+      const double2 r = crecip(K[j + j * ld]);
+      if (lane > j && lane < k) K[lane + j * ld] = cmul(K[lane + j * ld], r);
+    }
+    if (lane > j && lane < k) {
+      const double2 l = K[lane + j * ld];
+      for (int q = j + 1; q < k; ++q) K[lane + q * ld] = cfnma(K[lane + q * ld], l, K[j + q * ld]);
+    }
+    __syncwarp();
+  }
+  if (info == 0) {
+    for (int j = 0; j < k; ++j) {  // row interchanges, in order
+      const int p = __shfl_sync(0xffffffffu, piv_l, j);
+      if (p != j) {
+        const double2 bj = shfl2(w, j), bp = shfl2(w, p);
+        if (lane == j) w = bp;
+        else if (lane == p) w = bj;
+      }
+    }
+    for (int j = 0; j < k; ++j) {  // unit lower
+      const double2 bj = shfl2(w, j);
+      if (lane > j && lane < k) w = cfnma(w, K[lane + j * ld], bj);
+    }
+    for (int j = k - 1; j >= 0; --j) {  // upper
+      if (lane == j) w = cdiv(w, K[j + j * ld]);
+      const double2 bj = shfl2(w, j);
+      if (lane < j) w = cfnma(w, K[lane + j * ld], bj);
+    }
+  }
+  double2 z = cadd(einc_l, w);
+  if (d_l < 0) z = make_double2(-z.x, -z.y);
+  // newEobj = Eobj - R[:,s] z, reduced across the warp as k_eval does.
+  double2 eo[PNGF_MAX_EOBJ];
+  for (int e = 0; e < E; ++e) {
+    double2 acc = make_double2(0.0, 0.0);
+    if (lane < k) acc = cadd(acc, cmul(M.r(e, s_l), z));
+    for (int o = 16; o; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    eo[e] = csub(M.r(e, n), acc);
+  }
+  if (lane == 0) {
     for (int e = 0; e < E; ++e) new_eobj[cf * E + e] = eo[e];
     double pf[3];
     double F = objective_term(eo, E, fconst[f], oc, pf);
@@ -728,16 +884,44 @@ static size_t eval_smem(int kmax) {
   return sizeof(double2) * ((size_t)kmax * kmax + 2 * kmax) + sizeof(int) * kmax + kmax + 16;
 }
 
-template <typename TM> static cudaError_t launch_eval_t(Handle *h, int ncand) {
+template <typename TM, int NT> static cudaError_t launch_eval_cta(Handle *h, int ncand) {
   const int nf = h->cfg.num_freq;
   const size_t sm = eval_smem(h->kmax);
-  cudaError_t e = cudaFuncSetAttribute(k_eval<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t e = cudaFuncSetAttribute(k_eval<TM, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k_eval<TM><<<dim3(ncand, nf), 128, sm, h->stream>>>(
+  k_eval<TM, NT><<<dim3(ncand, nf), NT, sm, h->stream>>>(
       static_cast<const SV<TM> *>(h->d_views), reinterpret_cast<const double2 *const *>(h->d_Eincs), h->n, h->E,
       h->kmax, h->d_es, h->d_ed, h->d_ek, h->d_fconst, obj_const(h), nf, h->d_new_eobj, h->d_Ff, h->d_perf,
       h->d_status);
   return cudaGetLastError();
+}
+
+template <typename TM, int WPC> static cudaError_t launch_eval_warp(Handle *h, int ncand) {
+  const int nf = h->cfg.num_freq;
+  const size_t sm = sizeof(double2) * (size_t)WPC * (h->kmax | 1) * h->kmax;
+  cudaError_t e = cudaFuncSetAttribute(k_eval_warp<TM, WPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_eval_warp<TM, WPC><<<dim3((ncand + WPC - 1) / WPC, nf), 32 * WPC, sm, h->stream>>>(
+      static_cast<const SV<TM> *>(h->d_views), reinterpret_cast<const double2 *const *>(h->d_Eincs), h->n, h->E,
+      h->kmax, ncand, h->d_es, h->d_ed, h->d_ek, h->d_fconst, obj_const(h), nf, h->d_new_eobj, h->d_Ff, h->d_perf,
+      h->d_status);
+  return cudaGetLastError();
+}
+
+bool eval_variant_ok(const Handle *h, int v) {
+  if (v < 0 || v >= kEvalVariants) return false;
+  return kEvalForms[v].cands_per_cta == 1 || h->kmax <= 32;
+}
+
+template <typename TM> static cudaError_t launch_eval_t(Handle *h, int ncand) {
+  switch (eval_variant_ok(h, h->eval_variant) ? h->eval_variant : 0) {
+    case 1: return launch_eval_cta<TM, 64>(h, ncand);
+    case 2: return launch_eval_cta<TM, 256>(h, ncand);
+    case 3: return launch_eval_warp<TM, 2>(h, ncand);
+    case 4: return launch_eval_warp<TM, 4>(h, ncand);
+    case 5: return launch_eval_warp<TM, 8>(h, ncand);
+    default: return launch_eval_cta<TM, 128>(h, ncand);
+  }
 }
 
 cudaError_t launch_eval(Handle *h, int ncand, double F_best) {

@@ -17,6 +17,14 @@ constexpr int kMaxEvalK = 104;
 // Edges accepted per chunk when M is built from G for a design.
 constexpr int kInitChunk = 96;
 
+// Forms of the candidate kernel the autotuner chooses from: warps working on
+// one (candidate, frequency) and candidates per CTA. Index 0 is the default.
+struct EvalForm {
+  int warps_per_cand, cands_per_cta;
+};
+constexpr int kEvalVariants = 6;
+constexpr EvalForm kEvalForms[kEvalVariants] = {{4, 1}, {2, 1}, {8, 1}, {1, 2}, {1, 4}, {1, 8}};
+
 struct FreqConst {   // per-frequency scalars used by the objective
   double2 vinc, ln1, ln2;
   double k0;
@@ -61,6 +69,8 @@ struct Handle {
   long a16_rows = 0, b16_rows = 0;
   bool f64tc = false;                       // FP64 updates of up to f64tc_max_k() edges on tensor cores
   int init_chunk = kInitChunk;
+  int eval_variant = 0;                     // index into kEvalForms (set by the autotuner)
+  int c64_cols = 128;                       // output tile width of the complex64 update (64 or 128)
   std::vector<FreqConst> h_fconst;
 
   // design
@@ -160,6 +170,8 @@ cudaError_t launch_init_M(Handle *h, int f);
 cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const int *d_nflip);
 // Candidate evaluation + objective at every frequency, then the score.
 cudaError_t launch_eval(Handle *h, int ncand, double F_best);
+// Whether kEvalForms[v] applies to the handle (warp forms need kmax <= 32).
+bool eval_variant_ok(const Handle *h, int v);
 // Objective of the current design (from M's Eobj entries) into d_F[0].
 cudaError_t launch_current_objective(Handle *h);
 // Rank-k accept of an explicit edge list (device arrays s, d of length k) at

@@ -25,6 +25,8 @@ F64_TENSOR, F64_SIMT = 0, 1
 DBS_SYMMETRIC, DBS_SINGLE = 0, 1
 INIT_EMPTY, INIT_RANDOM = 0, 1
 MAX_FREQ = 16
+TUNE_MAX = 8
+BUILD_FP64, BUILD_C64 = 0, 1
 
 
 class PngfError(RuntimeError):
@@ -37,7 +39,8 @@ class Config(C.Structure):
     _fields_ = [("tiles_x", C.c_int), ("tiles_y", C.c_int), ("cells_x", C.c_int), ("cells_y", C.c_int),
                 ("num_eobj", C.c_int), ("max_flips", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
                 ("dz", C.c_double), ("num_freq", C.c_int), ("freq_hz", C.c_double * MAX_FREQ),
-                ("precision", C.c_int), ("defer_rank", C.c_int), ("device", C.c_int), ("fp64_update", C.c_int)]
+                ("precision", C.c_int), ("defer_rank", C.c_int), ("device", C.c_int), ("fp64_update", C.c_int),
+                ("c64_build", C.c_int)]
 
 
 class DbsParams(C.Structure):
@@ -61,6 +64,21 @@ class Timing(C.Structure):
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tune(C.Structure):
+    _fields_ = [("eval_form", C.c_int), ("eval_forms", C.c_int), ("warps_per_cand", C.c_int * TUNE_MAX),
+                ("cands_per_cta", C.c_int * TUNE_MAX), ("eval_us", C.c_double * TUNE_MAX), ("batch", C.c_int),
+                ("update_form", C.c_int), ("update_forms", C.c_int), ("update_cols", C.c_int * TUNE_MAX),
+                ("update_us", C.c_double * TUNE_MAX)]
+
+    def as_dict(self):
+        ne, nu = self.eval_forms, self.update_forms
+        return {"eval_form": self.eval_form, "batch": self.batch,
+                "eval": [{"warps_per_cand": self.warps_per_cand[i], "cands_per_cta": self.cands_per_cta[i],
+                          "us": self.eval_us[i]} for i in range(ne)],
+                "update_form": self.update_form,
+                "update": [{"cols": self.update_cols[i], "us": self.update_us[i]} for i in range(nu)]}
 
 
 _lib = None
@@ -99,6 +117,9 @@ def load():
         "pngf_eval_candidates_device": (I, [P, P, P, I, P, P, D, P]),
         "pngf_accept": (I, [P, I]),
         "pngf_drift_check": (I, [P, I, P]),
+        "pngf_drift_check_freq": (I, [P, I, I, P]),
+        "pngf_autotune": (I, [P, P]),
+        "pngf_set_eval_form": (I, [P, I]),
         "pngf_accept_edges_noalloc": (I, [P, L_, L_, I, P, P, P, I, P, P]),
         "pngf_refresh": (I, [P]),
         "pngf_timing_enable": (I, [P, I]),
@@ -169,7 +190,7 @@ class Handle:
     """Owns one pngf_handle (all frequencies of one DBS instance)."""
 
     def __init__(self, tiles_x, tiles_y, freqs, precision=PREC_FP64, max_flips=4, num_eobj=3, defer_rank=0,
-                 device=0, fp64_update=0):
+                 device=0, fp64_update=0, c64_build=0):
         L = load()
         self.L = L
         cfg = Config()
@@ -181,6 +202,7 @@ class Handle:
         cfg.defer_rank = defer_rank
         cfg.device = device
         cfg.fp64_update = fp64_update
+        cfg.c64_build = c64_build
         self.cfg = cfg
         self.nf = len(freqs)
         self.E = num_eobj
@@ -281,10 +303,27 @@ class Handle:
     def accept(self, c):
         self._chk(self.L.pngf_accept(self.h, c), "pngf_accept")
 
-    def drift_check(self, nrows=4):
+    def drift_check(self, nrows=4, f=None):
         r = C.c_double()
-        self._chk(self.L.pngf_drift_check(self.h, nrows, C.byref(r)), "pngf_drift_check")
+        if f is None:
+            self._chk(self.L.pngf_drift_check(self.h, nrows, C.byref(r)), "pngf_drift_check")
+        else:
+            self._chk(self.L.pngf_drift_check_freq(self.h, f, nrows, C.byref(r)), "pngf_drift_check_freq")
         return r.value
+
+    def refresh(self):
+        """Rebuilds the state for the current design from G in FP64."""
+        self._chk(self.L.pngf_refresh(self.h), "pngf_refresh")
+
+    def autotune(self):
+        """Times the kernel forms at the current design and keeps the fastest;
+        returns the chosen forms and the measured times (microseconds)."""
+        t = Tune()
+        self._chk(self.L.pngf_autotune(self.h, C.byref(t)), "pngf_autotune")
+        return t.as_dict()
+
+    def set_eval_form(self, form):
+        self._chk(self.L.pngf_set_eval_form(self.h, form), "pngf_set_eval_form")
 
 
 class Dbs:

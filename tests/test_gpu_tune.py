@@ -1,0 +1,155 @@
+"""Candidate-kernel forms, the autotuner, the complex64 build and the
+per-frequency drift check.
+
+- Every form of the candidate kernel (CTA of 2, 4 or 8 warps per candidate;
+  one warp per candidate with 2, 4 or 8 candidates per CTA) returns
+  bit-identical F, newEobj and status, so the autotuner's choice changes
+  speed only. Warp forms are refused when a candidate can flip more than 32
+  edges.
+- pngf_autotune leaves the state bit-identical (the update is timed with zero
+  operands).
+- PNGF_BUILD_C64 (state built directly in complex64 on the tensor cores)
+  stays within 1e-5 of max|T| of the FP64-built state and within 1e-7
+  relative in F; a DBS run from it ends within 1e-3 of the FP64 run.
+- The per-frequency drift check reports exactly the all-frequency check's
+  value at each frequency."""
+import numpy as np
+import pytest
+
+from conftest import case_G
+
+pytestmark = pytest.mark.gpu
+
+
+def make(c, Gs, gobj, tm, prec, max_flips, **kw):
+    from pngf_gb300 import lib
+    a = c["tiles"]
+    mid = (a - 1) // 2
+    h = lib.Handle(a, a, c["freqs"], precision=prec, max_flips=max_flips, **kw)
+    for f, G in enumerate(Gs):
+        h.load_G(f, G, gobj[f])
+    h.set_tile_map(tm)
+    h.set_source_port(mid, mid, 1, 2)
+    h.prepare()
+    return h
+
+
+def bits(x):
+    return np.ascontiguousarray(x).view(np.uint64)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("max_flips", [1, 4])
+def test_eval_forms_bit_identical(prec, max_flips, cases, built_lib):
+    from pngf_gb300 import lib
+    c = cases["sym_9x9_f2_seed3"]
+    Gs, gobj = case_G(c, built_lib)
+    a = c["tiles"]
+    rng = np.random.default_rng(11)
+    tm = [int(v) for v in rng.integers(0, 2, a * a)]
+    h = make(c, Gs, gobj, tm, prec, max_flips)
+    mid = (a - 1) // 2
+    pool = [t for t in range(a * a) if t != mid * a + mid]
+    cands = [[int(t) for t in rng.choice(pool, size=max_flips, replace=False)] for _ in range(70)]
+    h.set_eval_form(0)
+    eo0, F0 = h.eval_candidates(cands)
+    assert np.isfinite(F0).all()
+    for form in range(1, 6):
+        warp = form >= 3
+        if warp and max_flips > 1:  # kmax = 96 > 32
+            with pytest.raises(lib.PngfError):
+                h.set_eval_form(form)
+            continue
+        h.set_eval_form(form)
+        eo, F = h.eval_candidates(cands)
+        assert np.array_equal(bits(F), bits(F0)), form
+        assert np.array_equal(bits(eo), bits(eo0)), form
+    h.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_autotune_keeps_state(prec, cases, built_lib):
+    c = cases["sym_9x9_f2_seed3"]
+    Gs, gobj = case_G(c, built_lib)
+    a = c["tiles"]
+    rng = np.random.default_rng(5)
+    tm = [int(v) for v in rng.integers(0, 2, a * a)]
+    h = make(c, Gs, gobj, tm, prec, 1)
+    before = [h.get_M(f)[0] for f in range(len(Gs))]
+    t = h.autotune()
+    assert 0 <= t["eval_form"] < len(t["eval"]) and t["batch"] == a * a
+    assert t["eval"][t["eval_form"]]["us"] > 0
+    assert all(e["us"] > 0 for e in t["eval"])  # kmax = 24: every form applies
+    if prec == 1:
+        assert len(t["update"]) == 2 and all(u["us"] > 0 for u in t["update"])
+    for f in range(len(Gs)):
+        assert np.array_equal(bits(h.get_M(f)[0]), bits(before[f]))
+    cands = [[t_] for t_ in range(a * a) if t_ != ((a - 1) // 2) * (a + 1)]
+    _, F1 = h.eval_candidates(cands)
+    h.set_eval_form(0)
+    _, F0 = h.eval_candidates(cands)
+    assert np.array_equal(bits(F1), bits(F0))
+    h.close()
+
+
+def test_c64_build_matches_fp64_build(cases, built_lib):
+    from pngf_gb300 import lib
+    c = cases["sym_9x9_f2_seed3"]
+    Gs, gobj = case_G(c, built_lib)
+    a = c["tiles"]
+    rng = np.random.default_rng(3)
+    tm = [int(v) for v in rng.integers(0, 2, a * a)]
+    ha = make(c, Gs, gobj, tm, lib.PREC_C64, 1)
+    hb = make(c, Gs, gobj, tm, lib.PREC_C64, 1, c64_build=lib.BUILD_C64)
+    n = ha.n
+    for f in range(len(Gs)):
+        Ma, _ = ha.get_M(f)
+        Mb, _ = hb.get_M(f)
+        scale = np.abs(Ma[:n, :n]).max()
+        assert np.abs(Mb[:n, :n] - Ma[:n, :n]).max() <= 1e-5 * scale
+    assert abs(hb.objective() - ha.objective()) <= 1e-7 * abs(ha.objective())
+    assert hb.drift_check(4) < 1e-5
+    # a refresh rebuilds in FP64: the state then equals the FP64-built one up to chunking
+    hb.refresh()
+    for f in range(len(Gs)):
+        Ma, _ = ha.get_M(f)
+        Mb, _ = hb.get_M(f)
+        assert np.abs(Mb[:n, :n] - Ma[:n, :n]).max() <= 1e-7 * np.abs(Ma[:n, :n]).max()
+    ha.close()
+    hb.close()
+
+
+def test_c64_build_dbs_reaches_fp64_objective(cases, built_lib):
+    from pngf_gb300 import lib
+    c = cases["single_11x11_f3_seed2"]
+    Gs, gobj = case_G(c, built_lib)
+    a = c["tiles"]
+    F = []
+    for prec, build in ((lib.PREC_FP64, 0), (lib.PREC_C64, lib.BUILD_C64)):
+        h = lib.Handle(a, a, c["freqs"], precision=prec, max_flips=1, c64_build=build)
+        for f, G in enumerate(Gs):
+            h.load_G(f, G, gobj[f])
+        d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=c["seed"], drift_every=16, drift_tol=1e-4)
+        s = d.run()
+        assert s.converged
+        F.append(s.F_best)
+        d.close()
+        h.close()
+    assert abs(F[1] - F[0]) <= 1e-3 * abs(F[0])
+
+
+def test_drift_check_per_frequency(cases, built_lib):
+    from pngf_gb300 import lib
+    c = cases["single_11x11_f3_seed2"]
+    Gs, gobj = case_G(c, built_lib)
+    a = c["tiles"]
+    rng = np.random.default_rng(9)
+    tm = [int(v) for v in rng.integers(0, 2, a * a)]
+    h = make(c, Gs, gobj, tm, lib.PREC_C64, 1)
+    allf = h.drift_check(3)
+    per = [h.drift_check(3, f=f) for f in range(len(Gs))]
+    assert max(per) == allf
+    assert 0 < allf < 1e-6  # only the complex64 rounding of T after the FP64 build
+    with pytest.raises(lib.PngfError):
+        h.drift_check(3, f=len(Gs))
+    h.close()
