@@ -64,8 +64,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", default="fp64,c64", help="precision forms to run; the first is the headline")
     ap.add_argument("--nfreq", type=int, default=5, help="use the first NFREQ of the five frequencies")
-    ap.add_argument("--converge", action="store_true",
-                    help="also time plain FP64 DBS to convergence against proposal + complex64 DBS")
+    ap.add_argument("--no-converge", action="store_true",
+                    help="skip the wall time to convergence, plain FP64 DBS against proposal + complex64 DBS")
+    ap.add_argument("--no-group", action="store_true", help="skip the many-instance group run")
+    ap.add_argument("--instances", type=int, default=64, help="group run: DBS instances")
+    ap.add_argument("--group-evals", type=int, default=400, help="group run: flip evaluations per instance")
+    ap.add_argument("--group-batch", type=int, default=64, help="group run: speculative batch per instance")
     return ap.parse_args()
 
 
@@ -287,9 +291,12 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0)
+    torch.cuda.synchronize()
+    t_prep = time.perf_counter() - t0
     s = d.run()
     torch.cuda.synchronize()
-    out["plain_fp64"] = {"wall_s": time.perf_counter() - t0, "F_final": s.F_best, "F_init": s.F_init,
+    out["plain_fp64"] = {"wall_s": time.perf_counter() - t0, "prepare_s": t_prep, "F_final": s.F_best,
+                         "F_init": s.F_init,
                          "evals": s.evals, "accepts": s.accepts, "converged": bool(s.converged),
                          "eval_form": tune64["eval_form"]}
     F_target = s.F_best * (1.0 + 1e-3)
@@ -319,6 +326,9 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
     t0 = time.perf_counter()
     d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0, drift_every=32, drift_tol=1e-4)
     lib.dbs_set_proposal(d, prop, topk=topk, train_every=8, train_steps=20, train_batch=32, lr=1e-3)
+    torch.cuda.synchronize()
+    t_prep = time.perf_counter() - t0
+    h.timing_enable(True)
     t_reach = None
     while True:
         d.step()
@@ -331,7 +341,10 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
             break
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
-    out["proposal_c64"] = {"wall_s_to_target": t_reach, "wall_s": wall, "F_final": s.F_best, "evals": s.evals,
+    tmp = h.timing()
+    out["proposal_c64"] = {"wall_s_to_target": t_reach, "wall_s": wall, "prepare_s": t_prep,
+                           "device_ms": {k: tmp[k] for k in ("eval_ms", "accept_ms", "update_ms")},
+                           "F_final": s.F_best, "evals": s.evals,
                            "accepts": s.accepts, "prop_hits": s.prop_hits, "full_passes": s.full_passes,
                            "converged": bool(s.converged), "drift_max": s.drift_max,
                            "drift_checks": s.drift_checks, "refreshes": s.refreshes,
@@ -346,6 +359,98 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
     prop.close()
     h.close()
     torch.cuda.empty_cache()
+    return out
+
+
+FREQS_GROUP = [28.0e9, 30.0e9, 32.0e9]
+
+
+def group_member(tiles, seed, max_evals, batch, local):
+    """One instance of the group workload: complex64 state built on the tensor
+    cores, G generated on the device and not kept (state_only), single-tile
+    DBS from the 50%-fill design of `seed`, its kernel forms autotuned."""
+    from pngf_gb300 import lib
+    h = lib.Handle(tiles, tiles, FREQS_GROUP, precision=lib.PREC_C64, max_flips=1, device=local,
+                   c64_build=lib.BUILD_C64, state_only=1)
+    for f in range(len(FREQS_GROUP)):
+        h.load_G_synth(f, seed=seed)
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, max_evals=max_evals, batch=batch)
+    h.autotune()
+    return h, d
+
+
+def group_bench(a, local, n_check=8):
+    """Many independent DBS instances on one GPU: tile grids drawn uniformly
+    from 11x11..31x31 (seeded), 3 frequencies, complex64, 50%-fill designs from
+    seeds 1..I, each run for a fixed budget of flip evaluations. All instances
+    step together as one group (one CUDA graph launch per round for every
+    instance's batch; accepts run concurrently on the instances' streams).
+    The first n_check instances are also run one after another with
+    pngf_dbs_step, and their logs are compared with the group's (equivalence)
+    and their times with a group of the same n_check (speed-up)."""
+    import torch
+    from pngf_gb300 import lib
+    rng = np.random.default_rng(2024)
+    sizes = [int(v) for v in rng.integers(11, 32, a.instances)]
+    out = {"instances": a.instances, "tiles": sizes, "freqs_ghz": [f / 1e9 for f in FREQS_GROUP],
+           "evals_per_instance": a.group_evals, "batch": a.group_batch}
+
+    def logs_of(runs):
+        return [(d.log(), d.stats().F_best) for _, d in runs]
+
+    def close(runs):
+        for h, d in runs:
+            d.close()
+            h.close()
+        torch.cuda.empty_cache()
+
+    # equivalence and speed-up on the first n_check instances
+    nc = min(n_check, a.instances)
+    runs = [group_member(sizes[i], i + 1, a.group_evals, a.group_batch, local) for i in range(nc)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _, d in runs:
+        d.run()
+    torch.cuda.synchronize()
+    t_seq = time.perf_counter() - t0
+    seq_logs = logs_of(runs)
+    close(runs)
+    runs = [group_member(sizes[i], i + 1, a.group_evals, a.group_batch, local) for i in range(nc)]
+    g = lib.Group([d for _, d in runs], use_graphs=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.run()
+    torch.cuda.synchronize()
+    t_grp = time.perf_counter() - t0
+    same = all(np.array_equal(l1["tile"], l0["tile"]) and np.array_equal(l1["accept"], l0["accept"]) and
+               np.array_equal(l1["F"].view(np.uint64), l0["F"].view(np.uint64)) and F1 == F0
+               for (l0, F0), (l1, F1) in zip(seq_logs, logs_of(runs)))
+    g.close()
+    close(runs)
+    out["check"] = {"instances": nc, "sequential_s": t_seq, "group_s": t_grp, "speedup": t_seq / t_grp,
+                    "logs_identical": bool(same)}
+    # the whole group
+    free0 = torch.cuda.mem_get_info(local)[0]
+    t0 = time.perf_counter()
+    runs = [group_member(sizes[i], i + 1, a.group_evals, a.group_batch, local) for i in range(a.instances)]
+    torch.cuda.synchronize()
+    out["setup_s"] = time.perf_counter() - t0
+    out["device_gb_held"] = (free0 - torch.cuda.mem_get_info(local)[0]) / 1e9
+    out["edges_total"] = int(sum(h.n for h, _ in runs))
+    g = lib.Group([d for _, d in runs], use_graphs=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = g.run()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    evals = sum(d.stats().evals for _, d in runs)
+    accepts = sum(d.stats().accepts for _, d in runs)
+    out.update({"wall_s": wall, "flip_evals": evals, "accepts": accepts, "flip_evals_per_s": evals / wall,
+                "accepted_updates_per_s": accepts / wall, "rounds": st["rounds"],
+                "graph_launches": st["graph_launches"], "graph_captures": st["captures"],
+                "kernel_launches": st["kernel_launches"]})
+    g.close()
+    close(runs)
     return out
 
 
@@ -383,8 +488,9 @@ def gpu_arm(a, world, rank, local):
     if "c64" in forms:
         r32 = run_form(a, lib.PREC_C64, Gs, rank, local, dist)
         c64_red = reduce_form(r32, dist)
-    conv = converge_compare(a, Gs, local) if (a.converge and rank == 0) else None
+    conv = converge_compare(a, Gs, local) if (not a.no_converge and rank == 0) else None
     del Gs
+    grp = group_bench(a, local) if (not a.no_group and rank == 0) else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -493,6 +599,8 @@ def gpu_arm(a, world, rank, local):
         }
     if conv is not None:
         line["converge"] = conv
+    if grp is not None:
+        line["group"] = grp
     if world == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(a.tiles, a.mode, a.seed, FREQS[0], r64["evals"],
                                                    r64["accepts"], nf)

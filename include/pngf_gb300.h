@@ -70,7 +70,17 @@ typedef struct pngf_config {
   int device;            /* CUDA device ordinal */
   int fp64_update;       /* PNGF_PREC_FP64: PNGF_F64_TENSOR (default) or PNGF_F64_SIMT */
   int c64_build;         /* PNGF_PREC_C64: PNGF_BUILD_FP64 (default) or PNGF_BUILD_C64, see below */
+  int state_only;        /* 1: between calls the device holds only the state (see below) */
 } pngf_config;
+
+/* state_only = 1 (no reference counterpart): G comes from the built-in
+ * synthetic generator (pngf_load_G_synth) and is regenerated on the device
+ * whenever a build (pngf_prepare, pngf_refresh) or a drift check needs it,
+ * instead of being kept; a PNGF_PREC_C64 handle also allocates its FP64
+ * staging of M only for those calls. Device memory between calls is then the
+ * state alone (complex64 T: 8 N^2 bytes per frequency), which is what lets many
+ * large instances share one GPU. pngf_load_G / pngf_load_G_file return
+ * PNGF_ERR_UNSUPPORTED on such a handle. */
 
 /* How pngf_prepare builds the state of a PNGF_PREC_C64 handle for a design:
  * PNGF_BUILD_FP64 - in FP64 (as a PNGF_PREC_FP64 handle does), then T is
@@ -134,6 +144,10 @@ int pngf_dims(const pngf_handle *h, long *n_edges, long *ld_m);
 int pngf_load_G(pngf_handle *h, int f, const double *G, long ldg, const double *gobj_rows);
 /* Same, from an acmefdfd G file. Missing or short file -> PNGF_ERR_IO. */
 int pngf_load_G_file(pngf_handle *h, int f, const char *path);
+/* No reference counterpart: frequency f's G is the synthetic G of
+ * pngf_synth_G (same recipe, generated on the device; entries agree with
+ * the host generator to ~1e-15 relative), with zero objective rows. */
+int pngf_load_G_synth(pngf_handle *h, int f, unsigned long long seed, double eps_r);
 
 /* Sets the design (PNGF_Optimizer::set_tile_map, pngfopt.hpp:669-674). */
 int pngf_set_tile_map(pngf_handle *h, const int *tile_map);
@@ -313,6 +327,34 @@ int pngf_dbs_log(const pngf_dbs *d, long cap, int *tile, int *accept, double *F,
 /* Writes the log in Logger::save's text format (logger.hpp:75-106). */
 int pngf_dbs_save_log(const pngf_dbs *d, const char *path);
 int pngf_dbs_end(pngf_dbs *d);
+
+/* ---- many DBS runs at once (no reference counterpart: the reference runs
+ * one design per process) ----
+ * A group steps independent DBS runs, each on its own handle (so its own
+ * stream and device state; sizes may differ), so that their batches and
+ * accepts overlap on the GPU. One pngf_group_step draws every unfinished
+ * member's next speculative batch and launches all their evaluations, as one
+ * CUDA graph when use_graphs is set (captured once and replayed while every
+ * member's batch size stays the same; a fixed pngf_dbs_params.batch keeps it
+ * so), then takes each member's decision exactly as pngf_dbs_step would and
+ * launches its accept without waiting. Each member's accepted flips,
+ * objectives and log equal those of stepping it alone with pngf_dbs_step.
+ * Members with an attached proposal network are refused. */
+typedef struct pngf_group pngf_group;
+typedef struct pngf_group_stats {
+  long rounds;          /* group steps that launched work */
+  long graph_launches;  /* CUDA graph launches (use_graphs) */
+  long captures;        /* graph (re)captures */
+  long kernel_launches; /* kernels launched by group steps (graph kernels counted per replay) */
+  long evals;           /* flip evaluations over all members */
+  long accepts;         /* accepts taken in group steps */
+} pngf_group_stats;
+int pngf_group_create(pngf_dbs *const *members, int count, int use_graphs, pngf_group **out);
+/* One round over the members; *active = members not finished afterwards. */
+int pngf_group_step(pngf_group *g, int *active);
+int pngf_group_stats_get(const pngf_group *g, pngf_group_stats *out);
+/* Frees the group (not its members). */
+int pngf_group_destroy(pngf_group *g);
 
 /* ---- learned proposals (no reference counterpart) ----
  * A 4-layer 3x3 convolutional network over the tile map (3 input channels:

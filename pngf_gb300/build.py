@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpngf_gb300.so")
 
 SOURCES = ["kernels_fp64.cu", "kernels_c64.cu", "kernels_f64tc.cu", "capi.cu", "dbs.cpp", "gfile.cpp", "noalloc.cu",
-           "proposal.cu"]
+           "proposal.cu", "synth.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "-I" + os.path.join(ROOT, "include")]
 
@@ -51,7 +51,7 @@ def build(verbose: bool = False) -> str:
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
     with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(_compile, srcs))
-    cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", LIB] + objs + ["-lgomp"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-Xlinker", "--no-undefined", "-o", LIB] + objs + ["-lgomp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

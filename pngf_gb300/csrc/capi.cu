@@ -171,47 +171,74 @@ static int check_tiles(Handle *h, const int *tiles, const int *nflip, int ncand)
 }
 
 // Evaluates a batch whose tile lists are already in h->d_tiles / h->d_nflip.
-static int eval_resident(Handle *h, int ncand, double F_best) {
-  cudaEvent_t t0 = timing_mark(h);
+// The score reads F_best from d_fbest when it is given (the form a CUDA graph
+// can replay with a new F_best), else takes it by value.
+static int eval_resident(Handle *h, int ncand, double F_best, const double *d_fbest = nullptr) {
+  cudaEvent_t t0 = h->capturing ? nullptr : timing_mark(h);
   PNGF_CUDA(h, launch_edge_lists(h, ncand, h->d_tiles, h->d_nflip));
-  PNGF_CUDA(h, launch_eval(h, ncand, F_best));
+  PNGF_CUDA(h, launch_eval(h, ncand, F_best, d_fbest));
   timing_close(h, t0, T_EVAL, (double)ncand * h->cfg.num_freq, 0.0, 0.0);
   h->batch_n = ncand;
   h->batch_valid = true;
   return PNGF_OK;
 }
 
-int eval_launch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best) {
+// Layout of the pinned result block of a batch of ncand: F, perf, new_eobj
+// (as doubles), then ints: first, ek, status, and the tensor-core error flag
+// (set by an earlier accept).
+struct OutLayout {
+  size_t nF, nperf, neo, nint;
+  double *F, *perf, *eo;
+  int *ints;
+  OutLayout(const Handle *h, int ncand)
+      : nF(ncand), nperf((size_t)ncand * h->cfg.num_freq * 3), neo((size_t)ncand * h->cfg.num_freq * h->E * 2),
+        nint(2 + (size_t)ncand + (size_t)ncand * h->cfg.num_freq) {
+    F = h->h_out;
+    perf = F ? F + nF : nullptr;
+    eo = F ? perf + nperf : nullptr;
+    ints = F ? reinterpret_cast<int *>(eo + neo) : nullptr;
+  }
+  size_t doubles() const { return nF + nperf + neo + nint; }
+};
+
+int eval_stage(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best) {
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "pngf_prepare has not been called for this design");
   if (ncand <= 0) return set_error(h, PNGF_ERR_ARG, "ncand must be positive");
   int rc;
   if ((rc = check_tiles(h, tiles, nflip, ncand))) return rc;
   if ((rc = ensure_cand_cap(h, ncand))) return rc;
+  if ((rc = ensure_host_out(h, OutLayout(h, ncand).doubles()))) return rc;
   const int mf = h->cfg.max_flips, nf = h->cfg.num_freq;
   std::memcpy(h->h_tiles, tiles, sizeof(int) * (size_t)ncand * mf);
   std::memcpy(h->h_nflip, nflip, sizeof(int) * (size_t)ncand);
+  *h->h_fbest = F_best;
+  h->batch_tiles.assign(tiles, tiles + (size_t)ncand * mf);
+  h->batch_nflip.assign(nflip, nflip + ncand);
+  const OutLayout o(h, ncand);
+  o.ints[1 + ncand + (size_t)ncand * nf] = 0;
+  h->staged_n = ncand;
+  return PNGF_OK;
+}
+
+int eval_enqueue(Handle *h) {
+  const int ncand = h->staged_n, mf = h->cfg.max_flips, nf = h->cfg.num_freq;
+  if (ncand <= 0) return set_error(h, PNGF_ERR_STATE, "no staged batch");
   PNGF_CUDA(h, cudaMemcpyAsync(h->d_tiles, h->h_tiles, sizeof(int) * (size_t)ncand * mf, cudaMemcpyHostToDevice,
                                h->stream));
   PNGF_CUDA(h, cudaMemcpyAsync(h->d_nflip, h->h_nflip, sizeof(int) * (size_t)ncand, cudaMemcpyHostToDevice,
                                h->stream));
-  if ((rc = eval_resident(h, ncand, F_best))) return rc;
-  h->batch_tiles.assign(tiles, tiles + (size_t)ncand * mf);
-  h->batch_nflip.assign(nflip, nflip + ncand);
-  // One pinned block: F, perf, new_eobj (as doubles), then ints: first, ek,
-  // status, and the tensor-core error flag (set by an earlier accept).
-  const size_t nF = ncand, nperf = (size_t)ncand * nf * 3, neo = (size_t)ncand * nf * h->E * 2;
-  const size_t nint = 2 + (size_t)ncand + (size_t)ncand * nf;
-  if ((rc = ensure_host_out(h, nF + nperf + neo + nint))) return rc;
-  double *hF = h->h_out, *hperf = hF + nF, *heo = hperf + nperf;
-  int *hint = reinterpret_cast<int *>(heo + neo);
-  PNGF_CUDA(h, cudaMemcpyAsync(hF, h->d_F, sizeof(double) * nF, cudaMemcpyDeviceToHost, h->stream));
-  PNGF_CUDA(h, cudaMemcpyAsync(hperf, h->d_perf, sizeof(double) * nperf, cudaMemcpyDeviceToHost, h->stream));
-  PNGF_CUDA(h, cudaMemcpyAsync(heo, h->d_new_eobj, sizeof(double) * neo, cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(h->d_fbest, h->h_fbest, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int rc;
+  if ((rc = eval_resident(h, ncand, 0.0, h->d_fbest))) return rc;
+  const OutLayout o(h, ncand);
+  PNGF_CUDA(h, cudaMemcpyAsync(o.F, h->d_F, sizeof(double) * o.nF, cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(o.perf, h->d_perf, sizeof(double) * o.nperf, cudaMemcpyDeviceToHost, h->stream));
+  PNGF_CUDA(h, cudaMemcpyAsync(o.eo, h->d_new_eobj, sizeof(double) * o.neo, cudaMemcpyDeviceToHost, h->stream));
+  int *hint = o.ints;
   PNGF_CUDA(h, cudaMemcpyAsync(hint, h->d_first, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   PNGF_CUDA(h, cudaMemcpyAsync(hint + 1, h->d_ek, sizeof(int) * ncand, cudaMemcpyDeviceToHost, h->stream));
   PNGF_CUDA(h, cudaMemcpyAsync(hint + 1 + ncand, h->d_status, sizeof(int) * ncand * nf, cudaMemcpyDeviceToHost,
                                h->stream));
-  hint[1 + ncand + (size_t)ncand * nf] = 0;
   if (h->d_tc_err)
     PNGF_CUDA(h, cudaMemcpyAsync(hint + 1 + ncand + (size_t)ncand * nf, h->d_tc_err, sizeof(int),
                                  cudaMemcpyDeviceToHost, h->stream));
@@ -219,14 +246,20 @@ int eval_launch(Handle *h, const int *tiles, const int *nflip, int ncand, double
   return PNGF_OK;
 }
 
+int eval_launch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best) {
+  int rc = eval_stage(h, tiles, nflip, ncand, F_best);
+  if (rc) return rc;
+  return eval_enqueue(h);
+}
+
 int eval_collect(Handle *h, EvalOut *out) {
   const int ncand = h->launched_n, mf = h->cfg.max_flips, nf = h->cfg.num_freq;
   if (ncand <= 0) return set_error(h, PNGF_ERR_STATE, "no batch in flight");
   h->launched_n = 0;
-  const size_t nF = ncand, nperf = (size_t)ncand * nf * 3, neo = (size_t)ncand * nf * h->E * 2;
-  const size_t nint = 2 + (size_t)ncand + (size_t)ncand * nf;
-  double *hF = h->h_out, *hperf = hF + nF, *heo = hperf + nperf;
-  int *hint = reinterpret_cast<int *>(heo + neo);
+  const OutLayout o(h, ncand);
+  const size_t nF = o.nF, nperf = o.nperf, neo = o.neo, nint = o.nint;
+  const double *hF = o.F, *hperf = o.perf, *heo = o.eo;
+  const int *hint = o.ints;
   PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
   const int tc = hint[1 + ncand + (size_t)ncand * nf];
   if (tc != 0) {
@@ -366,6 +399,9 @@ int pngf_destroy(pngf_handle *ph) {
   dfree(h->d_piv);
   dfree(h->d_z);
   dfree(h->d_acc_status);
+  dfree(h->d_colmax);
+  dfree(h->d_fbest);
+  if (h->h_fbest) cudaFreeHost(h->h_fbest);
   if (h->h_tiles) cudaFreeHost(h->h_tiles);
   if (h->h_nflip) cudaFreeHost(h->h_nflip);
   if (h->h_out) cudaFreeHost(h->h_out);
@@ -384,6 +420,7 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
     return PNGF_ERR_ARG;
   if (c.precision != PNGF_PREC_FP64 && c.precision != PNGF_PREC_C64) return PNGF_ERR_ARG;
   if (c.c64_build != PNGF_BUILD_FP64 && c.c64_build != PNGF_BUILD_C64) return PNGF_ERR_ARG;
+  if (c.state_only != 0 && c.state_only != 1) return PNGF_ERR_ARG;
   const int kmax = c.max_flips * edges_per_tile(c);
   if (kmax > kMaxEvalK) return PNGF_ERR_UNSUPPORTED;
   int ndev = 0;
@@ -426,8 +463,10 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
   std::vector<void *> einc(c.num_freq);
   for (int f = 0; f < c.num_freq; ++f) {
     Freq &q = h->f[f];
-    if ((rc = dalloc(h, &q.G, (size_t)n * n)) || (rc = dalloc(h, &q.gobj, (size_t)std::max(1, h->E - 1) * n)) ||
-        (rc = dalloc(h, &q.Einc, (size_t)n)) || (rc = dalloc(h, &q.M64, (size_t)rows * h->ldm)))
+    // state_only: G (and a complex64 handle's FP64 staging of M) exist only while a build or check runs
+    if ((!c.state_only && (rc = dalloc(h, &q.G, (size_t)n * n))) ||
+        (rc = dalloc(h, &q.gobj, (size_t)std::max(1, h->E - 1) * n)) || (rc = dalloc(h, &q.Einc, (size_t)n)) ||
+        (!(c.state_only && c64) && (rc = dalloc(h, &q.M64, (size_t)rows * h->ldm))))
       return fail(rc);
     if (c64 && ((rc = dalloc(h, &q.T32, (size_t)n * h->ldm)) || (rc = dalloc(h, &q.y64, (size_t)n)) ||
                 (rc = dalloc(h, &q.R64, (size_t)h->E * h->ldm))))
@@ -472,12 +511,14 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
       (rc = dalloc(h, &h->d_W, (size_t)h->acc_cap * h->ldm)) || (rc = dalloc(h, &h->d_acc_s, (size_t)n)) ||
       (rc = dalloc(h, &h->d_acc_d, (size_t)n)) || (rc = dalloc(h, &h->d_LU, (size_t)h->acc_cap * h->acc_cap)) ||
       (rc = dalloc(h, &h->d_piv, (size_t)h->acc_cap)) || (rc = dalloc(h, &h->d_z, (size_t)h->acc_cap)) ||
-      (rc = dalloc(h, &h->d_acc_status, 1)))
+      (rc = dalloc(h, &h->d_acc_status, 1)) || (rc = dalloc(h, &h->d_colmax, (size_t)n)) ||
+      (rc = dalloc(h, &h->d_fbest, 1)))
     return fail(rc);
   if (cudaMemcpy(h->d_Eincs, einc.data(), sizeof(void *) * c.num_freq, cudaMemcpyHostToDevice) != cudaSuccess ||
       setup_views(h) != cudaSuccess)
     return fail(PNGF_ERR_CUDA);
   if ((rc = ensure_cand_cap(h, 64))) return fail(rc);
+  if (cudaMallocHost(&h->h_fbest, sizeof(double)) != cudaSuccess) return fail(PNGF_ERR_NOMEM);
   *out = reinterpret_cast<pngf_handle *>(h);
   return PNGF_OK;
 }
@@ -502,6 +543,8 @@ int pngf_load_G(pngf_handle *ph, int f, const double *G, long ldg, const double 
   Handle *h = H(ph);
   if (!h) return PNGF_ERR_ARG;
   if (f < 0 || f >= h->cfg.num_freq || !G || ldg < h->n) return set_error(h, PNGF_ERR_ARG, "pngf_load_G: bad argument");
+  if (h->cfg.state_only)
+    return set_error(h, PNGF_ERR_UNSUPPORTED, "a state_only handle takes G from pngf_load_G_synth");
   Freq &q = h->f[f];
   const long n = h->n;
   PNGF_CUDA(h, cudaMemcpy2DAsync(q.G, sizeof(double2) * n, G, sizeof(double2) * ldg, sizeof(double2) * n, n,
@@ -513,6 +556,23 @@ int pngf_load_G(pngf_handle *ph, int f, const double *G, long ldg, const double 
     else
       PNGF_CUDA(h, cudaMemsetAsync(q.gobj, 0, sizeof(double2) * (size_t)(h->E - 1) * n, h->stream));
   }
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  q.loaded = true;
+  h->prepared = false;
+  return PNGF_OK;
+}
+
+int pngf_load_G_synth(pngf_handle *ph, int f, unsigned long long seed, double eps_r) {
+  Handle *h = H(ph);
+  if (!h) return PNGF_ERR_ARG;
+  if (f < 0 || f >= h->cfg.num_freq || !(eps_r > 0.0))
+    return set_error(h, PNGF_ERR_ARG, "pngf_load_G_synth: bad argument");
+  Freq &q = h->f[f];
+  q.synth = true;
+  q.synth_seed = seed;
+  q.synth_eps = eps_r;
+  if (h->E > 1) PNGF_CUDA(h, cudaMemsetAsync(q.gobj, 0, sizeof(double2) * (size_t)(h->E - 1) * h->n, h->stream));
+  if (!h->cfg.state_only) PNGF_CUDA(h, launch_synth_G(h, f, q.G, h->n, h->d_colmax));
   PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
   q.loaded = true;
   h->prepared = false;
@@ -575,6 +635,31 @@ int pngf_set_source_port(pngf_handle *ph, int tile_x, int tile_y, int y_offset, 
   return PNGF_OK;
 }
 
+// state_only handles: frequency f's G (regenerated; need_G) and, for a
+// complex64 handle, its FP64 staging of M (need_M64) exist on the device
+// only between stage_in and stage_out. No-ops otherwise.
+static int stage_in(Handle *h, int f, bool need_G, bool need_M64) {
+  if (!h->cfg.state_only) return PNGF_OK;
+  Freq &q = h->f[f];
+  int rc;
+  if (need_G) {
+    if ((rc = dalloc(h, &q.G, (size_t)h->n * h->n))) return rc;
+    PNGF_CUDA(h, launch_synth_G(h, f, q.G, h->n, h->d_colmax));
+  }
+  if (need_M64 && h->cfg.precision == PNGF_PREC_C64 &&
+      (rc = dalloc(h, &q.M64, (size_t)(h->n + h->E) * h->ldm)))
+    return rc;
+  return PNGF_OK;
+}
+
+static void stage_out(Handle *h, int f) {
+  if (!h->cfg.state_only) return;
+  Freq &q = h->f[f];
+  cudaStreamSynchronize(h->stream);
+  dfree(q.G);
+  if (h->cfg.precision == PNGF_PREC_C64) dfree(q.M64);
+}
+
 // Builds the state for the current design from G. fp64: in FP64 (then T is
 // rounded for a complex64 handle); else directly in complex64.
 static int prepare_impl(Handle *h, bool fp64) {
@@ -594,7 +679,7 @@ static int prepare_impl(Handle *h, bool fp64) {
   }
   PNGF_CUDA(h, cudaMemsetAsync(h->d_acc_status, 0, sizeof(int), h->stream));
   const bool c64 = h->cfg.precision == PNGF_PREC_C64;
-  for (int f = 0; f < h->cfg.num_freq; ++f) {
+  auto build = [&](int f) -> int {
     PNGF_CUDA(h, launch_init_M(h, f));
     if (c64 && !fp64) PNGF_CUDA(h, launch_split_M(h, f));
     const int chunk = fp64 ? h->init_chunk : kInitChunk;
@@ -604,6 +689,13 @@ static int prepare_impl(Handle *h, bool fp64) {
                                        fp64 ? PNGF_PREC_FP64 : PNGF_PREC_C64));
     }
     if (c64 && fp64) PNGF_CUDA(h, launch_split_M(h, f));
+    return PNGF_OK;
+  };
+  for (int f = 0; f < h->cfg.num_freq; ++f) {
+    int rc = stage_in(h, f, true, true);
+    if (rc == PNGF_OK) rc = build(f);
+    stage_out(h, f);
+    if (rc) return rc;
   }
   int st = 0, tc = 0;
   PNGF_CUDA(h, cudaMemcpyAsync(&st, h->d_acc_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -664,13 +756,19 @@ int pngf_get_M(pngf_handle *ph, int f, double *M, long ld, double *einc) {
   if (!h || !M || f < 0 || f >= h->cfg.num_freq || ld < h->n + 1) return PNGF_ERR_ARG;
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
   const long rows = h->n + h->E;
-  if (h->cfg.precision == PNGF_PREC_C64) PNGF_CUDA(h, launch_merge_M(h, f));  // M64 is staging in this mode
-  PNGF_CUDA(h, cudaMemcpy2DAsync(M, sizeof(double2) * ld, h->f[f].M64, sizeof(double2) * h->ldm,
-                                 sizeof(double2) * (h->n + 1), rows, cudaMemcpyDeviceToHost, h->stream));
-  if (einc)
-    PNGF_CUDA(h, cudaMemcpyAsync(einc, h->f[f].Einc, sizeof(double2) * h->n, cudaMemcpyDeviceToHost, h->stream));
-  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
-  return PNGF_OK;
+  int rc = stage_in(h, f, false, true);
+  auto copy = [&]() -> int {
+    if (h->cfg.precision == PNGF_PREC_C64) PNGF_CUDA(h, launch_merge_M(h, f));  // M64 is staging in this mode
+    PNGF_CUDA(h, cudaMemcpy2DAsync(M, sizeof(double2) * ld, h->f[f].M64, sizeof(double2) * h->ldm,
+                                   sizeof(double2) * (h->n + 1), rows, cudaMemcpyDeviceToHost, h->stream));
+    if (einc)
+      PNGF_CUDA(h, cudaMemcpyAsync(einc, h->f[f].Einc, sizeof(double2) * h->n, cudaMemcpyDeviceToHost, h->stream));
+    PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+    return PNGF_OK;
+  };
+  if (rc == PNGF_OK) rc = copy();
+  stage_out(h, f);
+  return rc;
 }
 
 int pngf_eval_candidates(pngf_handle *ph, const int *tiles, const int *nflip, int ncand, double *new_eobj,
@@ -776,8 +874,15 @@ static int drift_impl(Handle *h, int f0, int f1, int nrows, double *max_rel) {
   if (e == cudaSuccess && !on.empty())
     e = cudaMemcpyAsync(h->d_acc_s, on.data(), sizeof(int) * on.size(), cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_out, 0, sizeof(unsigned long long) * 2 * h->cfg.num_freq, h->stream);
-  for (int f = f0; f < f1 && e == cudaSuccess; ++f)
+  for (int f = f0; f < f1 && e == cudaSuccess; ++f) {
+    if ((rc = stage_in(h, f, true, false))) {
+      stage_out(h, f);
+      release();
+      return rc;
+    }
     e = launch_drift_rows(h, f, d_rows, nrows, h->d_acc_s, (int)on.size(), X, PH, Rk, d_out + 2 * f);
+    stage_out(h, f);
+  }
   std::vector<unsigned long long> out(2 * h->cfg.num_freq);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(out.data(), d_out, sizeof(unsigned long long) * out.size(), cudaMemcpyDeviceToHost, h->stream);

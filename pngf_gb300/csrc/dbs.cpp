@@ -86,6 +86,12 @@ struct pngf_dbs {
   int topk = 0, train_every = 0, train_steps = 0, train_batch = 32;
   float train_lr = 1e-3f;
   long prop_steps = 0, prop_hits = 0, full_passes = 0;
+  // the batch being evaluated: hat state at its start, its draws, staging
+  Hat pend_hat{1, 1};
+  int pend_last = -1;
+  std::vector<Cand> pend;
+  bool pend_exhausted = false;
+  std::vector<int> tiles, nflip;
 };
 
 extern "C" {
@@ -242,6 +248,101 @@ int proposal_step(pngf_dbs *d, int *accepted) {
   return PNGF_OK;
 }
 
+// First half of a DBS decision: draws the next speculative batch in hat
+// order (main.cpp:343-392) and stages it on the handle (eval_stage).
+// *have = false when the run is over (evaluation budget spent or hat empty).
+int batch_draw(pngf_dbs *d, bool *have) {
+  *have = false;
+  if (d->done) return PNGF_OK;
+  pngf::Handle *h = d->h;
+  const int mf = h->cfg.max_flips;
+  const long budget = d->p.max_evals > 0 ? d->p.max_evals - d->evals : std::numeric_limits<long>::max();
+  if (budget <= 0) {
+    d->done = true;
+    return PNGF_OK;
+  }
+  d->pend_hat = d->hat;
+  d->pend_last = d->last_tried;
+  int B = d->p.batch > 0 ? d->p.batch : std::max(1, d->hat.left());
+  B = (int)std::min<long>(B, budget);
+  d->pend.clear();
+  d->pend_exhausted = false;
+  while ((int)d->pend.size() < B) {
+    Cand c;
+    if (!next_candidate(d, &c)) {
+      d->pend_exhausted = true;
+      break;
+    }
+    d->pend.push_back(c);
+  }
+  if (d->pend.empty()) {
+    d->converged = d->done = true;
+    return PNGF_OK;
+  }
+  const int nc = (int)d->pend.size();
+  d->tiles.assign((size_t)nc * mf, 0);
+  d->nflip.resize(nc);
+  for (int i = 0; i < nc; ++i) {
+    d->nflip[i] = d->pend[i].nflip;
+    for (int t = 0; t < d->pend[i].nflip; ++t) d->tiles[(size_t)i * mf + t] = d->pend[i].tiles[t];
+  }
+  const int rc = pngf::eval_stage(h, d->tiles.data(), d->nflip.data(), nc, d->F_best);
+  if (rc) return rc;
+  d->launched += nc;
+  *have = true;
+  return PNGF_OK;
+}
+
+// Second half: reads the batch's results and takes the reference's decisions
+// in draw order against the same F_best (main.cpp:401-456): logs every draw
+// up to the first improving one, accepts it, restores the hat to the start of
+// the batch, replays it to just after that draw and refills it. Draws after it
+// were speculative. With sync_accept = false the accept's launches are not
+// waited for (their bounded-wait status is read with the next batch).
+int batch_finish(pngf_dbs *d, int *accepted, bool sync_accept) {
+  if (accepted) *accepted = 0;
+  pngf::Handle *h = d->h;
+  const int nf = h->cfg.num_freq;
+  pngf::EvalOut o;
+  int rc = pngf::eval_collect(h, &o);
+  if (rc) return rc;
+  const int nc = (int)d->pend.size();
+  if (d->prop && d->p.mode == PNGF_DBS_SINGLE) {  // every exact evaluation is a training pair
+    std::vector<int> tl(nc);
+    std::vector<double> gains(nc);
+    for (int i = 0; i < nc; ++i) {
+      tl[i] = d->pend[i].tiles[0];
+      gains[i] = o.F[i] - d->F_best;
+    }
+    if ((rc = pngf_prop_record(d->prop, tl.data(), gains.data(), nc))) return rc;
+  }
+  const int j = o.first;
+  const int upto = j >= 0 ? j : nc - 1;
+  for (int i = 0; i <= upto; ++i) {
+    for (int f = 0; f < nf; ++f)
+      if (o.status[(size_t)i * nf + f] == PNGF_ERR_ARG)
+        return pngf::set_error(h, PNGF_ERR_ARG, "invalid candidate produced by the driver");
+    log_row(d, d->pend[i], i == j, o.F[i], o.perf.data() + (size_t)i * nf * 3, nf);
+  }
+  d->evals += upto + 1;
+  if (j >= 0) {
+    if ((rc = pngf::accept_cand_async(h, j, o.k[j], sync_accept))) return rc;
+    d->F_best = o.F[j];
+    ++d->accepts;
+    d->hat = d->pend_hat;  // replay to just after draw j, then refill (main.cpp:455)
+    d->last_tried = d->pend_last;
+    for (int i = 0; i <= j; ++i) {
+      Cand c;
+      next_candidate(d, &c);
+    }
+    d->hat.reset();
+    if (accepted) *accepted = 1;
+    return drift_after_accept(d);
+  }
+  if (d->pend_exhausted) d->converged = d->done = true;
+  return PNGF_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -319,81 +420,17 @@ int pngf_dbs_begin(pngf_handle *ph, const pngf_dbs_params *p, pngf_dbs **out) {
 int pngf_dbs_step(pngf_dbs *d, int *accepted) {
   if (!d) return PNGF_ERR_ARG;
   if (accepted) *accepted = 0;
-  pngf::Handle *h = d->h;
-  const int nf = h->cfg.num_freq, mf = h->cfg.max_flips;
   if (d->prop && d->topk > 0) return d->done ? PNGF_OK : proposal_step(d, accepted);
   while (!d->done) {
-    long budget = d->p.max_evals > 0 ? d->p.max_evals - d->evals : std::numeric_limits<long>::max();
-    if (budget <= 0) {
-      d->done = true;
-      break;
-    }
-    // Draw a speculative batch in hat order.
-    const Hat hat0 = d->hat;
-    const int last0 = d->last_tried;
-    int B = d->p.batch > 0 ? d->p.batch : std::max(1, d->hat.left());
-    B = (int)std::min<long>(B, budget);
-    std::vector<Cand> cands;
-    cands.reserve(B);
-    bool exhausted = false;
-    while ((int)cands.size() < B) {
-      Cand c;
-      if (!next_candidate(d, &c)) {
-        exhausted = true;
-        break;
-      }
-      cands.push_back(c);
-    }
-    if (cands.empty()) {
-      d->converged = d->done = true;
-      break;
-    }
-    const int nc = (int)cands.size();
-    std::vector<int> tiles((size_t)nc * mf, 0), nflip(nc);
-    for (int i = 0; i < nc; ++i) {
-      nflip[i] = cands[i].nflip;
-      for (int t = 0; t < cands[i].nflip; ++t) tiles[(size_t)i * mf + t] = cands[i].tiles[t];
-    }
-    pngf::EvalOut o;
-    int rc = pngf::eval_batch(h, tiles.data(), nflip.data(), nc, d->F_best, &o);
-    if (rc) return rc;
-    d->launched += nc;
-    if (d->prop && d->p.mode == PNGF_DBS_SINGLE) {  // every exact evaluation is a training pair
-      std::vector<int> tl(nc);
-      std::vector<double> gains(nc);
-      for (int i = 0; i < nc; ++i) {
-        tl[i] = cands[i].tiles[0];
-        gains[i] = o.F[i] - d->F_best;
-      }
-      if ((rc = pngf_prop_record(d->prop, tl.data(), gains.data(), nc))) return rc;
-    }
-    const int j = o.first;
-    const int upto = j >= 0 ? j : nc - 1;
-    for (int i = 0; i <= upto; ++i) {
-      for (int f = 0; f < nf; ++f)
-        if (o.status[(size_t)i * nf + f] == PNGF_ERR_ARG)
-          return pngf::set_error(h, PNGF_ERR_ARG, "invalid candidate produced by the driver");
-      log_row(d, cands[i], i == j, o.F[i], o.perf.data() + (size_t)i * nf * 3, nf);
-    }
-    d->evals += upto + 1;
-    if (j >= 0) {
-      if ((rc = pngf::accept_cand(h, j, o.k[j]))) return rc;
-      d->F_best = o.F[j];
-      ++d->accepts;
-      // Replay the hat to just after draw j, then refill it (main.cpp:455).
-      d->hat = hat0;
-      d->last_tried = last0;
-      for (int i = 0; i <= j; ++i) {
-        Cand c;
-        next_candidate(d, &c);
-      }
-      d->hat.reset();
+    bool have = false;
+    int rc = batch_draw(d, &have);
+    if (rc || !have) return rc;
+    if ((rc = pngf::eval_enqueue(d->h))) return rc;
+    int acc = 0;
+    if ((rc = batch_finish(d, &acc, true))) return rc;
+    if (acc) {
       if (accepted) *accepted = 1;
-      return drift_after_accept(d);
-    }
-    if (exhausted) {
-      d->converged = d->done = true;
-      break;
+      return PNGF_OK;
     }
   }
   return PNGF_OK;
@@ -458,6 +495,207 @@ int pngf_dbs_save_log(const pngf_dbs *d, const char *path) {
 
 int pngf_dbs_end(pngf_dbs *d) {
   delete d;
+  return PNGF_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Groups of independent DBS runs stepped together (no reference counterpart).
+//
+// A group step draws every unfinished member's next speculative batch on the
+// host, then launches all their evaluations at once: with graphs on, as one
+// CUDA graph (captured from the members' streams, forked from and joined to
+// the group's stream) that is replayed while the members' batch sizes and
+// staging buffers stay the same, else as each member's launches on its own
+// stream. The group then reads every member's results and takes its decision
+// exactly as pngf_dbs_step does, launching the accept without waiting, so the
+// members' accept updates run concurrently on their streams while the host
+// draws the next batches. A member's flips, objectives and log are therefore
+// those of pngf_dbs_step on that member alone.
+
+struct pngf_group {
+  std::vector<pngf_dbs *> m;
+  bool graphs = false;
+  cudaStream_t s0 = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> ready, join;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<long> key;  // per member: batch size and staging addresses the graph was captured with
+  long graph_nodes_launches = 0;
+  pngf_group_stats st{};
+};
+
+namespace {
+
+void group_release(pngf_group *g) {
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  for (cudaEvent_t e : g->ready)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : g->join)
+    if (e) cudaEventDestroy(e);
+  if (g->fork) cudaEventDestroy(g->fork);
+  if (g->s0) cudaStreamDestroy(g->s0);
+  delete g;
+}
+
+int group_err(pngf_group *g, cudaError_t e, const char *what) {
+  return pngf::cuda_check(g->m[0]->h, e, what);
+}
+
+// Captures the staged batches of the members marked in `on` into one graph.
+int group_capture(pngf_group *g, const std::vector<char> &on) {
+  if (g->exec) {
+    cudaGraphExecDestroy(g->exec);
+    g->exec = nullptr;
+  }
+  cudaError_t e = cudaStreamBeginCapture(g->s0, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return group_err(g, e, "cudaStreamBeginCapture");
+  int rc = PNGF_OK;
+  long nl = 0;
+  e = cudaEventRecord(g->fork, g->s0);
+  for (size_t i = 0; i < g->m.size() && e == cudaSuccess && rc == PNGF_OK; ++i) {
+    if (!on[i]) continue;
+    pngf::Handle *h = g->m[i]->h;
+    if ((e = cudaStreamWaitEvent(h->stream, g->fork, 0)) != cudaSuccess) break;
+    const long l0 = h->nlaunch;
+    h->capturing = true;
+    rc = pngf::eval_enqueue(h);
+    h->capturing = false;
+    nl += h->nlaunch - l0;
+    if (rc == PNGF_OK && (e = cudaEventRecord(g->join[i], h->stream)) == cudaSuccess)
+      e = cudaStreamWaitEvent(g->s0, g->join[i], 0);
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e2 = cudaStreamEndCapture(g->s0, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return group_err(g, e, "graph capture of the members' batches");
+  g->graph_nodes_launches = nl;
+  ++g->st.captures;
+  return PNGF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pngf_group_create(pngf_dbs *const *members, int count, int use_graphs, pngf_group **out) {
+  if (!members || count <= 0 || !out) return PNGF_ERR_ARG;
+  *out = nullptr;
+  for (int i = 0; i < count; ++i) {
+    if (!members[i]) return PNGF_ERR_ARG;
+    if (members[i]->prop && members[i]->topk > 0)
+      return pngf::set_error(members[i]->h, PNGF_ERR_UNSUPPORTED, "proposal-driven runs are stepped on their own");
+    for (int j = 0; j < i; ++j)
+      if (members[j]->h == members[i]->h)
+        return pngf::set_error(members[i]->h, PNGF_ERR_ARG, "two group members share a handle");
+  }
+  pngf_group *g = new (std::nothrow) pngf_group();
+  if (!g) return PNGF_ERR_NOMEM;
+  g->m.assign(members, members + count);
+  g->graphs = use_graphs != 0;
+  g->ready.assign(count, nullptr);
+  g->join.assign(count, nullptr);
+  cudaError_t e = cudaStreamCreateWithFlags(&g->s0, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+  for (int i = 0; i < count && e == cudaSuccess; ++i) {
+    e = cudaEventCreateWithFlags(&g->ready[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g->join[i], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    const int rc = group_err(g, e, "group streams and events");
+    group_release(g);
+    return rc;
+  }
+  *out = g;
+  return PNGF_OK;
+}
+
+int pngf_group_step(pngf_group *g, int *active) {
+  if (!g) return PNGF_ERR_ARG;
+  const size_t nm = g->m.size();
+  std::vector<char> on(nm, 0);
+  std::vector<long> key(3 * nm, 0);
+  int rc, n_on = 0;
+  for (size_t i = 0; i < nm; ++i) {  // draw and stage every unfinished member's batch
+    bool have = false;
+    if ((rc = batch_draw(g->m[i], &have))) return rc;
+    on[i] = have;
+    n_on += have;
+    const pngf::Handle *h = g->m[i]->h;
+    if (have) {
+      key[3 * i] = h->staged_n;
+      key[3 * i + 1] = reinterpret_cast<long>(h->h_tiles);
+      key[3 * i + 2] = reinterpret_cast<long>(h->h_out);
+    }
+  }
+  if (n_on > 0) {
+    ++g->st.rounds;
+    if (g->graphs) {
+      if (key != g->key || !g->exec) {
+        if ((rc = group_capture(g, on))) return rc;
+        g->key = key;
+      }
+      cudaError_t e = cudaSuccess;
+      for (size_t i = 0; i < nm && e == cudaSuccess; ++i) {  // after each member's earlier accepts
+        if (!on[i]) continue;
+        if ((e = cudaEventRecord(g->ready[i], g->m[i]->h->stream)) == cudaSuccess)
+          e = cudaStreamWaitEvent(g->s0, g->ready[i], 0);
+      }
+      if (e == cudaSuccess) e = cudaGraphLaunch(g->exec, g->s0);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(g->s0);
+      if (e != cudaSuccess) return group_err(g, e, "graph launch of the members' batches");
+      ++g->st.graph_launches;
+      g->st.kernel_launches += g->graph_nodes_launches;
+      for (size_t i = 0; i < nm; ++i) {  // the host-side effects of eval_enqueue, for the replay
+        if (!on[i]) continue;
+        pngf::Handle *h = g->m[i]->h;
+        h->launched_n = h->batch_n = h->staged_n;
+        h->batch_valid = true;
+      }
+    } else {
+      for (size_t i = 0; i < nm; ++i) {
+        if (!on[i]) continue;
+        pngf::Handle *h = g->m[i]->h;
+        const long l0 = h->nlaunch;
+        if ((rc = pngf::eval_enqueue(h))) return rc;
+        g->st.kernel_launches += h->nlaunch - l0;
+      }
+    }
+    for (size_t i = 0; i < nm; ++i) {  // decisions, in member order
+      if (!on[i]) continue;
+      int acc = 0;
+      pngf::Handle *h = g->m[i]->h;
+      const long l0 = h->nlaunch;
+      if ((rc = batch_finish(g->m[i], &acc, false))) return rc;
+      g->st.kernel_launches += h->nlaunch - l0;
+      g->st.accepts += acc;
+    }
+  }
+  int left = 0;
+  for (size_t i = 0; i < nm; ++i) left += !g->m[i]->done;
+  if (active) *active = left;
+  return PNGF_OK;
+}
+
+int pngf_group_stats_get(const pngf_group *g, pngf_group_stats *out) {
+  if (!g || !out) return PNGF_ERR_ARG;
+  *out = g->st;
+  out->evals = 0;
+  for (const pngf_dbs *d : g->m) out->evals += d->evals;
+  return PNGF_OK;
+}
+
+int pngf_group_destroy(pngf_group *g) {
+  if (!g) return PNGF_OK;
+  for (pngf_dbs *d : g->m) cudaStreamSynchronize(d->h->stream);
+  group_release(g);
   return PNGF_OK;
 }
 

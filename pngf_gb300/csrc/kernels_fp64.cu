@@ -605,10 +605,12 @@ __global__ void __launch_bounds__(32 * WPC)
 
 // Sums F over frequencies in frequency order and finds the first candidate
 // with F < F_best (a NaN F never passes, as in the reference's compare).
-__global__ void k_score(int ncand, int nf, const double *__restrict__ Ff, double F_best, double *__restrict__ F,
-                        int *__restrict__ first) {
+// F_best is read from F_best_dev when that is not null.
+__global__ void k_score(int ncand, int nf, const double *__restrict__ Ff, double F_best,
+                        const double *__restrict__ F_best_dev, double *__restrict__ F, int *__restrict__ first) {
   __shared__ int s_first;
   if (threadIdx.x == 0) s_first = 0x7fffffff;
+  if (F_best_dev) F_best = *F_best_dev;
   __syncthreads();
   for (int c = threadIdx.x; c < ncand; c += blockDim.x) {
     double acc = 0.0;
@@ -924,14 +926,14 @@ template <typename TM> static cudaError_t launch_eval_t(Handle *h, int ncand) {
   }
 }
 
-cudaError_t launch_eval(Handle *h, int ncand, double F_best) {
+cudaError_t launch_eval(Handle *h, int ncand, double F_best, const double *d_fbest) {
   cudaError_t e;
   if (h->cfg.precision == PNGF_PREC_FP64)
     e = launch_eval_t<double2>(h, ncand);
   else
     e = launch_eval_t<float2>(h, ncand);
   if (e != cudaSuccess) return e;
-  k_score<<<1, 256, 0, h->stream>>>(ncand, h->cfg.num_freq, h->d_Ff, F_best, h->d_F, h->d_first);
+  k_score<<<1, 256, 0, h->stream>>>(ncand, h->cfg.num_freq, h->d_Ff, F_best, d_fbest, h->d_F, h->d_first);
   h->nlaunch += 2;
   return cudaGetLastError();
 }

@@ -40,6 +40,9 @@ struct Freq {
   double2 *y64 = nullptr;    // C64 mode: y (N) in FP64
   double2 *R64 = nullptr;    // C64 mode: R and Eobj (E x ldm row-major, Eobj at column N) in FP64
   bool loaded = false;
+  bool synth = false;        // G is the built-in synthetic G (generated on the device)
+  unsigned long long synth_seed = 0;
+  double synth_eps = 1.0;
 };
 
 struct Handle {
@@ -95,6 +98,9 @@ struct Handle {
   int *d_status = nullptr;                      // per-candidate LU status
   int batch_n = 0;
   int launched_n = 0;      // batch enqueued by eval_launch, not yet collected
+  int staged_n = 0;        // batch staged by eval_stage
+  bool capturing = false;  // stream work is being captured into a CUDA graph (no timing events)
+  double *h_fbest = nullptr, *d_fbest = nullptr;  // F_best of the staged batch (pinned / device)
   bool batch_valid = false;
   std::vector<int> batch_tiles, batch_nflip;
   std::vector<int> last_k, last_status;   // per-candidate edge count / status of the host-API batch
@@ -109,6 +115,7 @@ struct Handle {
   int *d_piv = nullptr;             // acc_cap
   double2 *d_z = nullptr;           // acc_cap
   int *d_acc_status = nullptr;
+  unsigned long long *d_colmax = nullptr;  // N words of scratch for the synthetic G generator
 
   // host staging (pinned)
   int *h_tiles = nullptr, *h_nflip = nullptr;
@@ -156,6 +163,12 @@ int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double 
 // handle's stream, then wait for them and parse.
 int eval_launch(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best);
 int eval_collect(Handle *h, EvalOut *out);
+// eval_launch split again: eval_stage validates the batch and copies it (and
+// F_best) into pinned host staging; eval_enqueue issues the stream work
+// (host-to-device copies from the staging, kernels, result copies), which a
+// CUDA graph can capture and replay after a new eval_stage of the same size.
+int eval_stage(Handle *h, const int *tiles, const int *nflip, int ncand, double F_best);
+int eval_enqueue(Handle *h);
 // Applies candidate c (k flipped edges) of the last batch at every frequency.
 int accept_cand(Handle *h, int c, int k);
 // Same; with check_now = false nothing waits for the GPU (the tensor-core
@@ -168,8 +181,9 @@ int accept_cand_async(Handle *h, int c, int k, bool check_now);
 cudaError_t launch_init_M(Handle *h, int f);
 // Per-candidate flipped-edge lists (sorted, deduplicated) from tile lists.
 cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const int *d_nflip);
-// Candidate evaluation + objective at every frequency, then the score.
-cudaError_t launch_eval(Handle *h, int ncand, double F_best);
+// Candidate evaluation + objective at every frequency, then the score
+// against F_best (read from d_fbest when it is not null).
+cudaError_t launch_eval(Handle *h, int ncand, double F_best, const double *d_fbest = nullptr);
 // Whether kEvalForms[v] applies to the handle (warp forms need kmax <= 32).
 bool eval_variant_ok(const Handle *h, int v);
 // Objective of the current design (from M's Eobj entries) into d_F[0].
@@ -194,6 +208,10 @@ cudaError_t launch_merge_M(Handle *h, int f);
 // max) max |T32 - T| and max |T| over those rows. d_P: the set edges (np).
 cudaError_t launch_drift_rows(Handle *h, int f, const int *d_rows, int nr, const int *d_P, int np, double2 *X,
                               double2 *PH, double2 *Rk, unsigned long long *d_out);
+// ---- synthetic G on the device (synth.cu) ----
+// Writes frequency f's synthetic G (n x n column-major, leading dimension ldg);
+// colmax: n scratch words.
+cudaError_t launch_synth_G(Handle *h, int f, double2 *G, long ldg, unsigned long long *colmax);
 // ---- FP64-accurate update on the tensor cores (kernels_f64tc.cu) ----
 int f64tc_max_k();
 size_t f64tc_op_cols();

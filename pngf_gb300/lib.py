@@ -40,7 +40,7 @@ class Config(C.Structure):
                 ("num_eobj", C.c_int), ("max_flips", C.c_int), ("dx", C.c_double), ("dy", C.c_double),
                 ("dz", C.c_double), ("num_freq", C.c_int), ("freq_hz", C.c_double * MAX_FREQ),
                 ("precision", C.c_int), ("defer_rank", C.c_int), ("device", C.c_int), ("fp64_update", C.c_int),
-                ("c64_build", C.c_int)]
+                ("c64_build", C.c_int), ("state_only", C.c_int)]
 
 
 class DbsParams(C.Structure):
@@ -106,6 +106,7 @@ def load():
         "pngf_dims": (I, [P, P, P]),
         "pngf_load_G": (I, [P, I, P, L_, P]),
         "pngf_load_G_file": (I, [P, I, C.c_char_p]),
+        "pngf_load_G_synth": (I, [P, I, C.c_ulonglong, D]),
         "pngf_set_tile_map": (I, [P, P]),
         "pngf_get_tile_map": (I, [P, P]),
         "pngf_set_source_port": (I, [P, I, I, I, I]),
@@ -130,6 +131,10 @@ def load():
         "pngf_dbs_log": (I, [P, L_, P, P, P, P, P, P]),
         "pngf_dbs_save_log": (I, [P, C.c_char_p]),
         "pngf_dbs_end": (I, [P]),
+        "pngf_group_create": (I, [P, I, I, P]),
+        "pngf_group_step": (I, [P, P]),
+        "pngf_group_stats_get": (I, [P, P]),
+        "pngf_group_destroy": (I, [P]),
         "pngf_prop_create": (I, [P, I, C.c_ulonglong, P]),
         "pngf_prop_destroy": (I, [P]),
         "pngf_prop_num_params": (L_, [P]),
@@ -190,7 +195,7 @@ class Handle:
     """Owns one pngf_handle (all frequencies of one DBS instance)."""
 
     def __init__(self, tiles_x, tiles_y, freqs, precision=PREC_FP64, max_flips=4, num_eobj=3, defer_rank=0,
-                 device=0, fp64_update=0, c64_build=0):
+                 device=0, fp64_update=0, c64_build=0, state_only=0):
         L = load()
         self.L = L
         cfg = Config()
@@ -203,6 +208,7 @@ class Handle:
         cfg.device = device
         cfg.fp64_update = fp64_update
         cfg.c64_build = c64_build
+        cfg.state_only = state_only
         self.cfg = cfg
         self.nf = len(freqs)
         self.E = num_eobj
@@ -247,6 +253,10 @@ class Handle:
         G = np.asfortranarray(G, dtype=np.complex128)
         go = None if gobj_rows is None else np.ascontiguousarray(gobj_rows, dtype=np.complex128)
         self._chk(self.L.pngf_load_G(self.h, f, _ptr(G), G.shape[0], _ptr(go)), "pngf_load_G")
+
+    def load_G_synth(self, f, seed=1, eps_r=2.25):
+        """Frequency f's G from the built-in synthetic generator, on the device."""
+        self._chk(self.L.pngf_load_G_synth(self.h, f, seed, eps_r), "pngf_load_G_synth")
 
     def load_G_file(self, f, path):
         self._chk(self.L.pngf_load_G_file(self.h, f, path.encode()), "pngf_load_G_file")
@@ -376,6 +386,57 @@ class Dbs:
         if getattr(self, "d", None):
             self.hd.L.pngf_dbs_end(self.d)
             self.d = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GroupStats(C.Structure):
+    _fields_ = [("rounds", C.c_long), ("graph_launches", C.c_long), ("captures", C.c_long),
+                ("kernel_launches", C.c_long), ("evals", C.c_long), ("accepts", C.c_long)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Group:
+    """Independent DBS runs (each on its own handle) stepped together."""
+
+    def __init__(self, runs, use_graphs=True):
+        self.runs = list(runs)
+        self.L = self.runs[0].hd.L
+        arr = (C.c_void_p * len(self.runs))(*[r.d.value for r in self.runs])
+        g = C.c_void_p()
+        self.runs[0].hd._chk(self.L.pngf_group_create(arr, len(self.runs), int(bool(use_graphs)), C.byref(g)),
+                             "pngf_group_create")
+        self.g = g
+
+    def step(self):
+        """One round; returns the number of members still running."""
+        a = C.c_int()
+        self.runs[0].hd._chk(self.L.pngf_group_step(self.g, C.byref(a)), "pngf_group_step")
+        return a.value
+
+    def run(self, max_rounds=None):
+        r = 0
+        while self.step() > 0:
+            r += 1
+            if max_rounds is not None and r >= max_rounds:
+                break
+        return self.stats()
+
+    def stats(self):
+        s = GroupStats()
+        self.runs[0].hd._chk(self.L.pngf_group_stats_get(self.g, C.byref(s)), "pngf_group_stats_get")
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "g", None):
+            self.L.pngf_group_destroy(self.g)
+            self.g = None
 
     def __del__(self):
         try:
