@@ -682,7 +682,7 @@ static int prepare_impl(Handle *h, bool fp64) {
   auto build = [&](int f) -> int {
     PNGF_CUDA(h, launch_init_M(h, f));
     if (c64 && !fp64) PNGF_CUDA(h, launch_split_M(h, f));
-    const int chunk = fp64 ? h->init_chunk : kInitChunk;
+    const int chunk = fp64 ? h->init_chunk : kC64BuildChunk;
     for (size_t c0 = 0; c0 < on.size(); c0 += chunk) {
       const int k = (int)std::min<size_t>(chunk, on.size() - c0);
       PNGF_CUDA(h, launch_accept_edges(h, f, h->d_acc_s + c0, h->d_acc_d + c0, k,

@@ -25,12 +25,16 @@
 // Kernel k_tc_update_f64 is persistent: one CTA per SM walks a contiguous
 // range of 128-row x 32-double-column tiles of M (row-block major). Warp 0
 // issues TMA loads (the A row-block stays in shared memory across its column
-// tiles; B tiles are double-buffered), warp 1 issues the tcgen05.mma.kind::f16
-// (M=128, N=32, K=16) chains into one of two TMEM accumulator sets (7 levels x
-// 32 columns each), and 16 epilogue warps (four warpgroups, 8 columns each)
-// drain one accumulator set while the MMAs fill the other. Every wait is
-// bounded; on timeout the kernel records an error code, drains its own TMA
-// copies, frees its TMEM and returns.
+// tiles; B tiles are double-buffered; each tile of M is loaded into one of
+// two shared-memory slots ahead of its epilogue), warp 1 issues the
+// tcgen05.mma.kind::f16 (M=128, N=32, K=16) chains into one of two TMEM
+// accumulator sets (7 levels x 32 columns each), 16 epilogue warps (four
+// warpgroups, 8 columns each) drain one accumulator set while the MMAs fill
+// the other and update the staged tile in shared memory, and warp 2 writes
+// each finished tile back with a TMA store. M thus moves between HBM and the
+// SM only in whole swizzled tiles. Every wait is bounded; on timeout the
+// kernel records an error code, drains its own TMA copies, frees its TMEM
+// and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -59,8 +63,13 @@ constexpr uint32_t FB_ATOM_A = FB_BM * 128;  // one 64-element K atom of the A t
 constexpr uint32_t FB_ATOM_B = FB_BN * 128;
 constexpr int FB_MAX_ATOMS = 7;              // K extent up to 448 (k <= 32)
 constexpr int FB_EPI_WARPS = 16;
-constexpr int FB_THREADS = 64 + 32 * FB_EPI_WARPS;
-constexpr size_t FB_SMEM = FB_MAX_ATOMS * (FB_ATOM_A + 2 * FB_ATOM_B) + 1024 + 256;
+constexpr int FB_THREADS = 96 + 32 * FB_EPI_WARPS;  // producer, MMA and store warps + epilogue
+constexpr uint32_t FB_DBOX = FB_BM * 128;           // 128 rows x 16 doubles of M (one TMA box)
+constexpr uint32_t FB_DTILE = 2 * FB_DBOX;          // a 128 x 32-double tile of M
+// Dynamic shared memory for natoms K atoms and nd staged tiles of M.
+constexpr size_t fb_smem(int natoms, int nd) {
+  return 1024 + (size_t)natoms * (FB_ATOM_A + 2 * FB_ATOM_B) + (size_t)nd * FB_DTILE + 256;
+}
 
 // kind::f16 instruction descriptor: D f32, A and B bf16, K-major, N = 32, M = 128.
 constexpr uint32_t kIdescBF16 =
@@ -158,28 +167,39 @@ __device__ __forceinline__ double i64_scaled(long long Y, int E) {
   return __longlong_as_double((long long)((s << 63) | ((unsigned long long)be << 52) | (mant & ((1ull << 52) - 1))));
 }
 
-// D[i, j] -= sum_c A_real[i, c] B_real[j, c] for i < rows, j < cols; D
-// row-major doubles with leading dimension ldd. ncb = column tiles per row
-// block, ntiles = total tiles, natoms = 64-element K atoms of the operands.
-__global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_constant__ CUtensorMap tmA,
-                                                                 const __grid_constant__ CUtensorMap tmB,
-                                                                 double *__restrict__ D, long ldd, int rows, int cols,
-                                                                 int ncb, int ntiles, int natoms, int k2p,
-                                                                 const int *__restrict__ eA,
-                                                                 const int *__restrict__ fB, int *err) {
+// D[i, j] -= sum_c A_real[i, c] B_real[j, c] for i < rows, j < cols; D is
+// M viewed as row-major doubles, reached only through the tensor map tmD
+// (128 x 16-double boxes, 128-byte swizzle). ncb = column tiles per row
+// block, ntiles = total tiles, natoms = 64-element K atoms of the operands,
+// nd = staged tiles of M (1 or 2).
+//
+// Tiles of M travel by TMA: the producer loads tile t into a shared-memory
+// slot ahead of its epilogue, the 16 epilogue warps update the slot in place
+// (thread = row, 8 doubles each, conflict-free under the swizzle) and the
+// store warp writes the slot back with a TMA store, then frees the slot.
+__global__ void __launch_bounds__(FB_THREADS, 1)
+    k_tc_update_f64(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                    const __grid_constant__ CUtensorMap tmD, int rows, int cols, int ncb, int ntiles, int natoms, int k2p,
+                    int nd, const int *__restrict__ eA, const int *__restrict__ fB, int *err) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                           ~static_cast<uintptr_t>(1023));
   const uint32_t sA = smem_u32(base);
-  const uint32_t sB0 = sA + FB_MAX_ATOMS * FB_ATOM_A;  // B buffer b at sB0 + b * FB_MAX_ATOMS * FB_ATOM_B
-  uint64_t *bars = reinterpret_cast<uint64_t *>(base + FB_MAX_ATOMS * (FB_ATOM_A + 2 * FB_ATOM_B));
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 12);
+  const uint32_t bstride = (uint32_t)natoms * FB_ATOM_B;  // B buffer b at sB0 + b * bstride
+  const uint32_t sB0 = sA + (uint32_t)natoms * FB_ATOM_A;
+  const uint32_t dbase = (uint32_t)natoms * (FB_ATOM_A + 2 * FB_ATOM_B);  // byte offset of slot 0 from base
+  const uint32_t sD0 = sA + dbase;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(base + dbase + (uint32_t)nd * FB_DTILE);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 16);
   const uint32_t bar0 = smem_u32(bars);
   const uint32_t a_full = bar0, a_empty = bar0 + 8;
   auto b_full = [&](int b) { return bar0 + 16 + 8 * b; };
   auto b_empty = [&](int b) { return bar0 + 32 + 8 * b; };
   auto acc_full = [&](int b) { return bar0 + 48 + 8 * b; };
   auto acc_empty = [&](int b) { return bar0 + 64 + 8 * b; };
+  auto d_full = [&](int s) { return bar0 + 80 + 8 * s; };   // tile of M landed in slot s
+  auto d_done = [&](int s) { return bar0 + 96 + 8 * s; };   // epilogue finished slot s
+  auto d_empty = [&](int s) { return bar0 + 112 + 8 * s; }; // store has read slot s
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   // this CTA's contiguous tile range
@@ -194,6 +214,9 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
       mbar_init(b_empty(b), 1);
       mbar_init(acc_full(b), 1);
       mbar_init(acc_empty(b), FB_EPI_WARPS);
+      mbar_init(d_full(b), 1);
+      mbar_init(d_done(b), FB_EPI_WARPS);
+      mbar_init(d_empty(b), 1);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -207,7 +230,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
   if (warp == 0) {
     if (lane == 0) {
       bool ok = true;
-      int nA = 0, rb_loaded = -1, issuedB = 0;
+      int nA = 0, rb_loaded = -1, issuedB = 0, issuedD = 0;
       for (int t = t_begin; t < t_end && ok; ++t) {
         const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb;
         if (rb != rb_loaded) {
@@ -219,16 +242,24 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
         }
         const int b = li & 1;
         if (li >= 2 && !mbar_wait(b_empty(b), ((li >> 1) - 1) & 1)) { ok = false; break; }
-        const uint32_t sB = sB0 + b * FB_MAX_ATOMS * FB_ATOM_B;
+        const uint32_t sB = sB0 + b * bstride;
         mbar_expect_tx(b_full(b), b_bytes);
         for (int a = 0; a < natoms; ++a) tma_load_2d(sB + a * FB_ATOM_B, &tmB, a * 64, cb * FB_BN, b_full(b));
         ++issuedB;
+        const int s = li % nd;
+        if (li >= nd && !mbar_wait(d_empty(s), ((li / nd) - 1) & 1)) { ok = false; break; }
+        mbar_expect_tx(d_full(s), FB_DTILE);
+        tma_load_2d(sD0 + s * FB_DTILE, &tmD, cb * FB_BN, rb * FB_BM, d_full(s));
+        tma_load_2d(sD0 + s * FB_DTILE + FB_DBOX, &tmD, cb * FB_BN + 16, rb * FB_BM, d_full(s));
+        ++issuedD;
       }
       if (!ok) atomicExch(err, 21);
       // Drain the copies in flight before the CTA can exit.
       if (nA > 0 && !mbar_wait(a_full, (nA - 1) & 1)) atomicExch(err, 24);
       for (int li = issuedB > 2 ? issuedB - 2 : 0; li < issuedB; ++li)
         if (!mbar_wait(b_full(li & 1), (li >> 1) & 1)) atomicExch(err, 24);
+      for (int li = issuedD > nd ? issuedD - nd : 0; li < issuedD; ++li)
+        if (!mbar_wait(d_full(li % nd), (li / nd) & 1)) atomicExch(err, 24);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -245,7 +276,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
         if (!mbar_wait(b_full(b), (li >> 1) & 1)) { ok = false; break; }
         if (li >= 2 && !mbar_wait(acc_empty(b), ((li >> 1) - 1) & 1)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t sB = sB0 + b * FB_MAX_ATOMS * FB_ATOM_B;
+        const uint32_t sB = sB0 + b * bstride;
         const uint32_t acc = tmem + (uint32_t)(b * 256);
         for (int l = 2; l <= FB_LMAX; ++l) {
           const uint32_t dcol = acc + (uint32_t)((l - 2) * FB_BN);
@@ -270,32 +301,41 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
       if (!ok) atomicExch(err, 22);
     }
     __syncwarp();
+  } else if (warp == 2) {
+    if (lane == 0) {
+      bool ok = true;
+      for (int t = t_begin; t < t_end; ++t) {
+        const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb, s = li % nd;
+        if (!mbar_wait(d_done(s), (li / nd) & 1)) { ok = false; break; }
+        const uint32_t sd = sD0 + s * FB_DTILE;
+        tma_store_2d(&tmD, sd, cb * FB_BN, rb * FB_BM);  // rows / columns past M are clipped
+        if (cb * FB_BN + 16 < cols) tma_store_2d(&tmD, sd + FB_DBOX, cb * FB_BN + 16, rb * FB_BM);
+        bulk_commit();
+        bulk_wait_read_all();
+        mbar_arrive(d_empty(s));
+      }
+      bulk_wait_all();
+      if (!ok) atomicExch(err, 25);
+    }
+    __syncwarp();
   } else {
-    const int ew = warp - 2;          // 0..15
+    const int ew = warp - 3;          // 0..15
     const int part = ew >> 2;         // which 8 columns of the tile
     const int q = warp & 3;           // TMEM lanes 32q .. 32q+31
+    const int r = q * 32 + lane;      // row of the tile
+    // this thread's 8 doubles: box part / 2, 16-byte chunks c0 .. c0+3 of row r
+    const uint32_t rowoff = dbase + (uint32_t)(part >> 1) * FB_DBOX + (uint32_t)r * 128;
+    const int c0 = (part & 1) * 4;
     bool ok = true;
-    // D of a tile is fetched one tile ahead.
-    double2 cur[4], nxt[4];
-    auto fetch = [&](int t, double2 *dv) {
-      const int rb = t / ncb, cb = t - rb * ncb;
-      const int row = rb * FB_BM + q * 32 + lane, col0 = cb * FB_BN + part * 8;
-      const bool full8 = row < rows && col0 + 8 <= cols;
-      const double2 *src = reinterpret_cast<const double2 *>(D + (size_t)row * ldd + col0);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) dv[u] = full8 ? src[u] : make_double2(0.0, 0.0);
-    };
-    if (t_begin < t_end) fetch(t_begin, cur);
     for (int t = t_begin; t < t_end; ++t) {
       const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb;
-      const int b = li & 1;
-      const int row = rb * FB_BM + q * 32 + lane;
-      const bool rin = row < rows;
-      const int col0 = cb * FB_BN + part * 8;
-      double *drow = D + (size_t)row * ldd + col0;
-      const bool full8 = rin && col0 + 8 <= cols;
-      if (t + 1 < t_end) fetch(t + 1, nxt);
-      const int ea = rin ? eA[row] : 0;
+      const int b = li & 1, s = li % nd;
+      const int row = rb * FB_BM + r;
+      const int col0 = cb * FB_BN + part * 8;  // < ncb * 32, within the padded scale arrays
+      const int ea = row < rows ? eA[row] : 0;
+      int fb[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) fb[u] = fB[col0 + u];
       ok = __all_sync(0xffffffffu, mbar_wait(acc_full(b), (li >> 1) & 1));
       if (!ok) break;
       tc_fence_after();
@@ -308,7 +348,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
       // the accumulator set is free once every warp has read it
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(acc_empty(b)) : "memory");
+      if (lane == 0) mbar_arrive(acc_empty(b));
       // Levels in pairs: P = C_l * 2^7 + C_{l+1} is an exact int32;
       // Y = P23 2^28 + P45 2^14 + P67 + round(C8 / 2^7).
       long long Y[8];
@@ -318,24 +358,23 @@ __global__ void __launch_bounds__(FB_THREADS, 1) k_tc_update_f64(const __grid_co
         Y[u] = ((long long)(C(0) * 128 + C(1)) << 28) + ((long long)(C(2) * 128 + C(3)) << 14) +
                (long long)(C(4) * 128 + C(5)) + (long long)((C(6) + 64) >> 7);
       }
-      if (rin) {
-        const int E0 = ea - FB_B * (FB_LMAX - 1);
-        if (full8) {
-          double2 *p = reinterpret_cast<double2 *>(drow);
+      ok = __all_sync(0xffffffffu, mbar_wait(d_full(s), (li / nd) & 1));
+      if (!ok) break;
+      // Rows and columns past M hold the TMA's zero fill and Y = 0 there;
+      // the store clips them.
+      const int E0 = ea - FB_B * (FB_LMAX - 1);
+      unsigned char *slot = base + rowoff + (size_t)s * FB_DTILE;
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            double2 x = cur[u];
-            x.x -= i64_scaled(Y[2 * u], E0 + fB[col0 + 2 * u]);
-            x.y -= i64_scaled(Y[2 * u + 1], E0 + fB[col0 + 2 * u + 1]);
-            p[u] = x;
-          }
-        } else {
-          for (int u = 0; u < 8; ++u)
-            if (col0 + u < cols) drow[u] -= i64_scaled(Y[u], E0 + fB[col0 + u]);
-        }
+      for (int u = 0; u < 4; ++u) {
+        double2 *p = reinterpret_cast<double2 *>(slot + 16 * ((c0 + u) ^ (r & 7)));
+        double2 x = *p;
+        x.x -= i64_scaled(Y[2 * u], E0 + fb[2 * u]);
+        x.y -= i64_scaled(Y[2 * u + 1], E0 + fb[2 * u + 1]);
+        *p = x;
       }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) cur[u] = nxt[u];
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(d_done(s));
     }
     if (!ok && lane == 0) atomicExch(err, 23);
   }
@@ -370,7 +409,22 @@ cudaError_t make_map_bf16(CUtensorMap *m, const void *base, long rows, int K, lo
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// 2-D tensor map over M as row-major doubles: cols x rows, row pitch ldd
+// doubles, 16 x 128 boxes, 128-byte swizzle (zero fill outside M).
+cudaError_t make_map_f64(CUtensorMap *m, const double *base, long rows, long cols, long ldd) {
+  if (!g_enc) return cudaErrorNotSupported;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ldd * 8};
+  const cuuint32_t box[2] = {16, (cuuint32_t)FB_BM};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = g_enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double *>(base), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 int g_num_sms = 0;
+int g_smem_optin = 0;
 
 }  // namespace
 
@@ -391,26 +445,31 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
       A, rows, rows, k, k2p, (int)ldk, static_cast<__nv_bfloat16 *>(h->d_A16), h->d_eA);
   k_slice_B<<<(unsigned)((cols + 127) / 128), 128, 0, h->stream>>>(
       W, h->ldm, cols, k, k2p, (int)ldk, static_cast<__nv_bfloat16 *>(h->d_B16), h->d_fB);
-  CUtensorMap ma, mb;
+  CUtensorMap ma, mb, md;
   cudaError_t e;
   if ((e = make_map_bf16(&ma, h->d_A16, h->a16_rows, kop, ldk, FB_BM)) != cudaSuccess) return e;
   if ((e = make_map_bf16(&mb, h->d_B16, h->b16_rows, kop, ldk, FB_BN)) != cudaSuccess) return e;
-  if ((e = cudaFuncSetAttribute(k_tc_update_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FB_SMEM)) !=
-      cudaSuccess)
-    return e;
+  if ((e = make_map_f64(&md, reinterpret_cast<const double *>(M), rows, cols, 2 * h->ldm)) != cudaSuccess) return e;
   if (g_num_sms == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&g_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (g_num_sms <= 0) g_num_sms = 1;
   }
+  // two staged tiles of M when shared memory allows (k <= 24), else one
+  const int nd = fb_smem(natoms, 2) <= (size_t)g_smem_optin ? 2 : 1;
+  const size_t smem = fb_smem(natoms, nd);
+  if (smem > (size_t)g_smem_optin) return cudaErrorInvalidValue;
+  if ((e = cudaFuncSetAttribute(k_tc_update_f64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+      cudaSuccess)
+    return e;
   const int nrb = (int)((rows + FB_BM - 1) / FB_BM), ncb = (int)((cols + FB_BN - 1) / FB_BN);
   const int ntiles = nrb * ncb;
   const int grid = ntiles < g_num_sms ? ntiles : g_num_sms;
   cudaEvent_t t0 = timing_mark(h);
-  k_tc_update_f64<<<grid, FB_THREADS, FB_SMEM, h->stream>>>(ma, mb, reinterpret_cast<double *>(M), 2 * h->ldm,
-                                                            (int)rows, (int)cols, ncb, ntiles, natoms, k2p, h->d_eA,
-                                                            h->d_fB, h->d_tc_err);
+  k_tc_update_f64<<<grid, FB_THREADS, smem, h->stream>>>(ma, mb, md, (int)rows, (int)cols, ncb, ntiles, natoms, k2p, nd,
+                                                         h->d_eA, h->d_fB, h->d_tc_err);
   const double cells = (double)rows * (double)(n + 1);
   timing_close(h, t0, T_UPDATE, 8.0 * k * cells, 2.0 * 16.0 * cells + 2.0 * kop * ((double)rows + (double)cols),
                0.0);

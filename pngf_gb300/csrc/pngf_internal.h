@@ -16,6 +16,10 @@ constexpr int kMaxK = 192;
 constexpr int kMaxEvalK = 104;
 // Edges accepted per chunk when M is built from G for a design.
 constexpr int kInitChunk = 96;
+// Edges per chunk when a complex64 state is built directly in complex64: the
+// factor and W solve cost O(k^3) and O(k^2 N) in FP64, the tensor-core update
+// O(1) passes over T, so mid-sized chunks are cheapest.
+constexpr int kC64BuildChunk = 48;
 
 // Forms of the candidate kernel the autotuner chooses from: warps working on
 // one (candidate, frequency) and candidates per CTA. Index 0 is the default.
