@@ -35,161 +35,199 @@ namespace {
 
 constexpr int TC_BM = 128;       // rows per tile (MMA M)
 constexpr int TC_BK = 32;        // fp32 K elements per stage = one 128-byte swizzle row
-constexpr int TC_ST = 2;         // pipeline stages (3 CTAs per SM fit in shared memory and TMEM)
 constexpr uint32_t A_BYTES = TC_BM * TC_BK * 4;
-// Per output-tile width BN (fp32 columns, the MMA N; 64 or 128, picked by the autotuner):
-template <int BN> __host__ __device__ constexpr uint32_t b_bytes() { return BN * TC_BK * 4; }
-template <int BN> __host__ __device__ constexpr uint32_t stage_bytes() { return A_BYTES + b_bytes<BN>(); }
-template <int BN> __host__ __device__ constexpr size_t tc_smem() { return TC_ST * stage_bytes<BN>() + 1024 + 256; }
+constexpr uint32_t TC_DBOX = TC_BM * 128;  // 128 rows x 32 floats of T (one TMA box)
+constexpr int TC_EPI_WARPS = 8;
+constexpr int TC_THREADS = 96 + 32 * TC_EPI_WARPS;  // producer, MMA and store warps + epilogue
 using namespace tc;
 
-// Instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
-// (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits
-// 17-22, M >> 4 at bits 24-28.
-template <int BN> __host__ __device__ constexpr uint32_t idesc_tf32() {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
-}
+// Shapes per output tile width BN (fp32 columns = the MMA N; 64 or 128,
+// picked by the autotuner): operand stages in flight and shared memory.
+template <int BN> struct C64Tile {
+  static constexpr uint32_t B_BYTES = BN * TC_BK * 4;  // one K stage of B
+  static constexpr uint32_t STAGE = A_BYTES + B_BYTES;
+  static constexpr int ST = BN == 128 ? 2 : 4;         // operand stages
+  static constexpr uint32_t DTILE = (BN / 32) * TC_DBOX;  // a 128 x BN tile of T
+  static constexpr size_t SMEM = 1024 + ST * STAGE + 2 * DTILE + 256;
+  // Instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
+  // (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits
+  // 17-22, M >> 4 at bits 24-28.
+  static constexpr uint32_t IDESC =
+      (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+};
 
-// D[i, j] -= sum_k Aop[i, k] Bop[j, k] for i < rows, j < cols (fp32, D row-major
-// with leading dimension ldd). Aop / Bop come through TMA maps (K-major, 128B
-// swizzle). nkb = K / 32.
+// T[i, j] -= sum_k Aop[i, k] Bop[j, k] for i < rows, j < cols (fp32 view of
+// the complex64 T, reached through the tensor map tmD: 32 x 128 boxes,
+// 128-byte swizzle). Aop / Bop come through TMA maps (K-major, 128-byte
+// swizzle); nkb = K / 32.
+//
+// Persistent: one CTA per SM walks a contiguous range of 128 x BN tiles
+// (row-block major). Warp 0 issues TMA loads: each tile of T into one of two
+// shared-memory slots ahead of its epilogue, and the K stages of A and B
+// into an ST-deep ring. Warp 1 allocates TMEM and issues the
+// tcgen05.mma.kind::tf32 (M=128, N=BN, K=8) chains into one of two
+// accumulators. Eight epilogue warps (two per TMEM lane quadrant, half the
+// columns each) read the accumulator with tcgen05.ld and update the staged
+// tile in place (thread = row; the swizzle makes these accesses conflict-free);
+// warp 2 writes each finished tile back with a TMA store and frees its slot.
 template <int BN>
-__global__ void __launch_bounds__(192, 3) k_tc_update(const __grid_constant__ CUtensorMap tmA,
-                                                      const __grid_constant__ CUtensorMap tmB, float *__restrict__ D,
-                                                      long ldd, int rows, int cols, int nkb, int *err) {
-  constexpr uint32_t B_BYTES = b_bytes<BN>(), STAGE_BYTES = stage_bytes<BN>();
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_tc_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                const __grid_constant__ CUtensorMap tmD, int cols, int ncb, int ntiles, int nkb, int *err) {
+  using S = C64Tile<BN>;
+  constexpr int ST = S::ST;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                           ~static_cast<uintptr_t>(1023));
   const uint32_t sbase = smem_u32(base);
-  uint64_t *bars = reinterpret_cast<uint64_t *>(base + TC_ST * STAGE_BYTES);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2 * TC_ST + 1);
-  const uint32_t full0 = smem_u32(bars), empty0 = full0 + 8 * TC_ST, done = full0 + 16 * TC_ST;
+  constexpr uint32_t dbase = ST * S::STAGE;  // byte offset of slot 0 from base
+  const uint32_t sD0 = sbase + dbase;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(base + dbase + 2 * S::DTILE);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2 * ST + 10);
+  const uint32_t bar0 = smem_u32(bars);
+  auto full = [&](int s) { return bar0 + 8 * s; };
+  auto empty = [&](int s) { return bar0 + 8 * (ST + s); };
+  auto acc_full = [&](int b) { return bar0 + 8 * (2 * ST + b); };
+  auto acc_empty = [&](int b) { return bar0 + 8 * (2 * ST + 2 + b); };
+  auto d_full = [&](int s) { return bar0 + 8 * (2 * ST + 4 + s); };   // tile of T landed in slot s
+  auto d_done = [&](int s) { return bar0 + 8 * (2 * ST + 6 + s); };   // epilogue finished slot s
+  auto d_empty = [&](int s) { return bar0 + 8 * (2 * ST + 8 + s); };  // store has read slot s
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t_begin = (int)(((long long)ntiles * blockIdx.x) / gridDim.x);
+  const int t_end = (int)(((long long)ntiles * (blockIdx.x + 1)) / gridDim.x);
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < TC_ST; ++s) {
-      mbar_init(full0 + 8 * s, 1);
-      mbar_init(empty0 + 8 * s, 1);
+    for (int s = 0; s < ST; ++s) {
+      mbar_init(full(s), 1);
+      mbar_init(empty(s), 1);
     }
-    mbar_init(done, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(acc_full(b), 1);
+      mbar_init(acc_empty(b), TC_EPI_WARPS);
+      mbar_init(d_full(b), 1);
+      mbar_init(d_done(b), TC_EPI_WARPS);
+      mbar_init(d_empty(b), 1);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
-                 "r"((uint32_t)BN)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
+  if (warp == 1) tmem_alloc(smem_u32(tslot), 2 * BN);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * BN;
 
   if (warp == 0) {
     if (lane == 0) {
-      int issued = 0;
       bool ok = true;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % TC_ST;
-        if (kb >= TC_ST && !mbar_wait(empty0 + 8 * s, ((kb / TC_ST) - 1) & 1)) {
-          ok = false;
-          break;
+      int g = 0, issuedD = 0;
+      for (int t = t_begin; t < t_end && ok; ++t) {
+        const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb;
+        const int m0 = rb * TC_BM, n0 = cb * BN, s = li & 1;
+        if (li >= 2 && !mbar_wait(d_empty(s), ((li >> 1) - 1) & 1)) { ok = false; break; }
+        mbar_expect_tx(d_full(s), S::DTILE);
+        for (int j = 0; j < BN / 32; ++j) tma_load_2d(sD0 + s * S::DTILE + j * TC_DBOX, &tmD, n0 + 32 * j, m0, d_full(s));
+        ++issuedD;
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          const int st = g % ST;
+          if (g >= ST && !mbar_wait(empty(st), ((g / ST) - 1) & 1)) { ok = false; break; }
+          mbar_expect_tx(full(st), S::STAGE);
+          tma_load_2d(sbase + st * S::STAGE, &tmA, kb * TC_BK, m0, full(st));
+          tma_load_2d(sbase + st * S::STAGE + A_BYTES, &tmB, kb * TC_BK, n0, full(st));
         }
-        mbar_expect_tx(full0 + 8 * s, STAGE_BYTES);
-        tma_load_2d(sbase + s * STAGE_BYTES, &tmA, kb * TC_BK, m0, full0 + 8 * s);
-        tma_load_2d(sbase + s * STAGE_BYTES + A_BYTES, &tmB, kb * TC_BK, n0, full0 + 8 * s);
-        ++issued;
       }
-      if (!ok) atomicExch(err, 1);
+      if (!ok) atomicExch(err, 31);
       // Drain: every copy this thread issued has landed before the CTA exits.
-      for (int kb = issued > TC_ST ? issued - TC_ST : 0; kb < issued; ++kb)
-        if (!mbar_wait(full0 + 8 * (kb % TC_ST), (kb / TC_ST) & 1)) atomicExch(err, 4);
+      for (int q = g > ST ? g - ST : 0; q < g; ++q)
+        if (!mbar_wait(full(q % ST), (q / ST) & 1)) atomicExch(err, 34);
+      for (int q = issuedD > 2 ? issuedD - 2 : 0; q < issuedD; ++q)
+        if (!mbar_wait(d_full(q & 1), (q >> 1) & 1)) atomicExch(err, 34);
     }
   } else if (warp == 1) {
     if (lane == 0) {
       bool ok = true;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % TC_ST;
-        if (!mbar_wait(full0 + 8 * s, (kb / TC_ST) & 1)) {
-          ok = false;
-          break;
-        }
+      int g = 0;
+      for (int t = t_begin; t < t_end && ok; ++t) {
+        const int li = t - t_begin, b = li & 1;
+        if (li >= 2 && !mbar_wait(acc_empty(b), ((li >> 1) - 1) & 1)) { ok = false; break; }
         tc_fence_after();
-        const uint64_t ad = sw128_desc(sbase + s * STAGE_BYTES);
-        const uint64_t bd = sw128_desc(sbase + s * STAGE_BYTES + A_BYTES);
+        const uint32_t acc = tmem + (uint32_t)(b * BN);
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          const int st = g % ST;
+          if (!mbar_wait(full(st), (g / ST) & 1)) { ok = false; break; }
+          tc_fence_after();
+          const uint64_t ad = sw128_desc(sbase + st * S::STAGE);
+          const uint64_t bd = sw128_desc(sbase + st * S::STAGE + A_BYTES);
 #pragma unroll
-        for (int kk = 0; kk < TC_BK / 8; ++kk)  // K = 8 tf32 = 32 bytes per MMA: +2 in 16-byte units
-          mma_tf32(tmem, ad + 2 * kk, bd + 2 * kk, idesc_tf32<BN>(), (kb | kk) != 0);
-        mma_commit(empty0 + 8 * s);
+          for (int kk = 0; kk < TC_BK / 8; ++kk)  // K = 8 tf32 = 32 bytes per MMA: +2 in 16-byte units
+            mma_tf32(acc, ad + 2 * kk, bd + 2 * kk, S::IDESC, (kb | kk) != 0);
+          mma_commit(empty(st));
+        }
+        if (ok) mma_commit(acc_full(b));
       }
-      mma_commit(done);
-      if (!ok) atomicExch(err, 2);
+      if (!ok) atomicExch(err, 32);
+    }
+    __syncwarp();
+  } else if (warp == 2) {
+    if (lane == 0) {
+      bool ok = true;
+      for (int t = t_begin; t < t_end; ++t) {
+        const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb, s = li & 1;
+        if (!mbar_wait(d_done(s), (li >> 1) & 1)) { ok = false; break; }
+        for (int j = 0; j < BN / 32; ++j)  // rows / columns past T are clipped
+          if (cb * BN + 32 * j < cols) tma_store_2d(&tmD, sD0 + s * S::DTILE + j * TC_DBOX, cb * BN + 32 * j, rb * TC_BM);
+        bulk_commit();
+        bulk_wait_read_all();
+        mbar_arrive(d_empty(s));
+      }
+      bulk_wait_all();
+      if (!ok) atomicExch(err, 35);
     }
     __syncwarp();
   } else {
-    const int q = warp & 3;  // this warp may access TMEM lanes 32q .. 32q+31
-    const int row = m0 + q * 32 + lane;
-    const bool rin = row < rows;
-    float *drow = D + (size_t)row * ldd;
-    // The first half of this thread's row segment is read while the MMAs run;
-    // the second half is read while the first half is written back.
-    constexpr int HALF = BN / 2;
-    float4 pre[HALF / 4];
+    constexpr int HALF = BN / 2;      // columns per epilogue warp
+    const int ew = warp - 3, part = ew >> 2, q = warp & 3;
+    const int r = q * 32 + lane;      // row of the tile (TMEM lane)
+    bool ok = true;
+    for (int t = t_begin; t < t_end; ++t) {
+      const int li = t - t_begin, b = li & 1, s = li & 1;
+      ok = __all_sync(0xffffffffu, mbar_wait(acc_full(b), (li >> 1) & 1));
+      if (!ok) break;
+      tc_fence_after();
+      uint32_t v[HALF];
+      const uint32_t tbase = tmem + (uint32_t)(b * BN) + ((uint32_t)(q * 32) << 16) + (uint32_t)(part * HALF);
 #pragma unroll
-    for (int u = 0; u < HALF / 4; ++u) {
-      const int col = n0 + 4 * u;
-      pre[u] = (rin && col + 4 <= cols) ? *reinterpret_cast<const float4 *>(drow + col) : make_float4(0, 0, 0, 0);
-    }
-    // warp-uniform outcome: tcgen05.ld below is .sync.aligned
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
-    tc_fence_after();
-    if (!ok) {
-      if (lane == 0) atomicExch(err, 3);
-    } else {
+      for (int c = 0; c < HALF / 8; ++c) tmem_ld8_nowait(tbase + (uint32_t)(c * 8), v + 8 * c);
+      tmem_wait_ld();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(acc_empty(b));  // the accumulator may be refilled
+      ok = __all_sync(0xffffffffu, mbar_wait(d_full(s), (li >> 1) & 1));
+      if (!ok) break;
+      // Rows and columns past T hold the TMA's zero fill and a zero
+      // accumulator; the store clips them.
+      unsigned char *slot = base + dbase + (size_t)s * S::DTILE + (size_t)r * 128;
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-#pragma unroll
-        for (int c = 0; c < HALF / 16; ++c) {
-          float v[16];
-          const int cc = half * (HALF / 16) + c;
-          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cc * 16), v);
-          const int col0 = n0 + cc * 16;
-          if (rin) {
-            if (col0 + 16 <= cols) {
-              float4 *p = reinterpret_cast<float4 *>(drow + col0);
-#pragma unroll
-              for (int u = 0; u < 4; ++u) {
-                float4 x = pre[c * 4 + u];
-                x.x -= v[4 * u];
-                x.y -= v[4 * u + 1];
-                x.z -= v[4 * u + 2];
-                x.w -= v[4 * u + 3];
-                p[u] = x;
-              }
-            } else {
-              for (int u = 0; u < 16; ++u)
-                if (col0 + u < cols) drow[col0 + u] -= v[u];
-            }
-          }
-          if (half == 0) {  // refill this slot with the matching chunk of the second half
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const int col = n0 + HALF + c * 16 + 4 * u;
-              pre[c * 4 + u] =
-                  (rin && col + 4 <= cols) ? *reinterpret_cast<const float4 *>(drow + col) : make_float4(0, 0, 0, 0);
-            }
-          }
-        }
+      for (int c4 = 0; c4 < HALF / 4; ++c4) {  // 16-byte chunks of this thread's columns
+        const int col = part * HALF + 4 * c4;
+        float4 *p = reinterpret_cast<float4 *>(slot + (col >> 5) * TC_DBOX + 16 * (((col & 31) >> 2) ^ (r & 7)));
+        float4 x = *p;
+        x.x -= __uint_as_float(v[4 * c4]);
+        x.y -= __uint_as_float(v[4 * c4 + 1]);
+        x.z -= __uint_as_float(v[4 * c4 + 2]);
+        x.w -= __uint_as_float(v[4 * c4 + 3]);
+        *p = x;
       }
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(d_done(s));
     }
+    if (!ok && lane == 0) atomicExch(err, 33);
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
+    tmem_dealloc(tmem, 2 * BN);
   }
 }
 
@@ -429,6 +467,7 @@ __global__ void k_rows_compare(const float2 *__restrict__ T32, long ldm, const i
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+int g_c64_sms = 0;
 std::once_flag g_encode_once;
 
 cudaError_t get_encoder() {
@@ -507,24 +546,33 @@ cudaError_t launch_c64_update(Handle *h, int f, int k) {
   k_build_Aop<<<ga, 128, 0, h->stream>>>(h->d_A, rows, n, k, Kt, h->kt_cap, h->d_Aop);
   k_build_Bop<<<gb, 128, 0, h->stream>>>(h->d_W, h->ldm, n, k, Kt, h->kt_cap, h->d_Bop);
   const int bn = h->c64_cols == 64 ? 64 : 128;
-  CUtensorMap ma, mb;
+  const int dcols = (int)(2 * n);
+  CUtensorMap ma, mb, md;
   if ((e = make_map(&ma, h->d_Aop, h->aop_rows, Kt, h->kt_cap, TC_BM)) != cudaSuccess) return e;
   if ((e = make_map(&mb, h->d_Bop, h->bop_rows, Kt, h->kt_cap, bn)) != cudaSuccess) return e;
-  const int dcols = (int)(2 * n);
-  dim3 g((unsigned)((dcols + bn - 1) / bn), (unsigned)((n + TC_BM - 1) / TC_BM));
+  if ((e = make_map(&md, reinterpret_cast<const float *>(q.T32), n, dcols, 2 * h->ldm, TC_BM)) != cudaSuccess)
+    return e;
+  if (g_c64_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_c64_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_c64_sms <= 0) g_c64_sms = 1;
+  }
+  const int ncb = (dcols + bn - 1) / bn, ntiles = ncb * (int)((n + TC_BM - 1) / TC_BM);
+  const int grid = ntiles < g_c64_sms ? ntiles : g_c64_sms;
   cudaEvent_t t0 = timing_mark(h);
   if (bn == 64) {
     if ((e = cudaFuncSetAttribute(k_tc_update<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)tc_smem<64>())) != cudaSuccess)
+                                  (int)C64Tile<64>::SMEM)) != cudaSuccess)
       return e;
-    k_tc_update<64><<<g, 192, tc_smem<64>(), h->stream>>>(ma, mb, reinterpret_cast<float *>(q.T32), 2 * h->ldm,
-                                                          (int)n, dcols, Kt / TC_BK, h->d_tc_err);
+    k_tc_update<64><<<grid, TC_THREADS, C64Tile<64>::SMEM, h->stream>>>(ma, mb, md, dcols, ncb, ntiles, Kt / TC_BK,
+                                                                         h->d_tc_err);
   } else {
     if ((e = cudaFuncSetAttribute(k_tc_update<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)tc_smem<128>())) != cudaSuccess)
+                                  (int)C64Tile<128>::SMEM)) != cudaSuccess)
       return e;
-    k_tc_update<128><<<g, 192, tc_smem<128>(), h->stream>>>(ma, mb, reinterpret_cast<float *>(q.T32), 2 * h->ldm,
-                                                            (int)n, dcols, Kt / TC_BK, h->d_tc_err);
+    k_tc_update<128><<<grid, TC_THREADS, C64Tile<128>::SMEM, h->stream>>>(ma, mb, md, dcols, ncb, ntiles,
+                                                                           Kt / TC_BK, h->d_tc_err);
   }
   const double cells = (double)n * (double)n;  // complex entries of T updated
   timing_close(h, t0, T_UPDATE, 8.0 * k * cells,

@@ -145,26 +145,24 @@ constexpr int kMagicBits = 0x4B400000;
 __device__ __forceinline__ int fbits(float v) { return __float_as_int(v + 12582912.0f); }
 
 // Y * 2^E as a double, built from the bits on the integer pipe (round half
-// up to 53 bits). Falls back to ldexp outside the normal exponent range.
+// up to 53 bits), |Y| < 2^63. Branch-free except for the fallback to ldexp
+// outside the normal exponent range, so a thread's eight conversions
+// interleave instead of running as eight dependent chains.
 __device__ __forceinline__ double i64_scaled(long long Y, int E) {
-  if (Y == 0) return 0.0;
-  const unsigned long long s = Y < 0 ? 1ull : 0ull;
-  unsigned long long u = Y < 0 ? (unsigned long long)(-Y) : (unsigned long long)Y;
-  int msb = 63 - __clzll((long long)u);
-  unsigned long long mant;
-  if (msb > 52) {
-    const int sh = msb - 52;
-    mant = (u + (1ull << (sh - 1))) >> sh;
-    if (mant >> 53) {  // rounding carried into a new leading bit
-      mant >>= 1;
-      ++msb;
-    }
-  } else {
-    mant = u << (52 - msb);
-  }
+  const unsigned long long s = (unsigned long long)(Y >> 63);  // 0 or all ones
+  const unsigned long long u = ((unsigned long long)Y ^ s) - s;  // |Y|
+  int msb = 63 - __clzll((long long)u);                         // -1 for Y = 0
+  const int sh = max(msb - 52, 0);
+  const unsigned long long up = (u + ((1ull << max(sh - 1, 0)) & (sh > 0 ? ~0ull : 0ull))) >> sh;
+  unsigned long long mant = sh > 0 ? up : u << max(52 - msb, 0);
+  const unsigned long long c = mant >> 53;  // rounding carried into a new leading bit
+  mant >>= c;
+  msb += (int)c;
   const int be = msb + E + 1023;
-  if (be <= 0 || be >= 2047) return ldexp((double)Y, E);
-  return __longlong_as_double((long long)((s << 63) | ((unsigned long long)be << 52) | (mant & ((1ull << 52) - 1))));
+  const double r =
+      __longlong_as_double((long long)((s << 63) | ((unsigned long long)be << 52) | (mant & ((1ull << 52) - 1))));
+  if (u != 0 && (be <= 0 || be >= 2047)) return ldexp((double)Y, E);
+  return u == 0 ? 0.0 : r;
 }
 
 // D[i, j] -= sum_c A_real[i, c] B_real[j, c] for i < rows, j < cols; D is
