@@ -528,7 +528,13 @@ def gpu_arm(a, world, rank, local):
                       "frac": achieved / fp64_peak if achieved else None,
                       "algorithmic_flop_per_launch": tm["update_flop"] / max(1, tm["update_launches"]),
                       "peak_source": "cuBLAS DGEMM 4096^3 via torch on this GPU in this run, best of 5"},
-        "share_of_device_time": tm["update_ms"] / max(1e-9, tm["eval_ms"] + tm["accept_ms"]),
+        # the frequencies' updates of one accept run concurrently, one stream
+        # each: launch_ms is a launch's own duration among them; the
+        # aggregate counts every update byte over the accept steps' device
+        # time (factor, solves and operand slicing included)
+        "frequency_streams": nf,
+        "aggregate_gbs_over_accept_time": tm["update_bytes"] / (tm["accept_ms"] * 1e-3) / 1e9
+        if tm["accept_ms"] > 0 else None,
     }
     eval_s = tm["eval_ms"] * 1e-3
     line = {
@@ -591,6 +597,9 @@ def gpu_arm(a, world, rank, local):
                 "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": (t32["update_bytes"] / u32 / 1e9) / peaks["hbm_gbs"] if u32 > 0 else None,
                 "peak_source": peak_src,
+                "frequency_streams": nf,
+                "aggregate_gbs_over_accept_time": t32["update_bytes"] / (t32["accept_ms"] * 1e-3) / 1e9
+                if t32["accept_ms"] > 0 else None,
                 "launch_ms": t32["update_ms"] / max(1, t32["update_launches"]),
                 "algorithmic_bytes_per_launch": t32["update_bytes"] / max(1, t32["update_launches"]),
             },

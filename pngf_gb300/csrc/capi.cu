@@ -25,7 +25,7 @@ int cuda_check(Handle *h, cudaError_t e, const char *what) {
   return set_error(h, PNGF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-cudaEvent_t timing_mark(Handle *h) {
+cudaEvent_t timing_mark(Handle *h, cudaStream_t s) {
   if (!h->timing) return nullptr;
   cudaEvent_t e;
   if (!h->ev_pool.empty()) {
@@ -34,15 +34,36 @@ cudaEvent_t timing_mark(Handle *h) {
   } else if (cudaEventCreate(&e) != cudaSuccess) {
     return nullptr;
   }
-  cudaEventRecord(e, h->stream);
+  cudaEventRecord(e, s ? s : h->stream);
   return e;
 }
 
-void timing_close(Handle *h, cudaEvent_t start, int cat, double x1, double x2, double x3) {
+void timing_close(Handle *h, cudaEvent_t start, int cat, double x1, double x2, double x3, cudaStream_t s) {
   if (!start) return;
-  cudaEvent_t stop = timing_mark(h);
+  cudaEvent_t stop = timing_mark(h, s);
   if (!stop) return;
   h->pending.push_back({start, stop, cat, x1, x2, x3});
+}
+
+// With one lane per frequency: every lane's stream waits for the work queued
+// so far on the handle's stream (lanes_fork), and the handle's stream waits
+// for everything queued on the lanes (lanes_join).
+static int lanes_fork(Handle *h) {
+  if (h->lanes.size() < 2) return PNGF_OK;
+  cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
+  for (size_t i = 0; i < h->lanes.size() && e == cudaSuccess; ++i)
+    e = cudaStreamWaitEvent(h->lanes[i].stream, h->ev_fork, 0);
+  return cuda_check(h, e, "fork onto the frequency streams");
+}
+
+static int lanes_join(Handle *h) {
+  if (h->lanes.size() < 2) return PNGF_OK;
+  cudaError_t e = cudaSuccess;
+  for (size_t i = 0; i < h->lanes.size() && e == cudaSuccess; ++i) {
+    e = cudaEventRecord(h->lanes[i].done, h->lanes[i].stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->stream, h->lanes[i].done, 0);
+  }
+  return cuda_check(h, e, "join of the frequency streams");
 }
 
 static void timing_collect(Handle *h) {
@@ -58,7 +79,7 @@ static void timing_collect(Handle *h) {
       t.eval_flop += p.x3;
     } else if (p.cat == T_ACCEPT) {
       t.accept_ms += ms;
-      t.accepts += 1;
+      t.accepts += (long)p.x1;  // frequencies the accept covered
     } else {
       t.update_ms += ms;
       t.update_launches += 1;
@@ -300,12 +321,15 @@ int accept_cand_async(Handle *h, int c, int k, bool check_now) {
   if (c < 0 || c >= h->batch_n) return set_error(h, PNGF_ERR_ARG, "candidate index outside the last batch");
   if (k < 0 || k > h->kmax) return set_error(h, PNGF_ERR_ARG, "invalid flipped-edge count");
   PNGF_CUDA(h, cudaMemsetAsync(h->d_acc_status, 0, sizeof(int), h->stream));
-  for (int f = 0; f < h->cfg.num_freq; ++f) {
-    cudaEvent_t t0 = timing_mark(h);
+  // the frequencies' accepts are independent: one lane (stream + scratch) each
+  cudaEvent_t t0 = timing_mark(h);
+  int rc;
+  if ((rc = lanes_fork(h))) return rc;
+  for (int f = 0; f < h->cfg.num_freq; ++f)
     PNGF_CUDA(h, launch_accept_edges(h, f, h->d_es + (size_t)c * h->kmax, h->d_ed + (size_t)c * h->kmax, k,
                                      h->cfg.precision));
-    timing_close(h, t0, T_ACCEPT, 0.0, 0.0, 0.0);
-  }
+  if ((rc = lanes_join(h))) return rc;
+  timing_close(h, t0, T_ACCEPT, (double)h->cfg.num_freq, 0.0, 0.0);
   PNGF_CUDA(h, launch_commit(h, c));
   if (h->d_tc_err && check_now) {  // the tensor-core kernels' bounded waits report here (else at the next collect)
     int tc = 0;
@@ -371,13 +395,24 @@ int pngf_destroy(pngf_handle *ph) {
   dfree(h->d_fconst);
   dfree(h->d_views);
   dfree(h->d_Eincs);
-  dfree(h->d_Aop);
-  dfree(h->d_Bop);
   dfree(h->d_tc_err);
-  dfree(h->d_A16);
-  dfree(h->d_B16);
-  dfree(h->d_eA);
-  dfree(h->d_fB);
+  for (Lane &L : h->lanes) {
+    if (L.stream) cudaStreamSynchronize(L.stream);
+    dfree(L.A);
+    dfree(L.W);
+    dfree(L.LU);
+    dfree(L.z);
+    dfree(L.piv);
+    dfree(L.Aop);
+    dfree(L.Bop);
+    dfree(L.A16);
+    dfree(L.B16);
+    dfree(L.eA);
+    dfree(L.fB);
+    if (L.done) cudaEventDestroy(L.done);
+    if (L.stream) cudaStreamDestroy(L.stream);
+  }
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   dfree(h->d_tile_map);
   dfree(h->d_P);
   dfree(h->d_tiles);
@@ -391,13 +426,8 @@ int pngf_destroy(pngf_handle *ph) {
   dfree(h->d_F);
   dfree(h->d_first);
   dfree(h->d_status);
-  dfree(h->d_A);
-  dfree(h->d_W);
   dfree(h->d_acc_s);
   dfree(h->d_acc_d);
-  dfree(h->d_LU);
-  dfree(h->d_piv);
-  dfree(h->d_z);
   dfree(h->d_acc_status);
   dfree(h->d_colmax);
   dfree(h->d_fbest);
@@ -473,32 +503,53 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
       return fail(rc);
     einc[f] = q.Einc;
   }
-  if (c64) {  // tensor-core operands: rows padded to the 128-row tile, zero outside what each update writes
-    h->kt_cap = (6 * std::max(kmax, kInitChunk) + 31) / 32 * 32;  // accepts and complex64 build chunks
+  // Tensor-core operands: rows padded to the 128-row tile, zero outside what
+  // each update writes. Complex64 updates (accepts and build chunks); FP64
+  // updates of up to f64tc_max_k() edges (and the FP64 build of M) on the
+  // tensor cores unless PNGF_F64_SIMT.
+  if (c64) {
+    h->kt_cap = (6 * std::max(kmax, kInitChunk) + 31) / 32 * 32;
     h->aop_rows = (n + 127) / 128 * 128;
     h->bop_rows = (2 * n + 127) / 128 * 128;
-    if ((rc = dalloc(h, &h->d_Aop, (size_t)h->aop_rows * h->kt_cap)) ||
-        (rc = dalloc(h, &h->d_Bop, (size_t)h->bop_rows * h->kt_cap)) || (rc = dalloc(h, &h->d_tc_err, 1)))
-      return fail(rc);
-    if (cudaMemset(h->d_Aop, 0, sizeof(float) * h->aop_rows * h->kt_cap) != cudaSuccess ||
-        cudaMemset(h->d_Bop, 0, sizeof(float) * h->bop_rows * h->kt_cap) != cudaSuccess ||
-        cudaMemset(h->d_tc_err, 0, sizeof(int)) != cudaSuccess)
-      return fail(PNGF_ERR_CUDA);
   }
-  if (c.fp64_update != PNGF_F64_SIMT) {  // FP64 updates (and the FP64 build of M) on the tensor cores
+  if (c.fp64_update != PNGF_F64_SIMT) {
     h->f64tc = true;
     h->init_chunk = f64tc_max_k();
     h->a16_rows = (rows + 127) / 128 * 128;
     h->b16_rows = (2 * (n + 1) + 127) / 128 * 128;
-    const size_t ca = (size_t)h->a16_rows * f64tc_op_cols(), cb = (size_t)h->b16_rows * f64tc_op_cols();
-    if (cudaMalloc(&h->d_A16, 2 * ca) != cudaSuccess || cudaMalloc(&h->d_B16, 2 * cb) != cudaSuccess)
-      return fail(PNGF_ERR_NOMEM);
-    if ((rc = dalloc(h, &h->d_eA, (size_t)h->a16_rows)) || (rc = dalloc(h, &h->d_fB, (size_t)h->b16_rows)) ||
-        (rc = dalloc(h, &h->d_tc_err, 1)))
-      return fail(rc);
-    if (cudaMemset(h->d_A16, 0, 2 * ca) != cudaSuccess || cudaMemset(h->d_B16, 0, 2 * cb) != cudaSuccess ||
-        cudaMemset(h->d_tc_err, 0, sizeof(int)) != cudaSuccess)
+  }
+  if ((rc = dalloc(h, &h->d_tc_err, 1))) return fail(rc);
+  if (cudaMemset(h->d_tc_err, 0, sizeof(int)) != cudaSuccess) return fail(PNGF_ERR_CUDA);
+  // One lane (stream + accept scratch) per frequency; one lane on the
+  // handle's stream for a state_only handle, which keeps device memory to the state.
+  h->lanes.resize(c.state_only ? 1 : c.num_freq);
+  if (h->lanes.size() > 1 && cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess)
+    return fail(PNGF_ERR_CUDA);
+  for (Lane &L : h->lanes) {
+    if (h->lanes.size() > 1 && (cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking) != cudaSuccess ||
+                                cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming) != cudaSuccess))
       return fail(PNGF_ERR_CUDA);
+    if ((rc = dalloc(h, &L.A, (size_t)rows * h->acc_cap)) || (rc = dalloc(h, &L.W, (size_t)h->acc_cap * h->ldm)) ||
+        (rc = dalloc(h, &L.LU, (size_t)h->acc_cap * h->acc_cap)) || (rc = dalloc(h, &L.piv, (size_t)h->acc_cap)) ||
+        (rc = dalloc(h, &L.z, (size_t)h->acc_cap)))
+      return fail(rc);
+    if (c64) {
+      if ((rc = dalloc(h, &L.Aop, (size_t)h->aop_rows * h->kt_cap)) ||
+          (rc = dalloc(h, &L.Bop, (size_t)h->bop_rows * h->kt_cap)))
+        return fail(rc);
+      if (cudaMemset(L.Aop, 0, sizeof(float) * h->aop_rows * h->kt_cap) != cudaSuccess ||
+          cudaMemset(L.Bop, 0, sizeof(float) * h->bop_rows * h->kt_cap) != cudaSuccess)
+        return fail(PNGF_ERR_CUDA);
+    }
+    if (h->f64tc) {
+      const size_t ca = (size_t)h->a16_rows * f64tc_op_cols(), cb = (size_t)h->b16_rows * f64tc_op_cols();
+      if (cudaMalloc(&L.A16, 2 * ca) != cudaSuccess || cudaMalloc(&L.B16, 2 * cb) != cudaSuccess)
+        return fail(PNGF_ERR_NOMEM);
+      if ((rc = dalloc(h, &L.eA, (size_t)h->a16_rows)) || (rc = dalloc(h, &L.fB, (size_t)h->b16_rows)))
+        return fail(rc);
+      if (cudaMemset(L.A16, 0, 2 * ca) != cudaSuccess || cudaMemset(L.B16, 0, 2 * cb) != cudaSuccess)
+        return fail(PNGF_ERR_CUDA);
+    }
   }
   {
     void *v = nullptr;
@@ -507,11 +558,9 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
   }
   if ((rc = dalloc(h, &h->d_fconst, (size_t)c.num_freq)) || (rc = dalloc(h, &h->d_Eincs, (size_t)c.num_freq)) ||
       (rc = dalloc(h, &h->d_tile_map, (size_t)h->map_sz)) || (rc = dalloc(h, &h->d_P, (size_t)n)) ||
-      (rc = dalloc(h, &h->d_first, 1)) || (rc = dalloc(h, &h->d_A, (size_t)rows * h->acc_cap)) ||
-      (rc = dalloc(h, &h->d_W, (size_t)h->acc_cap * h->ldm)) || (rc = dalloc(h, &h->d_acc_s, (size_t)n)) ||
-      (rc = dalloc(h, &h->d_acc_d, (size_t)n)) || (rc = dalloc(h, &h->d_LU, (size_t)h->acc_cap * h->acc_cap)) ||
-      (rc = dalloc(h, &h->d_piv, (size_t)h->acc_cap)) || (rc = dalloc(h, &h->d_z, (size_t)h->acc_cap)) ||
-      (rc = dalloc(h, &h->d_acc_status, 1)) || (rc = dalloc(h, &h->d_colmax, (size_t)n)) ||
+      (rc = dalloc(h, &h->d_first, 1)) || (rc = dalloc(h, &h->d_acc_s, (size_t)n)) ||
+      (rc = dalloc(h, &h->d_acc_d, (size_t)n)) || (rc = dalloc(h, &h->d_acc_status, 1)) ||
+      (rc = dalloc(h, &h->d_colmax, (size_t)n)) ||
       (rc = dalloc(h, &h->d_fbest, 1)))
     return fail(rc);
   if (cudaMemcpy(h->d_Eincs, einc.data(), sizeof(void *) * c.num_freq, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -691,12 +740,17 @@ static int prepare_impl(Handle *h, bool fp64) {
     if (c64 && fp64) PNGF_CUDA(h, launch_split_M(h, f));
     return PNGF_OK;
   };
-  for (int f = 0; f < h->cfg.num_freq; ++f) {
-    int rc = stage_in(h, f, true, true);
+  // frequencies build independently, one lane (stream + scratch) each
+  int rc = lanes_fork(h);
+  if (rc) return rc;
+  for (int f = 0; f < h->cfg.num_freq && rc == PNGF_OK; ++f) {
+    rc = stage_in(h, f, true, true);
     if (rc == PNGF_OK) rc = build(f);
     stage_out(h, f);
-    if (rc) return rc;
   }
+  const int rj = lanes_join(h);
+  if (rc) return rc;
+  if (rj) return rj;
   int st = 0, tc = 0;
   PNGF_CUDA(h, cudaMemcpyAsync(&st, h->d_acc_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   if (h->d_tc_err) PNGF_CUDA(h, cudaMemcpyAsync(&tc, h->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -950,8 +1004,12 @@ static int tune_update(Handle *h, pngf_tune *out) {
   const int widths[2] = {128, 64};
   const int k = std::min(h->kmax, 24);
   const long rows = h->n + h->E;
-  PNGF_CUDA(h, cudaMemsetAsync(h->d_A, 0, sizeof(double2) * rows * k, h->stream));
-  PNGF_CUDA(h, cudaMemsetAsync(h->d_W, 0, sizeof(double2) * k * h->ldm, h->stream));
+  int rc = lanes_fork(h);  // frequency 0's lane runs the timed updates
+  if (rc) return rc;
+  Lane &L = lane_of(h, 0);
+  cudaStream_t st = lane_stream(h, 0);
+  PNGF_CUDA(h, cudaMemsetAsync(L.A, 0, sizeof(double2) * rows * k, st));
+  PNGF_CUDA(h, cudaMemsetAsync(L.W, 0, sizeof(double2) * k * h->ldm, st));
   cudaEvent_t a = nullptr, b = nullptr;
   if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
     if (a) cudaEventDestroy(a);
@@ -969,9 +1027,9 @@ static int tune_update(Handle *h, pngf_tune *out) {
     out->update_cols[i] = widths[i];
     out->update_us[i] = -1.0;
     if ((e = launch_c64_update(h, 0, k)) != cudaSuccess) break;  // warm-up
-    cudaEventRecord(a, h->stream);
+    cudaEventRecord(a, st);
     for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_c64_update(h, 0, k);
-    cudaEventRecord(b, h->stream);
+    cudaEventRecord(b, st);
     if (e == cudaSuccess) e = cudaEventSynchronize(b);
     float ms = 0.f;
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
@@ -989,6 +1047,7 @@ static int tune_update(Handle *h, pngf_tune *out) {
   out->update_form = bi;
   out->update_forms = 2;
   if (e != cudaSuccess) return cuda_check(h, e, "autotune (update)");
+  if ((rc = lanes_join(h))) return rc;
   int tc = 0;
   PNGF_CUDA(h, cudaMemcpy(&tc, h->d_tc_err, sizeof(int), cudaMemcpyDeviceToHost));
   if (tc != 0) {

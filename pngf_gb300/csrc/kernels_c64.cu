@@ -500,7 +500,7 @@ cudaError_t make_map(CUtensorMap *m, const float *base, long rows, int K, long l
 cudaError_t launch_split_M(Handle *h, int f) {
   Freq &q = h->f[f];
   dim3 g((unsigned)((h->ldm + 255) / 256), (unsigned)(h->n + h->E));
-  k_split_M<<<g, 256, 0, h->stream>>>(q.M64, h->n, h->E, h->ldm, q.T32, q.y64, q.R64);
+  k_split_M<<<g, 256, 0, lane_stream(h, f)>>>(q.M64, h->n, h->E, h->ldm, q.T32, q.y64, q.R64);
   h->nlaunch += 1;
   return cudaGetLastError();
 }
@@ -537,19 +537,21 @@ cudaError_t launch_c64_update(Handle *h, int f, int k) {
   if (e != cudaSuccess) return e;
   const int Kt = (6 * k + TC_BK - 1) / TC_BK * TC_BK;
   if (Kt > h->kt_cap) return cudaErrorInvalidValue;
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
   // FP64 side: y and R/Eobj
   const long side = n + (long)h->E * (n + 1);
-  k_c64_side_update<<<(unsigned)((side + 255) / 256), 256, 0, h->stream>>>(q.y64, q.R64, n, h->E, h->ldm, h->d_A,
-                                                                           rows, h->d_W, k);
+  k_c64_side_update<<<(unsigned)((side + 255) / 256), 256, 0, st>>>(q.y64, q.R64, n, h->E, h->ldm, L.A, rows, L.W,
+                                                                    k);
   // tensor-core operands
   const dim3 ga((unsigned)((Kt + 127) / 128), (unsigned)n), gb((unsigned)((Kt + 127) / 128), (unsigned)(2 * n));
-  k_build_Aop<<<ga, 128, 0, h->stream>>>(h->d_A, rows, n, k, Kt, h->kt_cap, h->d_Aop);
-  k_build_Bop<<<gb, 128, 0, h->stream>>>(h->d_W, h->ldm, n, k, Kt, h->kt_cap, h->d_Bop);
+  k_build_Aop<<<ga, 128, 0, st>>>(L.A, rows, n, k, Kt, h->kt_cap, L.Aop);
+  k_build_Bop<<<gb, 128, 0, st>>>(L.W, h->ldm, n, k, Kt, h->kt_cap, L.Bop);
   const int bn = h->c64_cols == 64 ? 64 : 128;
   const int dcols = (int)(2 * n);
   CUtensorMap ma, mb, md;
-  if ((e = make_map(&ma, h->d_Aop, h->aop_rows, Kt, h->kt_cap, TC_BM)) != cudaSuccess) return e;
-  if ((e = make_map(&mb, h->d_Bop, h->bop_rows, Kt, h->kt_cap, bn)) != cudaSuccess) return e;
+  if ((e = make_map(&ma, L.Aop, h->aop_rows, Kt, h->kt_cap, TC_BM)) != cudaSuccess) return e;
+  if ((e = make_map(&mb, L.Bop, h->bop_rows, Kt, h->kt_cap, bn)) != cudaSuccess) return e;
   if ((e = make_map(&md, reinterpret_cast<const float *>(q.T32), n, dcols, 2 * h->ldm, TC_BM)) != cudaSuccess)
     return e;
   if (g_c64_sms == 0) {
@@ -560,23 +562,23 @@ cudaError_t launch_c64_update(Handle *h, int f, int k) {
   }
   const int ncb = (dcols + bn - 1) / bn, ntiles = ncb * (int)((n + TC_BM - 1) / TC_BM);
   const int grid = ntiles < g_c64_sms ? ntiles : g_c64_sms;
-  cudaEvent_t t0 = timing_mark(h);
+  cudaEvent_t t0 = timing_mark(h, st);
   if (bn == 64) {
     if ((e = cudaFuncSetAttribute(k_tc_update<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)C64Tile<64>::SMEM)) != cudaSuccess)
       return e;
-    k_tc_update<64><<<grid, TC_THREADS, C64Tile<64>::SMEM, h->stream>>>(ma, mb, md, dcols, ncb, ntiles, Kt / TC_BK,
-                                                                         h->d_tc_err);
+    k_tc_update<64><<<grid, TC_THREADS, C64Tile<64>::SMEM, st>>>(ma, mb, md, dcols, ncb, ntiles, Kt / TC_BK,
+                                                                  h->d_tc_err);
   } else {
     if ((e = cudaFuncSetAttribute(k_tc_update<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)C64Tile<128>::SMEM)) != cudaSuccess)
       return e;
-    k_tc_update<128><<<grid, TC_THREADS, C64Tile<128>::SMEM, h->stream>>>(ma, mb, md, dcols, ncb, ntiles,
-                                                                           Kt / TC_BK, h->d_tc_err);
+    k_tc_update<128><<<grid, TC_THREADS, C64Tile<128>::SMEM, st>>>(ma, mb, md, dcols, ncb, ntiles, Kt / TC_BK,
+                                                                    h->d_tc_err);
   }
   const double cells = (double)n * (double)n;  // complex entries of T updated
   timing_close(h, t0, T_UPDATE, 8.0 * k * cells,
-               2.0 * 8.0 * cells + 4.0 * Kt * ((double)h->aop_rows + (double)h->bop_rows), 0.0);
+               2.0 * 8.0 * cells + 4.0 * Kt * ((double)h->aop_rows + (double)h->bop_rows), 0.0, st);
   h->nlaunch += 4;
   return cudaGetLastError();
 }

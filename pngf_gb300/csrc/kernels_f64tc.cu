@@ -438,15 +438,17 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
   const int kop = (FB_S * k2p + 63) / 64 * 64;
   const int natoms = kop / 64;
   const long ldk = (long)f64tc_op_cols();
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
   // operand rows have pitch ldk; each update fills its rows up to the pitch
-  k_slice_A<<<(unsigned)((rows + 127) / 128), 128, 0, h->stream>>>(
-      A, rows, rows, k, k2p, (int)ldk, static_cast<__nv_bfloat16 *>(h->d_A16), h->d_eA);
-  k_slice_B<<<(unsigned)((cols + 127) / 128), 128, 0, h->stream>>>(
-      W, h->ldm, cols, k, k2p, (int)ldk, static_cast<__nv_bfloat16 *>(h->d_B16), h->d_fB);
+  k_slice_A<<<(unsigned)((rows + 127) / 128), 128, 0, st>>>(A, rows, rows, k, k2p, (int)ldk,
+                                                            static_cast<__nv_bfloat16 *>(L.A16), L.eA);
+  k_slice_B<<<(unsigned)((cols + 127) / 128), 128, 0, st>>>(W, h->ldm, cols, k, k2p, (int)ldk,
+                                                            static_cast<__nv_bfloat16 *>(L.B16), L.fB);
   CUtensorMap ma, mb, md;
   cudaError_t e;
-  if ((e = make_map_bf16(&ma, h->d_A16, h->a16_rows, kop, ldk, FB_BM)) != cudaSuccess) return e;
-  if ((e = make_map_bf16(&mb, h->d_B16, h->b16_rows, kop, ldk, FB_BN)) != cudaSuccess) return e;
+  if ((e = make_map_bf16(&ma, L.A16, h->a16_rows, kop, ldk, FB_BM)) != cudaSuccess) return e;
+  if ((e = make_map_bf16(&mb, L.B16, h->b16_rows, kop, ldk, FB_BN)) != cudaSuccess) return e;
   if ((e = make_map_f64(&md, reinterpret_cast<const double *>(M), rows, cols, 2 * h->ldm)) != cudaSuccess) return e;
   if (g_num_sms == 0) {
     int dev = 0;
@@ -465,14 +467,13 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
   const int nrb = (int)((rows + FB_BM - 1) / FB_BM), ncb = (int)((cols + FB_BN - 1) / FB_BN);
   const int ntiles = nrb * ncb;
   const int grid = ntiles < g_num_sms ? ntiles : g_num_sms;
-  cudaEvent_t t0 = timing_mark(h);
-  k_tc_update_f64<<<grid, FB_THREADS, smem, h->stream>>>(ma, mb, md, (int)rows, (int)cols, ncb, ntiles, natoms, k2p, nd,
-                                                         h->d_eA, h->d_fB, h->d_tc_err);
+  cudaEvent_t t0 = timing_mark(h, st);
+  k_tc_update_f64<<<grid, FB_THREADS, smem, st>>>(ma, mb, md, (int)rows, (int)cols, ncb, ntiles, natoms, k2p, nd,
+                                                  L.eA, L.fB, h->d_tc_err);
   const double cells = (double)rows * (double)(n + 1);
   timing_close(h, t0, T_UPDATE, 8.0 * k * cells, 2.0 * 16.0 * cells + 2.0 * kop * ((double)rows + (double)cols),
-               0.0);
+               0.0, st);
   h->nlaunch += 3;
-  (void)f;
   return cudaGetLastError();
 }
 

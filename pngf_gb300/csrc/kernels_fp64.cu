@@ -854,19 +854,19 @@ size_t view_bytes() { return sizeof(SV<double2>) > sizeof(SV<float2>) ? sizeof(S
 cudaError_t launch_init_M(Handle *h, int f) {
   Freq &q = h->f[f];
   const long n = h->n;
+  cudaStream_t st = lane_stream(h, f);
   dim3 tb(32, 8), tg((unsigned)((h->ldm + 31) / 32), (unsigned)((n + 31) / 32));
-  k_init_M_tile<<<tg, tb, 0, h->stream>>>(q.G, n, h->ldm, q.M64);
+  k_init_M_tile<<<tg, tb, 0, st>>>(q.G, n, h->ldm, q.M64);
   long *d_port = nullptr;
-  cudaError_t e = cudaMallocAsync(&d_port, sizeof(long) * h->port.size(), h->stream);
+  cudaError_t e = cudaMallocAsync(&d_port, sizeof(long) * h->port.size(), st);
   if (e != cudaSuccess) return e;
-  e = cudaMemcpyAsync(d_port, h->port.data(), sizeof(long) * h->port.size(), cudaMemcpyHostToDevice, h->stream);
+  e = cudaMemcpyAsync(d_port, h->port.data(), sizeof(long) * h->port.size(), cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return e;
-  k_init_M_rows<<<(unsigned)((h->ldm + 255) / 256), 256, 0, h->stream>>>(q.G, q.gobj, n, h->E, h->ldm, d_port,
-                                                                         (int)h->port.size(), q.M64, q.Einc);
+  k_init_M_rows<<<(unsigned)((h->ldm + 255) / 256), 256, 0, st>>>(q.G, q.gobj, n, h->E, h->ldm, d_port,
+                                                                  (int)h->port.size(), q.M64, q.Einc);
   const double k0 = 2.0 * M_PI * h->cfg.freq_hz[f] / 2.997924579998211e8;
-  k_port_const<<<1, 1, 0, h->stream>>>(q.Einc, q.gobj, n, h->E, d_port, (int)h->port.size(), k0,
-                                       h->d_fconst + f);
-  cudaFreeAsync(d_port, h->stream);
+  k_port_const<<<1, 1, 0, st>>>(q.Einc, q.gobj, n, h->E, d_port, (int)h->port.size(), k0, h->d_fconst + f);
+  cudaFreeAsync(d_port, st);
   h->nlaunch += 3;
   return cudaGetLastError();
 }
@@ -975,26 +975,28 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   Freq &q = h->f[f];
   const long n = h->n, rows = n + h->E;
   if (k <= 0) return cudaSuccess;
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
   cudaError_t e;
   if (layout == PNGF_PREC_C64) {
-    e = accept_prologue<float2>(view32(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, h->d_LU, h->d_piv, h->d_z,
-                                h->d_A, h->d_W, h->d_acc_status, h->stream);
+    e = accept_prologue<float2>(view32(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, L.LU, L.piv, L.z, L.A, L.W,
+                                h->d_acc_status, st);
     if (e != cudaSuccess) return e;
     h->nlaunch += 3;
     return launch_c64_update(h, f, k);
   }
-  e = accept_prologue<double2>(view64(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, h->d_LU, h->d_piv, h->d_z,
-                               h->d_A, h->d_W, h->d_acc_status, h->stream);
+  e = accept_prologue<double2>(view64(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, L.LU, L.piv, L.z, L.A, L.W,
+                               h->d_acc_status, st);
   if (e != cudaSuccess) return e;
   if (h->f64tc && k <= f64tc_max_k()) {
     h->nlaunch += 3;
-    return launch_f64tc_update(h, f, k, q.M64, h->d_A, h->d_W);
+    return launch_f64tc_update(h, f, k, q.M64, L.A, L.W);
   }
   dim3 g((unsigned)((n + 1 + RU_T - 1) / RU_T), (unsigned)((rows + RU_T - 1) / RU_T));
-  cudaEvent_t t0 = timing_mark(h);
-  k_rank_update<<<g, 256, 0, h->stream>>>(q.M64, h->ldm, rows, n + 1, h->d_A, rows, h->d_W, h->ldm, k);
+  cudaEvent_t t0 = timing_mark(h, st);
+  k_rank_update<<<g, 256, 0, st>>>(q.M64, h->ldm, rows, n + 1, L.A, rows, L.W, h->ldm, k);
   const double cells = (double)rows * (double)(n + 1);
-  timing_close(h, t0, T_UPDATE, 8.0 * k * cells, 2.0 * 16.0 * cells + 16.0 * k * (double)(rows + n + 1), 0.0);
+  timing_close(h, t0, T_UPDATE, 8.0 * k * cells, 2.0 * 16.0 * cells + 16.0 * k * (double)(rows + n + 1), 0.0, st);
   h->nlaunch += 4;
   return cudaGetLastError();
 }

@@ -49,6 +49,24 @@ struct Freq {
   double synth_eps = 1.0;
 };
 
+// Accept scratch and stream of one frequency ("lane"). The frequencies of an
+// accept, and of a design build, are independent: with one lane per frequency
+// they run on their own streams and overlap on the GPU. A state_only handle
+// has a single lane on the handle's stream (its frequencies run in turn).
+struct Lane {
+  cudaStream_t stream = nullptr;  // own stream (several lanes only)
+  cudaEvent_t done = nullptr;
+  double2 *A = nullptr;           // (N+E) x acc_cap, column-major (ld = N+E)
+  double2 *W = nullptr;           // acc_cap x ldm row-major
+  double2 *LU = nullptr;          // acc_cap^2
+  double2 *z = nullptr;           // acc_cap
+  int *piv = nullptr;             // acc_cap
+  float *Aop = nullptr;           // complex64 update operands: aop_rows x kt_cap fp32, K-major
+  float *Bop = nullptr;           // bop_rows x kt_cap
+  void *A16 = nullptr, *B16 = nullptr;  // FP64 tensor-core update: bf16 slices, a16_rows / b16_rows x f64tc_op_cols()
+  int *eA = nullptr, *fB = nullptr;     // per-row / per-column power-of-two scales
+};
+
 struct Handle {
   pngf_config cfg{};
   long n = 0;        // design edges
@@ -64,15 +82,13 @@ struct Handle {
   FreqConst *d_fconst = nullptr;
   void *d_views = nullptr;     // device array of per-frequency state views (kernels_fp64.cu)
   void **d_Eincs = nullptr;    // device array of per-frequency Einc pointers
-  // C64 tensor-core update operands (kernels_c64.cu)
-  float *d_Aop = nullptr;      // rows_pad x kt_cap fp32, K-major
-  float *d_Bop = nullptr;      // cols_pad x kt_cap fp32, K-major
+  // per-frequency accept scratch and streams
+  std::vector<Lane> lanes;
+  cudaEvent_t ev_fork = nullptr;
+  // tensor-core update operand shapes (kernels_c64.cu, kernels_f64tc.cu)
   int kt_cap = 0;
   long aop_rows = 0, bop_rows = 0;
   int *d_tc_err = nullptr;     // set by bounded waits in the tensor-core kernels
-  // FP64 tensor-core update operands (kernels_f64tc.cu)
-  void *d_A16 = nullptr, *d_B16 = nullptr;  // bf16 slices, a16_rows / b16_rows x f64tc_op_cols()
-  int *d_eA = nullptr, *d_fB = nullptr;     // per-row / per-column power-of-two scales
   long a16_rows = 0, b16_rows = 0;
   bool f64tc = false;                       // FP64 updates of up to f64tc_max_k() edges on tensor cores
   int init_chunk = kInitChunk;
@@ -109,16 +125,11 @@ struct Handle {
   std::vector<int> batch_tiles, batch_nflip;
   std::vector<int> last_k, last_status;   // per-candidate edge count / status of the host-API batch
 
-  // accept scratch
-  int acc_cap = 0;                  // columns of A / rows of W
-  double2 *d_A = nullptr;           // (N+E) x acc_cap, column-major (ld = N+E)
-  double2 *d_W = nullptr;           // acc_cap x ldm row-major
+  // accept
+  int acc_cap = 0;                  // columns of A / rows of W in each lane
   int *d_acc_s = nullptr;            // explicit edge list (init chunks)
   signed char *d_acc_d = nullptr;
-  double2 *d_LU = nullptr;          // acc_cap^2
-  int *d_piv = nullptr;             // acc_cap
-  double2 *d_z = nullptr;           // acc_cap
-  int *d_acc_status = nullptr;
+  int *d_acc_status = nullptr;      // sticky: PNGF_ERR_SINGULAR from any lane
   unsigned long long *d_colmax = nullptr;  // N words of scratch for the synthetic G generator
 
   // host staging (pinned)
@@ -141,13 +152,21 @@ struct Handle {
   std::string err;
 };
 
+// The lane of frequency f and the stream its work goes to.
+inline Lane &lane_of(Handle *h, int f) { return h->lanes[(size_t)f % h->lanes.size()]; }
+inline cudaStream_t lane_stream(const Handle *h, int f) {
+  return h->lanes.size() < 2 ? h->stream : h->lanes[(size_t)f % h->lanes.size()].stream;
+}
+
 // Timing categories.
 enum { T_EVAL = 0, T_ACCEPT = 1, T_UPDATE = 2 };
-// Records an event on the handle's stream if timing is on (else nullptr).
-cudaEvent_t timing_mark(Handle *h);
-// Closes a span opened by timing_mark: category and algorithmic work
-// (T_EVAL: cand x freq, bytes, flops; T_UPDATE: flops, bytes).
-void timing_close(Handle *h, cudaEvent_t start, int cat, double x1, double x2, double x3);
+// Records an event on stream s (the handle's stream when null) if timing is
+// on (else nullptr).
+cudaEvent_t timing_mark(Handle *h, cudaStream_t s = nullptr);
+// Closes a span opened by timing_mark on the same stream: category and
+// algorithmic work (T_EVAL: cand x freq, bytes, flops; T_ACCEPT: frequencies;
+// T_UPDATE: flops, bytes).
+void timing_close(Handle *h, cudaEvent_t start, int cat, double x1, double x2, double x3, cudaStream_t s = nullptr);
 
 int set_error(Handle *h, int code, const std::string &msg);
 int cuda_check(Handle *h, cudaError_t e, const char *what);
@@ -181,7 +200,7 @@ int accept_cand_async(Handle *h, int c, int k, bool check_now);
 
 // ---- kernels (kernels_fp64.cu) ----
 // Builds M for P = 0 from G and the objective rows; computes Einc and the
-// port constants.
+// port constants (on the frequency's lane stream).
 cudaError_t launch_init_M(Handle *h, int f);
 // Per-candidate flipped-edge lists (sorted, deduplicated) from tile lists.
 cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const int *d_nflip);
@@ -194,16 +213,19 @@ bool eval_variant_ok(const Handle *h, int v);
 cudaError_t launch_current_objective(Handle *h);
 // Rank-k accept of an explicit edge list (device arrays s, d of length k) at
 // frequency f, on the FP64 layout (M64) or the complex64 layout (layout =
-// PNGF_PREC_C64: T32 on tensor cores, y64 / R64 in FP64).
+// PNGF_PREC_C64: T32 on tensor cores, y64 / R64 in FP64), with the
+// frequency's lane scratch, on its lane stream.
 cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k, int layout);
 // Uploads the per-frequency state views for the handle's precision.
 cudaError_t setup_views(Handle *h);
 size_t view_bytes();
 // ---- complex64 form (kernels_c64.cu) ----
-// Splits the FP64 M of frequency f into T32 (complex64), y64 and R64.
+// Splits the FP64 M of frequency f into T32 (complex64), y64 and R64 (on the
+// frequency's lane stream).
 cudaError_t launch_split_M(Handle *h, int f);
-// After the accept prologue (h->d_A, h->d_W in FP64): updates y64 and R64 in
-// FP64 and T32 -= A W on the tensor cores (3xTF32 split products).
+// After the accept prologue (A, W in FP64 in the frequency's lane): updates
+// y64 and R64 in FP64 and T32 -= A W on the tensor cores (3xTF32 split
+// products), on the lane's stream.
 cudaError_t launch_c64_update(Handle *h, int f, int k);
 // Reassembles frequency f's M in FP64 (into M64) from T32, y64, R64.
 cudaError_t launch_merge_M(Handle *h, int f);
@@ -219,7 +241,8 @@ cudaError_t launch_synth_G(Handle *h, int f, double2 *G, long ldg, unsigned long
 // ---- FP64-accurate update on the tensor cores (kernels_f64tc.cu) ----
 int f64tc_max_k();
 size_t f64tc_op_cols();
-// M -= A W for M ((N+E) x ldm complex128), A ((N+E) x k column-major), W (k x ldm).
+// M -= A W for M ((N+E) x ldm complex128), A ((N+E) x k column-major), W (k x ldm),
+// with frequency f's lane scratch and stream.
 cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W);
 // Commits P and the tile map on the device for candidate c of the batch.
 cudaError_t launch_commit(Handle *h, int c);
