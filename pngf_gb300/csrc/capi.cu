@@ -516,7 +516,7 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
     h->f64tc = true;
     h->init_chunk = f64tc_max_k();
     h->a16_rows = (rows + 127) / 128 * 128;
-    h->b16_rows = (2 * (n + 1) + 127) / 128 * 128;
+    h->b16_rows = f64tc_b_rows(n);
   }
   if ((rc = dalloc(h, &h->d_tc_err, 1))) return fail(rc);
   if (cudaMemset(h->d_tc_err, 0, sizeof(int)) != cudaSuccess) return fail(PNGF_ERR_CUDA);
@@ -542,10 +542,11 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
         return fail(PNGF_ERR_CUDA);
     }
     if (h->f64tc) {
-      const size_t ca = (size_t)h->a16_rows * f64tc_op_cols(), cb = (size_t)h->b16_rows * f64tc_op_cols();
+      const size_t ca = (size_t)h->a16_rows * f64tc_op_cols(), cb = (size_t)h->b16_rows * f64tc_b_cols();
       if (cudaMalloc(&L.A16, 2 * ca) != cudaSuccess || cudaMalloc(&L.B16, 2 * cb) != cudaSuccess)
         return fail(PNGF_ERR_NOMEM);
-      if ((rc = dalloc(h, &L.eA, (size_t)h->a16_rows)) || (rc = dalloc(h, &L.fB, (size_t)h->b16_rows)))
+      // one scale per output column, padded to the 32-column tiles
+      if ((rc = dalloc(h, &L.eA, (size_t)h->a16_rows)) || (rc = dalloc(h, &L.fB, (size_t)(2 * (n + 1) + 127) / 128 * 128)))
         return fail(rc);
       if (cudaMemset(L.A16, 0, 2 * ca) != cudaSuccess || cudaMemset(L.B16, 0, 2 * cb) != cudaSuccess)
         return fail(PNGF_ERR_CUDA);

@@ -60,20 +60,22 @@ constexpr int FB_LMAX = 8;            // highest level kept (p + q <= 8)
 constexpr int FB_NLEV = FB_LMAX - 1;  // levels 2..8
 constexpr int FB_ACC = FB_NLEV * FB_BN;  // TMEM columns of one accumulator set (224)
 constexpr uint32_t FB_ATOM_A = FB_BM * 128;  // one 64-element K atom of the A tile
-constexpr uint32_t FB_ATOM_B = FB_BN * 128;
-constexpr int FB_MAX_ATOMS = 7;              // K extent up to 448 (k <= 32)
+constexpr int FB_MAX_ATOMS = 7;              // K extent of A up to 448 (k <= 32)
+constexpr int FB_BROWS = FB_S * FB_BN;       // B tile: the 7 slices of 32 output columns stacked along N
+constexpr uint32_t FB_BTILE = FB_BROWS * 128;  // 224 rows x one 64-element K atom (2k <= 64)
 constexpr int FB_EPI_WARPS = 16;
 constexpr int FB_THREADS = 96 + 32 * FB_EPI_WARPS;  // producer, MMA and store warps + epilogue
 constexpr uint32_t FB_DBOX = FB_BM * 128;           // 128 rows x 16 doubles of M (one TMA box)
 constexpr uint32_t FB_DTILE = 2 * FB_DBOX;          // a 128 x 32-double tile of M
 // Dynamic shared memory for natoms K atoms and nd staged tiles of M.
 constexpr size_t fb_smem(int natoms, int nd) {
-  return 1024 + (size_t)natoms * (FB_ATOM_A + 2 * FB_ATOM_B) + (size_t)nd * FB_DTILE + 256;
+  return 1024 + (size_t)natoms * FB_ATOM_A + 2 * FB_BTILE + (size_t)nd * FB_DTILE + 256;
 }
 
-// kind::f16 instruction descriptor: D f32, A and B bf16, K-major, N = 32, M = 128.
-constexpr uint32_t kIdescBF16 =
-    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(FB_BN >> 3) << 17) | ((uint32_t)(FB_BM >> 4) << 24);
+// kind::f16 instruction descriptor: D f32, A and B bf16, K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t idesc_bf16(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(FB_BM >> 4) << 24);
+}
 
 __device__ __forceinline__ int scale_exp(double m) {
   if (m == 0.0) return 0;
@@ -114,9 +116,14 @@ __global__ void k_slice_A(const double2 *__restrict__ A, long lda, long rows, in
   }
 }
 
-// B_op row j' < 2(N+1): output column j' = 2j (real part) or 2j+1 (imaginary)
-// of M[:, j]; W is k x ldw (row-major, complex).
-__global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, int k, int k2p, int ld,
+// B_op for output column j' < 2(N+1) (j' = 2j: real part, 2j+1: imaginary, of
+// M[:, j]; W is k x ldw, row-major complex). The 7 slices of the 32 output
+// columns of tile c = j' / 32 are stacked along N: slice q of column j' is row
+// c * 224 + (q - 1) * 32 + j' % 32, its 2k K entries (then zeros) in a row
+// of 64. A tile's MMA with A-slice p then takes rows of slices 1 .. 8 - p in one
+// instruction (N = (8 - p) * 32) and lands slice q in TMEM columns of level
+// p + q.
+__global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, int k,
                           __nv_bfloat16 *__restrict__ Bop, int *__restrict__ fB) {
   const long jp = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (jp >= ncols2) return;
@@ -129,13 +136,14 @@ __global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, 
   }
   const int f = scale_exp(m);
   fB[jp] = f;
-  __nv_bfloat16 *row = Bop + (size_t)jp * ld;
-  for (int c = 0; c < ld; ++c) row[c] = __float2bfloat16_rn(0.f);
+  __nv_bfloat16 *row = Bop + ((size_t)(jp / FB_BN) * FB_BROWS + (jp % FB_BN)) * 64;  // slice 1; slice q at +(q-1)*32 rows
+  for (int q = 0; q < FB_S; ++q)
+    for (int c = 2 * k; c < 64; ++c) row[(size_t)q * FB_BN * 64 + c] = __float2bfloat16_rn(0.f);
   for (int r = 0; r < k; ++r) {
     const double2 w = W[(size_t)r * ldw + j];
     // Re out: Re A Re W - Im A Im W; Im out: Re A Im W + Im A Re W
-    write_slices(im ? w.y : w.x, f, row + 2 * r, k2p);
-    write_slices(im ? w.x : -w.y, f, row + 2 * r + 1, k2p);
+    write_slices(im ? w.y : w.x, f, row + 2 * r, FB_BN * 64);
+    write_slices(im ? w.x : -w.y, f, row + 2 * r + 1, FB_BN * 64);
   }
 }
 
@@ -183,9 +191,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                                           ~static_cast<uintptr_t>(1023));
   const uint32_t sA = smem_u32(base);
-  const uint32_t bstride = (uint32_t)natoms * FB_ATOM_B;  // B buffer b at sB0 + b * bstride
-  const uint32_t sB0 = sA + (uint32_t)natoms * FB_ATOM_A;
-  const uint32_t dbase = (uint32_t)natoms * (FB_ATOM_A + 2 * FB_ATOM_B);  // byte offset of slot 0 from base
+  const uint32_t sB0 = sA + (uint32_t)natoms * FB_ATOM_A;  // B buffer b at sB0 + b * FB_BTILE
+  const uint32_t dbase = (uint32_t)natoms * FB_ATOM_A + 2 * FB_BTILE;  // byte offset of slot 0 from base
   const uint32_t sD0 = sA + dbase;
   uint64_t *bars = reinterpret_cast<uint64_t *>(base + dbase + (uint32_t)nd * FB_DTILE);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 16);
@@ -223,7 +230,7 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tslot;
-  const uint32_t a_bytes = (uint32_t)natoms * FB_ATOM_A, b_bytes = (uint32_t)natoms * FB_ATOM_B;
+  const uint32_t a_bytes = (uint32_t)natoms * FB_ATOM_A;
 
   if (warp == 0) {
     if (lane == 0) {
@@ -240,9 +247,8 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         }
         const int b = li & 1;
         if (li >= 2 && !mbar_wait(b_empty(b), ((li >> 1) - 1) & 1)) { ok = false; break; }
-        const uint32_t sB = sB0 + b * bstride;
-        mbar_expect_tx(b_full(b), b_bytes);
-        for (int a = 0; a < natoms; ++a) tma_load_2d(sB + a * FB_ATOM_B, &tmB, a * 64, cb * FB_BN, b_full(b));
+        mbar_expect_tx(b_full(b), FB_BTILE);
+        tma_load_2d(sB0 + b * FB_BTILE, &tmB, 0, cb * FB_BROWS, b_full(b));
         ++issuedB;
         const int s = li % nd;
         if (li >= nd && !mbar_wait(d_empty(s), ((li / nd) - 1) & 1)) { ok = false; break; }
@@ -274,21 +280,19 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
         if (!mbar_wait(b_full(b), (li >> 1) & 1)) { ok = false; break; }
         if (li >= 2 && !mbar_wait(acc_empty(b), ((li >> 1) - 1) & 1)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t sB = sB0 + b * bstride;
+        const uint32_t sB = sB0 + b * FB_BTILE;
         const uint32_t acc = tmem + (uint32_t)(b * 256);
-        for (int l = 2; l <= FB_LMAX; ++l) {
-          const uint32_t dcol = acc + (uint32_t)((l - 2) * FB_BN);
-          bool first = true;
-          for (int p = 1; p <= FB_S; ++p) {
-            const int q = l - p;
-            if (q < 1 || q > FB_S) continue;
-            for (int kc = 0; kc < k2p; kc += 16) {
-              const int oa = (p - 1) * k2p + kc, ob = (q - 1) * k2p + kc;
-              const uint64_t ad = sw128_desc(sA + (oa >> 6) * FB_ATOM_A + (oa & 63) * 2);
-              const uint64_t bd = sw128_desc(sB + (ob >> 6) * FB_ATOM_B + (ob & 63) * 2);
-              mma_bf16(dcol, ad, bd, kIdescBF16, first ? 0u : 1u);
-              first = false;
-            }
+        // A-slice p against B-slices 1 .. 8-p in one MMA (N = (8-p) * 32): the
+        // product with slice q lands in the columns of level l = p + q (levels
+        // 2..8 at columns 32 (l-2)). p = 1 covers every level and starts them.
+        for (int p = 1; p <= FB_S; ++p) {
+          const uint32_t dcol = acc + (uint32_t)((p - 1) * FB_BN);
+          const uint32_t idesc = idesc_bf16((FB_LMAX - p) * FB_BN);
+          for (int kc = 0; kc < k2p; kc += 16) {
+            const int oa = (p - 1) * k2p + kc;
+            const uint64_t ad = sw128_desc(sA + (oa >> 6) * FB_ATOM_A + (oa & 63) * 2);
+            const uint64_t bd = sw128_desc(sB + kc * 2);
+            mma_bf16(dcol, ad, bd, idesc, (p > 1 || kc > 0) ? 1u : 0u);
           }
         }
         mma_commit(b_empty(b));
@@ -430,6 +434,10 @@ int f64tc_max_k() { return 32; }
 
 size_t f64tc_op_cols() { return (size_t)FB_MAX_ATOMS * 64; }
 
+size_t f64tc_b_cols() { return 64; }
+
+long f64tc_b_rows(long n) { return (2 * (n + 1) + FB_BN - 1) / FB_BN * FB_BROWS; }
+
 cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W) {
   const long n = h->n, rows = n + h->E;
   const long cols = 2 * (n + 1);
@@ -443,12 +451,12 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
   // operand rows have pitch ldk; each update fills its rows up to the pitch
   k_slice_A<<<(unsigned)((rows + 127) / 128), 128, 0, st>>>(A, rows, rows, k, k2p, (int)ldk,
                                                             static_cast<__nv_bfloat16 *>(L.A16), L.eA);
-  k_slice_B<<<(unsigned)((cols + 127) / 128), 128, 0, st>>>(W, h->ldm, cols, k, k2p, (int)ldk,
+  k_slice_B<<<(unsigned)((cols + 127) / 128), 128, 0, st>>>(W, h->ldm, cols, k,
                                                             static_cast<__nv_bfloat16 *>(L.B16), L.fB);
   CUtensorMap ma, mb, md;
   cudaError_t e;
   if ((e = make_map_bf16(&ma, L.A16, h->a16_rows, kop, ldk, FB_BM)) != cudaSuccess) return e;
-  if ((e = make_map_bf16(&mb, L.B16, h->b16_rows, kop, ldk, FB_BN)) != cudaSuccess) return e;
+  if ((e = make_map_bf16(&mb, L.B16, h->b16_rows, 64, (long)f64tc_b_cols(), FB_BROWS)) != cudaSuccess) return e;
   if ((e = make_map_f64(&md, reinterpret_cast<const double *>(M), rows, cols, 2 * h->ldm)) != cudaSuccess) return e;
   if (g_num_sms == 0) {
     int dev = 0;

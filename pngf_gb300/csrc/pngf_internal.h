@@ -63,7 +63,8 @@ struct Lane {
   int *piv = nullptr;             // acc_cap
   float *Aop = nullptr;           // complex64 update operands: aop_rows x kt_cap fp32, K-major
   float *Bop = nullptr;           // bop_rows x kt_cap
-  void *A16 = nullptr, *B16 = nullptr;  // FP64 tensor-core update: bf16 slices, a16_rows / b16_rows x f64tc_op_cols()
+  void *A16 = nullptr, *B16 = nullptr;  // FP64 tensor-core update: bf16 slices, a16_rows x f64tc_op_cols(),
+                                        // b16_rows x f64tc_b_cols()
   int *eA = nullptr, *fB = nullptr;     // per-row / per-column power-of-two scales
 };
 
@@ -240,7 +241,9 @@ cudaError_t launch_drift_rows(Handle *h, int f, const int *d_rows, int nr, const
 cudaError_t launch_synth_G(Handle *h, int f, double2 *G, long ldg, unsigned long long *colmax);
 // ---- FP64-accurate update on the tensor cores (kernels_f64tc.cu) ----
 int f64tc_max_k();
-size_t f64tc_op_cols();
+size_t f64tc_op_cols();  // row pitch of the A slices (elements)
+size_t f64tc_b_cols();   // row pitch of the B slices (elements)
+long f64tc_b_rows(long n);  // rows of the B slices: 7 per output column, 32-column tiles stacked
 // M -= A W for M ((N+E) x ldm complex128), A ((N+E) x k column-major), W (k x ldm),
 // with frequency f's lane scratch and stream.
 cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W);
