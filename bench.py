@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--no-converge", action="store_true",
                     help="skip the wall time to convergence, plain FP64 DBS against proposal + complex64 DBS")
     ap.add_argument("--no-group", action="store_true", help="skip the many-instance group run")
+    ap.add_argument("--c5", action="store_true",
+                    help="only the learned-proposal form at 41x41 tiles x 4 frequencies against plain FP64 DBS")
     ap.add_argument("--instances", type=int, default=64, help="group run: DBS instances")
     ap.add_argument("--group-evals", type=int, default=400, help="group run: flip evaluations per instance")
     ap.add_argument("--group-batch", type=int, default=64, help="group run: speculative batch per instance")
@@ -274,23 +276,24 @@ def autotune_on(h, mode_single=True):
     return t
 
 
-def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_steps=600, topk=64):
+def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), train_evals=1500, train_steps=600,
+                     topk=64, state_only=0):
     """Wall time to the converged objective: plain FP64 DBS (reference order,
     run until the hat is empty) against the proposal + complex64 form, whose
     network is trained only on plain complex64 runs from other seeds. The
     proposal run stops once its objective is within 1e-3 relative of the plain
-    run's final objective (or at its own convergence)."""
+    run's final objective (or at its own convergence). load_G(handle) loads
+    every frequency's G."""
     import torch
     from pngf_gb300 import lib
-    out = {}
+    out = {"tiles": tiles, "freqs_ghz": [f / 1e9 for f in freqs]}
     nfl = 1
-    h = lib.Handle(a.tiles, a.tiles, FREQS, precision=lib.PREC_FP64, max_flips=nfl, device=local)
-    for f, G in enumerate(Gs):
-        h.load_G(f, G, None)
+    h = lib.Handle(tiles, tiles, freqs, precision=lib.PREC_FP64, max_flips=nfl, device=local, state_only=state_only)
+    load_G(h)
     tune64 = autotune_on(h)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0)
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, batch=0)
     torch.cuda.synchronize()
     t_prep = time.perf_counter() - t0
     s = d.run()
@@ -304,16 +307,16 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
     h.close()
     torch.cuda.empty_cache()
     # complex64 state built directly in complex64 on the tensor cores
-    h = lib.Handle(a.tiles, a.tiles, FREQS, precision=lib.PREC_C64, max_flips=nfl, device=local,
-                   c64_build=lib.BUILD_C64)
-    for f, G in enumerate(Gs):
-        h.load_G(f, G, None)
+    h = lib.Handle(tiles, tiles, freqs, precision=lib.PREC_C64, max_flips=nfl, device=local,
+                   c64_build=lib.BUILD_C64, state_only=state_only)
+    load_G(h)
     prop = lib.Proposal(h, channels=32, seed=1)
     t0 = time.perf_counter()
+    pairs = 0
     for sd in train_seeds:  # training pairs from plain complex64 runs of other designs
         d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=sd, max_evals=train_evals)
         lib.dbs_set_proposal(d, prop, topk=0)
-        d.run()
+        pairs += d.run().launched  # every evaluated candidate is a (design, exact gain) pair
         d.close()
     t_collect = time.perf_counter() - t0
     t0 = time.perf_counter()
@@ -324,7 +327,7 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
     tune32 = autotune_on(h)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0, drift_every=32, drift_tol=1e-4)
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, batch=0, drift_every=32, drift_tol=1e-4)
     lib.dbs_set_proposal(d, prop, topk=topk, train_every=8, train_steps=20, train_batch=32, lr=1e-3)
     torch.cuda.synchronize()
     t_prep = time.perf_counter() - t0
@@ -351,7 +354,8 @@ def converge_compare(a, Gs, local, train_seeds=(2, 3), train_evals=1500, train_s
                            "eval_form": tune32["eval_form"], "update_cols": tune32["update"][tune32["update_form"]]["cols"],
                            "reached_target": t_reach is not None,
                            "training": {"seeds": list(train_seeds), "collect_s": t_collect, "train_s": t_train,
-                                        "samples": samples, "final_loss": loss, "steps": train_steps}}
+                                        "samples": samples, "pairs": pairs, "final_loss": loss,
+                                        "steps": train_steps}}
     out["F_target"] = F_target
     if t_reach:
         out["speedup_wall_to_objective"] = out["plain_fp64"]["wall_s"] / t_reach
@@ -454,6 +458,24 @@ def group_bench(a, local, n_check=8):
     return out
 
 
+FREQS_C5 = [28.0e9, 29.33e9, 30.67e9, 32.0e9]
+
+
+def c5_run(a, local):
+    """The learned-proposal form at 41x41 tiles (N = 30504), 4 frequencies,
+    synthetic G generated on the device: wall time to the converged objective
+    of plain FP64 DBS against proposal + complex64 DBS (network trained on
+    plain complex64 runs of other seeds at this size). One JSON line."""
+    import torch
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    out = converge_compare(41, FREQS_C5, lambda h: [h.load_G_synth(f, seed=1) for f in range(len(FREQS_C5))],
+                           a.seed, local, train_evals=3000, train_steps=1000)
+    print(json.dumps({"metric": "wall time to converged objective, 41x41 tiles x 4 frequencies, proposal + "
+                                "complex64 vs plain FP64", "c5": out, "total_s": time.perf_counter() - t0}),
+          flush=True)
+
+
 def reduce_form(r, dist, device="cuda"):
     """Whole-job figures: sums of work over ranks, max of times over ranks
     (each rank runs its own DBS instance; the job ends with the slowest)."""
@@ -488,7 +510,10 @@ def gpu_arm(a, world, rank, local):
     if "c64" in forms:
         r32 = run_form(a, lib.PREC_C64, Gs, rank, local, dist)
         c64_red = reduce_form(r32, dist)
-    conv = converge_compare(a, Gs, local) if (not a.no_converge and rank == 0) else None
+    conv = None
+    if not a.no_converge and rank == 0:
+        conv = converge_compare(a.tiles, FREQS, lambda h: [h.load_G(f, G, None) for f, G in enumerate(Gs)], a.seed,
+                                local)
     del Gs
     grp = group_bench(a, local) if (not a.no_group and rank == 0) else None
     if rank != 0:
@@ -661,6 +686,10 @@ def main():
     a = parse()
     FREQS = FREQS[:max(1, min(a.nfreq, len(FREQS)))]
     world, rank, local = dist_env()
+    if a.c5:
+        if rank == 0:
+            c5_run(a, local)
+        return
     if a.impl == "reference":
         reference_arm(a, world, rank)
     else:
