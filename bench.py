@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--mode", choices=["single", "sym"], default="single")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--forms", default="fp64,c64", help="precision forms to run; the first is the headline")
+    ap.add_argument("--forms", default="fp64,c64,c64d", help="precision forms to run; the first is the headline")
     ap.add_argument("--nfreq", type=int, default=5, help="use the first NFREQ of the five frequencies")
     ap.add_argument("--no-converge", action="store_true",
                     help="skip the wall time to convergence, plain FP64 DBS against proposal + complex64 DBS")
@@ -223,13 +223,13 @@ def cpu_baseline_sample(tiles, mode, seed, freq, gpu_evals, gpu_accepts, nf, bud
     }
 
 
-def run_form(a, precision, Gs, rank, local, dist):
+def run_form(a, precision, Gs, rank, local, dist, defer_rank=0):
     """Runs W + K DBS decisions of one precision form; returns its counters."""
     import torch
     from pngf_gb300 import lib
     t_setup = time.perf_counter()
     h = lib.Handle(a.tiles, a.tiles, FREQS, precision=precision, max_flips=1 if a.mode == "single" else 4,
-                   device=local)
+                   device=local, defer_rank=defer_rank)
     for f, G in enumerate(Gs):
         h.load_G(f, G, None)
     d = lib.Dbs(h, mode=lib.DBS_SINGLE if a.mode == "single" else lib.DBS_SYMMETRIC, init=lib.INIT_RANDOM,
@@ -510,6 +510,10 @@ def gpu_arm(a, world, rank, local):
     if "c64" in forms:
         r32 = run_form(a, lib.PREC_C64, Gs, rank, local, dist)
         c64_red = reduce_form(r32, dist)
+    r32d = None
+    if "c64d" in forms:  # complex64 with the rank-k updates deferred to rank 192
+        r32d = run_form(a, lib.PREC_C64, Gs, rank, local, dist, defer_rank=192)
+        c64d_red = reduce_form(r32d, dist)
     conv = None
     if not a.no_converge and rank == 0:
         conv = converge_compare(a.tiles, FREQS, lambda h: [h.load_G(f, G, None) for f, G in enumerate(Gs)], a.seed,
@@ -602,14 +606,12 @@ def gpu_arm(a, world, rank, local):
             "fp64_gemm_tflops": fp64_peak, "autotune": r64["tune"],
         },
     }
-    if r32 is not None:
+    def c64_block(r32, c64_red, what):
         w32, d32, e32, acc32, l32 = c64_red
         t32 = r32["tm"]
         u32 = t32["update_ms"] * 1e-3
-        line["c64_form"] = {
-            "what": "T in complex64, rank-k update on tcgen05 tensor cores (kind::tf32, 3xTF32 split products, "
-                    "FP32 accumulation in TMEM); capacitance LU, y, R, Eobj, objective and accept test in FP64; "
-                    "same workload and steps",
+        return {
+            "what": what,
             "value": e32 / d32 if d32 > 0 else None, "e2e": e32 / w32, "unit": "flip_evals/s",
             "evals": e32, "accepts": acc32, "F_init": r32["F_init"], "F_best": r32["F_best"],
             "F_best_rel_diff_vs_fp64": abs(r32["F_best"] - r64["F_best"]) / abs(r64["F_best"]),
@@ -627,10 +629,29 @@ def gpu_arm(a, world, rank, local):
                 if t32["accept_ms"] > 0 else None,
                 "launch_ms": t32["update_ms"] / max(1, t32["update_launches"]),
                 "algorithmic_bytes_per_launch": t32["update_bytes"] / max(1, t32["update_launches"]),
+                # 3xTF32: the tensor pipe does 3 real products per complex-equivalent
+                # flop counted in update_flop (8 r N^2 per launch of rank r)
+                "tensor_view": {
+                    "tf32_tflops": 3.0 * t32["update_flop"] / u32 / 1e12 if u32 > 0 else None,
+                    "peak_tflops": peaks["bf16_tflops"] / 2.0,
+                    "peak_source": "half the measured dense BF16 rate (TF32 runs at half the BF16 rate)",
+                    "frac": 3.0 * t32["update_flop"] / u32 / 1e12 / (peaks["bf16_tflops"] / 2.0) if u32 > 0 else None,
+                },
             },
             "clocks": r32["clocks"], "gpu_launches": t32["kernel_launches"], "setup_s": r32["setup_s"],
             "autotune": r32["tune"],
         }
+
+    if r32 is not None:
+        line["c64_form"] = c64_block(
+            r32, c64_red, "T in complex64, rank-k update on tcgen05 tensor cores (kind::tf32, 3xTF32 split products, "
+                          "FP32 accumulation in TMEM) at every accept; capacitance LU, y, R, Eobj, objective and accept "
+                          "test in FP64; same workload and steps")
+    if r32d is not None:
+        line["c64_deferred_form"] = c64_block(
+            r32d, c64d_red, "the complex64 form with the T part of each accept appended to pending rank-k factors "
+                            "(candidates and accepts read T minus the pending product) and flushed to T on the tensor "
+                            "cores when the pending rank reaches 192 - 24: roofline per flush launch")
     if conv is not None:
         line["converge"] = conv
     if grp is not None:

@@ -325,10 +325,20 @@ int accept_cand_async(Handle *h, int c, int k, bool check_now) {
   cudaEvent_t t0 = timing_mark(h);
   int rc;
   if ((rc = lanes_fork(h))) return rc;
-  for (int f = 0; f < h->cfg.num_freq; ++f)
-    PNGF_CUDA(h, launch_accept_edges(h, f, h->d_es + (size_t)c * h->kmax, h->d_ed + (size_t)c * h->kmax, k,
-                                     h->cfg.precision));
+  // deferred complex64 updates: append this accept to the pending factors and
+  // flush them to T when another accept might not fit
+  h->defer_now = h->defer_cap > 0;
+  h->defer_flush = h->defer_now && h->defer_rp + k + h->kmax > h->defer_cap;
+  for (int f = 0; f < h->cfg.num_freq && rc == PNGF_OK; ++f)
+    rc = cuda_check(h, launch_accept_edges(h, f, h->d_es + (size_t)c * h->kmax, h->d_ed + (size_t)c * h->kmax, k,
+                                           h->cfg.precision), "accept");
+  h->defer_now = false;
+  if (rc) return rc;
   if ((rc = lanes_join(h))) return rc;
+  if (h->defer_cap > 0) {
+    h->defer_rp = h->defer_flush ? 0 : h->defer_rp + k;
+    PNGF_CUDA(h, launch_set_pending_rank(h));
+  }
   timing_close(h, t0, T_ACCEPT, (double)h->cfg.num_freq, 0.0, 0.0);
   PNGF_CUDA(h, launch_commit(h, c));
   if (h->d_tc_err && check_now) {  // the tensor-core kernels' bounded waits report here (else at the next collect)
@@ -391,6 +401,8 @@ int pngf_destroy(pngf_handle *ph) {
     dfree(q.T32);
     dfree(q.y64);
     dfree(q.R64);
+    dfree(q.U);
+    dfree(q.Vt);
   }
   dfree(h->d_fconst);
   dfree(h->d_views);
@@ -453,6 +465,9 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
   if (c.state_only != 0 && c.state_only != 1) return PNGF_ERR_ARG;
   const int kmax = c.max_flips * edges_per_tile(c);
   if (kmax > kMaxEvalK) return PNGF_ERR_UNSUPPORTED;
+  // deferred updates (complex64): the pending rank must hold at least one accept
+  const int defer_cap = c.precision == PNGF_PREC_C64 ? c.defer_rank : 0;
+  if (defer_cap < 0 || (defer_cap > 0 && (defer_cap < kmax || defer_cap > kMaxDeferRank))) return PNGF_ERR_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= c.device || c.device < 0) {
     cudaGetLastError();
@@ -476,6 +491,7 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
   h->ey_ysz = c.tiles_y * c.cells_y;
   h->nx = (long)h->ex_xsz * h->ex_ysz;
   h->kmax = kmax;
+  h->defer_cap = defer_cap;
   h->acc_cap = std::max(kmax, kInitChunk);
   h->f.resize(c.num_freq);
   h->h_fconst.resize(c.num_freq);
@@ -501,6 +517,9 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
     if (c64 && ((rc = dalloc(h, &q.T32, (size_t)n * h->ldm)) || (rc = dalloc(h, &q.y64, (size_t)n)) ||
                 (rc = dalloc(h, &q.R64, (size_t)h->E * h->ldm))))
       return fail(rc);
+    if (defer_cap > 0 &&
+        ((rc = dalloc(h, &q.U, (size_t)n * defer_cap)) || (rc = dalloc(h, &q.Vt, (size_t)n * defer_cap))))
+      return fail(rc);
     einc[f] = q.Einc;
   }
   // Tensor-core operands: rows padded to the 128-row tile, zero outside what
@@ -508,7 +527,7 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
   // updates of up to f64tc_max_k() edges (and the FP64 build of M) on the
   // tensor cores unless PNGF_F64_SIMT.
   if (c64) {
-    h->kt_cap = (6 * std::max(kmax, kInitChunk) + 31) / 32 * 32;
+    h->kt_cap = (6 * std::max(std::max(kmax, kInitChunk), defer_cap) + 31) / 32 * 32;
     h->aop_rows = (n + 127) / 128 * 128;
     h->bop_rows = (2 * n + 127) / 128 * 128;
   }
@@ -685,6 +704,20 @@ int pngf_set_source_port(pngf_handle *ph, int tile_x, int tile_y, int y_offset, 
   return PNGF_OK;
 }
 
+// Deferred complex64 updates: subtracts the pending factors from T at every
+// frequency (before anything reads T32 directly).
+static int flush_pending(Handle *h) {
+  if (h->defer_rp == 0) return PNGF_OK;
+  int rc = lanes_fork(h);
+  for (int f = 0; f < h->cfg.num_freq && rc == PNGF_OK; ++f) rc = cuda_check(h, launch_c64_flush(h, f), "flush");
+  const int rj = lanes_join(h);
+  if (rc) return rc;
+  if (rj) return rj;
+  h->defer_rp = 0;
+  PNGF_CUDA(h, launch_set_pending_rank(h));
+  return PNGF_OK;
+}
+
 // state_only handles: frequency f's G (regenerated; need_G) and, for a
 // complex64 handle, its FP64 staging of M (need_M64) exist on the device
 // only between stage_in and stage_out. No-ops otherwise.
@@ -717,6 +750,8 @@ static int prepare_impl(Handle *h, bool fp64) {
     if (!h->f[f].loaded) return set_error(h, PNGF_ERR_STATE, "G not loaded for frequency " + std::to_string(f));
   if (!h->have_map) return set_error(h, PNGF_ERR_STATE, "tile map not set");
   if (!h->have_port) return set_error(h, PNGF_ERR_STATE, "source port not set");
+  h->defer_rp = 0;  // a build starts from G: nothing is pending (build chunks are not deferred)
+  PNGF_CUDA(h, launch_set_pending_rank(h));
   // Set edges of the design, ascending; M is built from P = 0 by accepting
   // them in chunks (every chunk is a +1 flip of those edges).
   std::vector<int> on;
@@ -811,7 +846,9 @@ int pngf_get_M(pngf_handle *ph, int f, double *M, long ld, double *einc) {
   if (!h || !M || f < 0 || f >= h->cfg.num_freq || ld < h->n + 1) return PNGF_ERR_ARG;
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
   const long rows = h->n + h->E;
-  int rc = stage_in(h, f, false, true);
+  int rc = flush_pending(h);
+  if (rc) return rc;
+  rc = stage_in(h, f, false, true);
   auto copy = [&]() -> int {
     if (h->cfg.precision == PNGF_PREC_C64) PNGF_CUDA(h, launch_merge_M(h, f));  // M64 is staging in this mode
     PNGF_CUDA(h, cudaMemcpy2DAsync(M, sizeof(double2) * ld, h->f[f].M64, sizeof(double2) * h->ldm,
@@ -902,6 +939,10 @@ static int drift_impl(Handle *h, int f0, int f1, int nrows, double *max_rel) {
     return set_error(h, PNGF_ERR_UNSUPPORTED, "drift check applies to PNGF_PREC_C64 handles");
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
   if (nrows < 1 || nrows > 8) return set_error(h, PNGF_ERR_ARG, "drift check samples 1 to 8 rows");
+  {
+    const int rf = flush_pending(h);  // the check reads T32 directly
+    if (rf) return rf;
+  }
   const long n = h->n;
   std::vector<int> on, rows(nrows);
   for (long e = 0; e < n; ++e)

@@ -270,6 +270,57 @@ __global__ void k_build_Bop(const double2 *__restrict__ W, long ldw, long n, int
   Bop[(size_t)jp * ldk + c] = v;
 }
 
+// Deferred updates: appends the T part of an accept to the pending factors,
+// U[i][rp + c] = A[i][c] and Vt[j][rp + c] = W[c][j] (i, j < N), in complex64.
+__global__ void k_defer_append(const double2 *__restrict__ A, long lda, const double2 *__restrict__ W, long ldw,
+                               long n, int k, int rp, int rcap, float2 *__restrict__ U, float2 *__restrict__ Vt) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int c = 0; c < k; ++c) {
+    const double2 a = A[(size_t)c * lda + i], w = W[(size_t)c * ldw + i];
+    U[(size_t)i * rcap + rp + c] = make_float2((float)a.x, (float)a.y);
+    Vt[(size_t)i * rcap + rp + c] = make_float2((float)w.x, (float)w.y);
+  }
+}
+
+// A_op and B_op (as k_build_Aop / k_build_Bop) from the pending factors:
+// A = U (rows i, rank r), W[r][j] = Vt[j][r].
+__global__ void k_build_Aop_f(const float2 *__restrict__ U, int rcap, long n, int k, int Kt, long ldk,
+                              float *__restrict__ Aop) {
+  const long i = (long)blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || c >= Kt) return;
+  float v = 0.f;
+  const int k2 = 2 * k;
+  if (c < 3 * k2) {
+    const int seg = c / k2, w = c - seg * k2, r = w >> 1;
+    const float2 a = U[(size_t)i * rcap + r];
+    const float x = (w & 1) ? a.y : a.x;
+    const float hi = to_tf32(x);
+    v = seg == 2 ? to_tf32(x - hi) : hi;
+  }
+  Aop[(size_t)i * ldk + c] = v;
+}
+
+__global__ void k_build_Bop_f(const float2 *__restrict__ Vt, int rcap, long n, int k, int Kt, long ldk,
+                              float *__restrict__ Bop) {
+  const long jp = (long)blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jp >= 2 * n || c >= Kt) return;
+  float v = 0.f;
+  const int k2 = 2 * k;
+  if (c < 3 * k2) {
+    const int seg = c / k2, w = c - seg * k2, r = w >> 1;
+    const float2 wv = Vt[(size_t)(jp >> 1) * rcap + r];
+    float b;
+    if ((jp & 1) == 0) b = (w & 1) ? -wv.y : wv.x;  // Re out: Re A Re W - Im A Im W
+    else b = (w & 1) ? wv.x : wv.y;                 // Im out: Re A Im W + Im A Re W
+    const float hi = to_tf32(b);
+    v = seg == 1 ? to_tf32(b - hi) : hi;
+  }
+  Bop[(size_t)jp * ldk + c] = v;
+}
+
 // FP64 part of the complex64 accept: y_i -= sum_r A[i,r] W[r,N] (i < N) and
 // R[e, j] -= sum_r A[N+e, r] W[r, j] (j <= N).
 __global__ void k_c64_side_update(double2 *__restrict__ y64, double2 *__restrict__ R64, long n, int E, long ldm,
@@ -530,23 +581,17 @@ cudaError_t launch_merge_M(Handle *h, int f) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_c64_update(Handle *h, int f, int k) {
+namespace {
+
+// T32 -= A_op B_op^T from the lane's operands (built for K = Kt), on the
+// lane's stream; rank is the complex rank the operands carry (for the timing).
+cudaError_t launch_c64_tc(Handle *h, int f, int Kt, int rank) {
   Freq &q = h->f[f];
-  const long n = h->n, rows = n + h->E;
+  const long n = h->n;
   cudaError_t e = get_encoder();
   if (e != cudaSuccess) return e;
-  const int Kt = (6 * k + TC_BK - 1) / TC_BK * TC_BK;
-  if (Kt > h->kt_cap) return cudaErrorInvalidValue;
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
-  // FP64 side: y and R/Eobj
-  const long side = n + (long)h->E * (n + 1);
-  k_c64_side_update<<<(unsigned)((side + 255) / 256), 256, 0, st>>>(q.y64, q.R64, n, h->E, h->ldm, L.A, rows, L.W,
-                                                                    k);
-  // tensor-core operands
-  const dim3 ga((unsigned)((Kt + 127) / 128), (unsigned)n), gb((unsigned)((Kt + 127) / 128), (unsigned)(2 * n));
-  k_build_Aop<<<ga, 128, 0, st>>>(L.A, rows, n, k, Kt, h->kt_cap, L.Aop);
-  k_build_Bop<<<gb, 128, 0, st>>>(L.W, h->ldm, n, k, Kt, h->kt_cap, L.Bop);
   const int bn = h->c64_cols == 64 ? 64 : 128;
   const int dcols = (int)(2 * n);
   CUtensorMap ma, mb, md;
@@ -577,10 +622,73 @@ cudaError_t launch_c64_update(Handle *h, int f, int k) {
                                                                     h->d_tc_err);
   }
   const double cells = (double)n * (double)n;  // complex entries of T updated
-  timing_close(h, t0, T_UPDATE, 8.0 * k * cells,
+  timing_close(h, t0, T_UPDATE, 8.0 * rank * cells,
                2.0 * 8.0 * cells + 4.0 * Kt * ((double)h->aop_rows + (double)h->bop_rows), 0.0, st);
-  h->nlaunch += 4;
+  h->nlaunch += 1;
   return cudaGetLastError();
+}
+
+cudaError_t launch_side_update(Handle *h, int f, int k) {
+  Freq &q = h->f[f];
+  const long n = h->n, rows = n + h->E;
+  Lane &L = lane_of(h, f);
+  const long side = n + (long)h->E * (n + 1);
+  k_c64_side_update<<<(unsigned)((side + 255) / 256), 256, 0, lane_stream(h, f)>>>(q.y64, q.R64, n, h->E, h->ldm,
+                                                                                   L.A, rows, L.W, k);
+  h->nlaunch += 1;
+  return cudaGetLastError();
+}
+
+int kt_of(int rank) { return (6 * rank + TC_BK - 1) / TC_BK * TC_BK; }
+
+}  // namespace
+
+cudaError_t launch_c64_update(Handle *h, int f, int k) {
+  const long n = h->n, rows = n + h->E;
+  const int Kt = kt_of(k);
+  if (Kt > h->kt_cap) return cudaErrorInvalidValue;
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
+  cudaError_t e = launch_side_update(h, f, k);  // FP64 side: y and R/Eobj
+  if (e != cudaSuccess) return e;
+  const dim3 ga((unsigned)((Kt + 127) / 128), (unsigned)n), gb((unsigned)((Kt + 127) / 128), (unsigned)(2 * n));
+  k_build_Aop<<<ga, 128, 0, st>>>(L.A, rows, n, k, Kt, h->kt_cap, L.Aop);
+  k_build_Bop<<<gb, 128, 0, st>>>(L.W, h->ldm, n, k, Kt, h->kt_cap, L.Bop);
+  h->nlaunch += 2;
+  return launch_c64_tc(h, f, Kt, k);
+}
+
+cudaError_t launch_c64_flush(Handle *h, int f) {
+  const long n = h->n;
+  const int rank = h->defer_rp;
+  if (rank <= 0) return cudaSuccess;
+  const int Kt = kt_of(rank);
+  if (Kt > h->kt_cap) return cudaErrorInvalidValue;
+  Freq &q = h->f[f];
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
+  const dim3 ga((unsigned)((Kt + 127) / 128), (unsigned)n), gb((unsigned)((Kt + 127) / 128), (unsigned)(2 * n));
+  k_build_Aop_f<<<ga, 128, 0, st>>>(q.U, h->defer_cap, n, rank, Kt, h->kt_cap, L.Aop);
+  k_build_Bop_f<<<gb, 128, 0, st>>>(q.Vt, h->defer_cap, n, rank, Kt, h->kt_cap, L.Bop);
+  h->nlaunch += 2;
+  return launch_c64_tc(h, f, Kt, rank);
+}
+
+cudaError_t launch_c64_defer(Handle *h, int f, int k) {
+  const long n = h->n, rows = n + h->E;
+  Freq &q = h->f[f];
+  Lane &L = lane_of(h, f);
+  cudaError_t e = launch_side_update(h, f, k);
+  if (e != cudaSuccess) return e;
+  k_defer_append<<<(unsigned)((n + 127) / 128), 128, 0, lane_stream(h, f)>>>(L.A, rows, L.W, h->ldm, n, k,
+                                                                               h->defer_rp, h->defer_cap, q.U, q.Vt);
+  h->nlaunch += 1;
+  if ((e = cudaGetLastError()) != cudaSuccess || !h->defer_flush) return e;
+  const int rp = h->defer_rp;
+  h->defer_rp = rp + k;  // the flush covers the accept just appended
+  e = launch_c64_flush(h, f);
+  h->defer_rp = rp;
+  return e;
 }
 
 }  // namespace pngf

@@ -71,6 +71,11 @@ template <> __device__ __forceinline__ double2 ldM<float2>(const float2 *M, size
 // objective rows (R[e*ldr + j], with Eobj_e at column N). In the FP64 layout
 // all three live in M; in the complex64 layout T is stored in complex64 and y,
 // R, Eobj stay in FP64.
+//
+// Deferred updates (complex64 layout, rp > 0): the stored T lags the true T
+// by the pending rank-rp correction, T_true = T - U Vt^T with U and Vt N x rp
+// complex64 (row i of each at [i * rcap]); t() returns T_true, the correction
+// summed in FP32.
 template <typename TM> struct SV {
   const TM *T;
   long ldt;
@@ -78,7 +83,25 @@ template <typename TM> struct SV {
   long ys;
   const double2 *R;
   long ldr;
-  __device__ __forceinline__ double2 t(size_t i, size_t j) const { return ldM(T, i * ldt + j); }
+  const float2 *U = nullptr;
+  const float2 *Vt = nullptr;
+  int rp = 0;
+  int rcap = 0;
+  __device__ __forceinline__ double2 t(size_t i, size_t j) const {
+    double2 v = ldM(T, i * ldt + j);
+    if (rp > 0) {
+      const float2 *u = U + i * rcap, *w = Vt + j * rcap;
+      float cx = 0.f, cy = 0.f;
+      for (int q = 0; q < rp; ++q) {
+        const float2 a = u[q], b = w[q];
+        cx = fmaf(a.x, b.x, fmaf(-a.y, b.y, cx));
+        cy = fmaf(a.x, b.y, fmaf(a.y, b.x, cy));
+      }
+      v.x -= (double)cx;
+      v.y -= (double)cy;
+    }
+    return v;
+  }
   __device__ __forceinline__ double2 yv(size_t i) const { return y[i * ys]; }
   __device__ __forceinline__ double2 r(int e, size_t j) const { return R[(size_t)e * ldr + j]; }
 };
@@ -834,7 +857,12 @@ static SV<double2> view64(const Handle *h, int f) {
   return SV<double2>{M, h->ldm, M + h->n, h->ldm, M + (size_t)h->n * h->ldm, h->ldm};
 }
 static SV<float2> view32(const Handle *h, int f) {
-  return SV<float2>{h->f[f].T32, h->ldm, h->f[f].y64, 1, h->f[f].R64, h->ldm};
+  SV<float2> v{h->f[f].T32, h->ldm, h->f[f].y64, 1, h->f[f].R64, h->ldm};
+  v.U = h->f[f].U;
+  v.Vt = h->f[f].Vt;
+  v.rp = h->defer_rp;
+  v.rcap = h->defer_cap;
+  return v;
 }
 
 cudaError_t setup_views(Handle *h) {
@@ -850,6 +878,17 @@ cudaError_t setup_views(Handle *h) {
 }
 
 size_t view_bytes() { return sizeof(SV<double2>) > sizeof(SV<float2>) ? sizeof(SV<double2>) : sizeof(SV<float2>); }
+
+__global__ void k_set_pending_rank(SV<float2> *views, int nf, int rp) {
+  if (threadIdx.x < nf) views[threadIdx.x].rp = rp;
+}
+
+cudaError_t launch_set_pending_rank(Handle *h) {
+  if (h->cfg.precision != PNGF_PREC_C64) return cudaSuccess;
+  k_set_pending_rank<<<1, 32, 0, h->stream>>>(static_cast<SV<float2> *>(h->d_views), h->cfg.num_freq, h->defer_rp);
+  h->nlaunch += 1;
+  return cudaGetLastError();
+}
 
 cudaError_t launch_init_M(Handle *h, int f) {
   Freq &q = h->f[f];
@@ -983,7 +1022,7 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
                                 h->d_acc_status, st);
     if (e != cudaSuccess) return e;
     h->nlaunch += 3;
-    return launch_c64_update(h, f, k);
+    return h->defer_now ? launch_c64_defer(h, f, k) : launch_c64_update(h, f, k);
   }
   e = accept_prologue<double2>(view64(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, L.LU, L.piv, L.z, L.A, L.W,
                                h->d_acc_status, st);

@@ -20,6 +20,8 @@ constexpr int kInitChunk = 96;
 // factor and W solve cost O(k^3) and O(k^2 N) in FP64, the tensor-core update
 // O(1) passes over T, so mid-sized chunks are cheapest.
 constexpr int kC64BuildChunk = 48;
+// Largest pending rank of deferred complex64 updates.
+constexpr int kMaxDeferRank = 256;
 
 // Forms of the candidate kernel the autotuner chooses from: warps working on
 // one (candidate, frequency) and candidates per CTA. Index 0 is the default.
@@ -44,6 +46,8 @@ struct Freq {
   double2 *y64 = nullptr;    // C64 mode: y (N) in FP64
   double2 *R64 = nullptr;    // C64 mode: R and Eobj (E x ldm row-major, Eobj at column N) in FP64
   bool loaded = false;
+  float2 *U = nullptr;       // C64 with deferred updates: pending factors, N x defer_cap each
+  float2 *Vt = nullptr;      //   (T_true = T32 - U Vt^T over the first defer_rp columns)
   bool synth = false;        // G is the built-in synthetic G (generated on the device)
   unsigned long long synth_seed = 0;
   double synth_eps = 1.0;
@@ -95,6 +99,10 @@ struct Handle {
   int init_chunk = kInitChunk;
   int eval_variant = 0;                     // index into kEvalForms (set by the autotuner)
   int c64_cols = 128;                       // output tile width of the complex64 update (64 or 128)
+  int defer_cap = 0;                        // C64: pending rank at which deferred updates are flushed (0 = off)
+  int defer_rp = 0;                         //   rank pending now (same at every frequency)
+  bool defer_now = false;                   //   accepts being launched are deferred (DBS accepts, not builds)
+  bool defer_flush = false;                 //   the accept being launched flushes after appending
   std::vector<FreqConst> h_fconst;
 
   // design
@@ -217,6 +225,8 @@ cudaError_t launch_current_objective(Handle *h);
 // PNGF_PREC_C64: T32 on tensor cores, y64 / R64 in FP64), with the
 // frequency's lane scratch, on its lane stream.
 cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k, int layout);
+// Writes h->defer_rp into the device copies of the complex64 views (stream-ordered).
+cudaError_t launch_set_pending_rank(Handle *h);
 // Uploads the per-frequency state views for the handle's precision.
 cudaError_t setup_views(Handle *h);
 size_t view_bytes();
@@ -228,6 +238,13 @@ cudaError_t launch_split_M(Handle *h, int f);
 // y64 and R64 in FP64 and T32 -= A W on the tensor cores (3xTF32 split
 // products), on the lane's stream.
 cudaError_t launch_c64_update(Handle *h, int f, int k);
+// Deferred form of the update: y64 and R64 updated in FP64 now, the T part
+// appended to the pending factors (U gets A's T rows, Vt gets W's T columns,
+// in complex64); with h->defer_flush the pending rank-(defer_rp + k) product
+// is then subtracted from T32 on the tensor cores.
+cudaError_t launch_c64_defer(Handle *h, int f, int k);
+// Subtracts the pending product U Vt^T (rank h->defer_rp) from T32 of frequency f.
+cudaError_t launch_c64_flush(Handle *h, int f);
 // Reassembles frequency f's M in FP64 (into M64) from T32, y64, R64.
 cudaError_t launch_merge_M(Handle *h, int f);
 // FP64 rows of T for the current design at rows d_rows (nr <= 8) by iterative
