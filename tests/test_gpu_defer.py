@@ -28,35 +28,45 @@ def make(c, Gs, gobj, tm, prec, defer_rank=0):
     return h
 
 
-def test_deferred_accepts_match_immediate(cases, built_lib):
+@pytest.mark.parametrize("cap", [48, 192])
+def test_deferred_accepts_match_immediate(cap, cases, built_lib):
+    """cap 48: a flush every accept or two (k <= 24); cap 192: nothing flushed
+    until the state is read. Both complex64 forms are compared with the FP64
+    form: deferral may not make the complex64 error more than twice larger."""
     from pngf_gb300 import lib
     c = cases["sym_9x9_f2_seed3"]
     Gs, gobj = case_G(c, built_lib)
     a = c["tiles"]
     rng = np.random.default_rng(21)
     tm = [int(v) for v in rng.integers(0, 2, a * a)]
+    h64 = make(c, Gs, gobj, tm, lib.PREC_FP64)
     h0 = make(c, Gs, gobj, tm, lib.PREC_C64)
-    h1 = make(c, Gs, gobj, tm, lib.PREC_C64, defer_rank=48)  # flush every accept or two at k <= 24
+    h1 = make(c, Gs, gobj, tm, lib.PREC_C64, defer_rank=cap)
     mid = (a - 1) // 2
     pool = [t for t in range(a * a) if t not in (mid * a + mid, mid * a + mid - 1, mid * a + mid + 1)]
     for step in range(7):
         cands = [[int(t)] for t in rng.choice(pool, size=30, replace=False)]
+        _, F64 = h64.eval_candidates(cands)
         _, F0 = h0.eval_candidates(cands)
         _, F1 = h1.eval_candidates(cands)
         np.testing.assert_allclose(F1, F0, rtol=1e-6)
-        pick = int(np.nanargmin(F0))
-        h0.accept(pick)
-        h1.accept(pick)
+        np.testing.assert_allclose(F1, F64, rtol=1e-6)
+        pick = int(np.nanargmin(F64))
+        for h in (h64, h0, h1):
+            h.accept(pick)
     n = h0.n
     for f in range(len(Gs)):
+        M64, _ = h64.get_M(f)
         M0, _ = h0.get_M(f)
         M1, _ = h1.get_M(f)  # flushes what is pending
-        scale = np.abs(M0[:n, :n]).max()
-        assert np.abs(M1[:n, :n] - M0[:n, :n]).max() <= 5e-6 * scale
-        np.testing.assert_allclose(M1[n:], M0[n:], rtol=0, atol=1e-6 * np.abs(M0[n:]).max())
-    assert abs(h1.objective() - h0.objective()) <= 1e-6 * abs(h0.objective())
-    h0.close()
-    h1.close()
+        scale = np.abs(M64[:n, :n]).max()
+        e0 = np.abs(M0[:n, :n] - M64[:n, :n]).max()
+        e1 = np.abs(M1[:n, :n] - M64[:n, :n]).max()
+        assert e1 <= 2.0 * e0 + 1e-6 * scale, (f, e0 / scale, e1 / scale)
+        np.testing.assert_allclose(M1[n:], M64[n:], rtol=0, atol=1e-5 * np.abs(M64[n:]).max())
+    assert abs(h1.objective() - h64.objective()) <= 1e-6 * abs(h64.objective())
+    for h in (h64, h0, h1):
+        h.close()
 
 
 def test_deferred_dbs_reaches_fp64_objective(cases, built_lib):
