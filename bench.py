@@ -524,9 +524,9 @@ def gpu_arm(a, world, rank, local):
         if dist:
             dist.destroy_process_group()
         return
-    if r64 is None:  # complex64 form alone (profiling runs)
-        print(json.dumps({"c64_only": {k: v for k, v in r32.items() if k != "tm"}, "timing": r32["tm"]}),
-              flush=True)
+    if r64 is None:  # complex64 forms alone (profiling runs)
+        print(json.dumps({name: {"counters": {k: v for k, v in r.items() if k != "tm"}, "timing": r["tm"]}
+                          for name, r in (("c64", r32), ("c64d", r32d)) if r is not None}), flush=True)
         return
     tm, n = r64["tm"], r64["n"]
     upd_s = tm["update_ms"] * 1e-3
