@@ -10,15 +10,18 @@
 // K = 6k accumulates hi*hi + hi*lo + lo*hi in FP32 (TMEM). The small parts of
 // the state that feed the objective (y, R, Eobj) are updated in FP64.
 //
-// Kernel k_tc_update: one CTA per 128 x 128 output tile, 6 warps:
-//   warp 0  TMA producer: 128B-swizzled K-major tiles of A_op and B_op into a
-//           2-stage shared-memory ring (mbarrier complete_tx), 3 CTAs per SM;
-//   warp 1  TMEM allocation and a single elected thread issuing
-//           tcgen05.mma.cta_group::1.kind::tf32 (M=128, N=128, K=8) into a
-//           128-column FP32 accumulator in TMEM, tcgen05.commit per stage;
-//   warps 2-5 epilogue: tcgen05.ld 32x32b rows of the accumulator, D -= acc.
-// Every mbarrier wait is bounded; on timeout the kernel records an error code,
-// drains its own TMA copies, frees its TMEM and returns.
+// Kernel k_tc_update (persistent, one CTA per SM, described at the kernel):
+// TMA-staged tiles of T, an operand ring for A_op / B_op, two TMEM
+// accumulators, eight epilogue warps and a TMA-store warp. Every mbarrier
+// wait is bounded; on timeout the kernel records an error code, drains its own
+// TMA copies, frees its TMEM and returns.
+//
+// Deferred updates: an accept appends its T part to pending factors U, Vt
+// (k_defer_append) and the pending product is flushed by the same kernel with
+// K = 6 x the pending rank (k_build_Aop_f / k_build_Bop_f build its operands).
+//
+// Drift check kernels (k_rows_*) and the FP64 <-> complex64 state conversion
+// (k_split_M, k_merge_M) are here too.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
