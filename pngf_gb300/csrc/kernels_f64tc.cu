@@ -77,42 +77,79 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(FB_BM >> 4) << 24);
 }
 
-__device__ __forceinline__ int scale_exp(double m) {
-  if (m == 0.0) return 0;
-  return ilogb(m) + 1;  // m * 2^-e < 1
+// Power-of-two row / column scale e with max |x| 2^-e < 1, from the largest
+// |x|'s bit pattern (non-negative doubles order like unsigned integers).
+__device__ __forceinline__ int scale_exp_bits(unsigned long long mb) {
+  if (mb == 0) return 0;
+  const int be = (int)(mb >> 52);
+  if (be > 0) return be - 1022;                        // ilogb + 1
+  return (63 - __clzll((long long)mb)) - 1074 + 1;     // subnormal maximum
 }
 
-// Writes the 7 slices of x * 2^-e (|x 2^-e| < 1) into dst[0], dst[stride], ...
-__device__ __forceinline__ void write_slices(double x, int e, __nv_bfloat16 *dst, int stride) {
-  double r = ldexp(x, -e);
-#pragma unroll
-  for (int p = 0; p < FB_S; ++p) {
-    const double t = r * 128.0;
-    const double a = rint(t);
-    r = t - a;
-    dst[p * stride] = __float2bfloat16_rn((float)a);
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// The 7 balanced base-128 digits of x 2^-e (|x| 2^-e < 1), on the integer
+// pipes: S = x 2^(49-e) rounded to the nearest integer (ties to even), then
+// S = sum_p a_p 2^(49-7p) with each digit rounded from the top (a_1 in
+// [-128, 128], the others in [-64, 64]). The remainder dropped below the last
+// digit is at most 2^-50 of the scale.
+__device__ __forceinline__ void digits7(double x, int e, int *a) {
+  const long long b = __double_as_longlong(x);
+  const int be = (int)((b >> 52) & 0x7FF);
+  const unsigned long long frac = (unsigned long long)b & ((1ull << 52) - 1);
+  const unsigned long long m = be ? (frac | (1ull << 52)) : frac;
+  const int sh = (be ? be : 1) - 1075 + 49 - e;  // x 2^(49-e) = m 2^sh
+  unsigned long long q;
+  if (sh >= 0) {
+    q = m << sh;
+  } else if (sh <= -64) {
+    q = 0;
+  } else {
+    const int s = -sh;
+    q = m >> s;
+    const unsigned long long rem = m & ((1ull << s) - 1), half = 1ull << (s - 1);
+    if (rem > half || (rem == half && (q & 1))) ++q;
   }
+  long long S = b < 0 ? -(long long)q : (long long)q;
+#pragma unroll
+  for (int p = 0; p < FB_S - 1; ++p) {
+    const int t = FB_B * (FB_S - 1 - p);  // 42, 35, ..., 7
+    const long long d = (S + (1ll << (t - 1))) >> t;
+    a[p] = (int)d;
+    S -= d << t;
+  }
+  a[FB_S - 1] = (int)S;
 }
 
-// A_op row i (i < rows): slices of the interleaved real row of A[i, :].
-// Row pitch ld; slice p at columns [p*k2p, p*k2p + 2k), zeros elsewhere.
+// A_op row i (i < rows): slices of the interleaved real row of A[i, :]. One
+// warp per row, lanes over the 2k values. Row pitch ld; slice p at columns
+// [p*k2p, p*k2p + 2k), zeros elsewhere.
 __global__ void k_slice_A(const double2 *__restrict__ A, long lda, long rows, int k, int k2p, int ld,
                           __nv_bfloat16 *__restrict__ Aop, int *__restrict__ eA) {
-  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long i = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (i >= rows) return;
-  double m = 0.0;
-  for (int r = 0; r < k; ++r) {
+  unsigned long long mb = 0;
+  for (int r = lane; r < k; r += 32) {
     const double2 a = A[(size_t)r * lda + i];
-    m = fmax(m, fmax(fabs(a.x), fabs(a.y)));
+    mb = max(mb, max(abs_bits(a.x), abs_bits(a.y)));
   }
-  const int e = scale_exp(m);
-  eA[i] = e;
+  for (int o = 16; o; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+  const int e = scale_exp_bits(mb);
+  if (lane == 0) eA[i] = e;
   __nv_bfloat16 *row = Aop + (size_t)i * ld;
-  for (int c = 0; c < ld; ++c) row[c] = __float2bfloat16_rn(0.f);
-  for (int r = 0; r < k; ++r) {
-    const double2 a = A[(size_t)r * lda + i];
-    write_slices(a.x, e, row + 2 * r, k2p);
-    write_slices(a.y, e, row + 2 * r + 1, k2p);
+  for (int v = lane; v < 2 * k; v += 32) {
+    const double2 a = A[(size_t)(v >> 1) * lda + i];
+    int d[FB_S];
+    digits7((v & 1) ? a.y : a.x, e, d);
+#pragma unroll
+    for (int p = 0; p < FB_S; ++p) row[p * k2p + v] = __int2bfloat16_rn(d[p]);
+  }
+  for (int c = lane; c < ld; c += 32) {  // padding of each slice and past the last one
+    const int p = c / k2p, w = c - p * k2p;
+    if (p >= FB_S || w >= 2 * k) row[c] = __float2bfloat16_rn(0.f);
   }
 }
 
@@ -122,29 +159,34 @@ __global__ void k_slice_A(const double2 *__restrict__ A, long lda, long rows, in
 // c * 224 + (q - 1) * 32 + j' % 32, its 2k K entries (then zeros) in a row
 // of 64. A tile's MMA with A-slice p then takes rows of slices 1 .. 8 - p in one
 // instruction (N = (8 - p) * 32) and lands slice q in TMEM columns of level
-// p + q.
+// p + q. One warp per output column, lanes over the 2k values.
 __global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, int k,
                           __nv_bfloat16 *__restrict__ Bop, int *__restrict__ fB) {
-  const long jp = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long jp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (jp >= ncols2) return;
   const long j = jp >> 1;
   const bool im = jp & 1;
-  double m = 0.0;
-  for (int r = 0; r < k; ++r) {
+  unsigned long long mb = 0;
+  for (int r = lane; r < k; r += 32) {
     const double2 w = W[(size_t)r * ldw + j];
-    m = fmax(m, fmax(fabs(w.x), fabs(w.y)));
+    mb = max(mb, max(abs_bits(w.x), abs_bits(w.y)));
   }
-  const int f = scale_exp(m);
-  fB[jp] = f;
+  for (int o = 16; o; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+  const int f = scale_exp_bits(mb);
+  if (lane == 0) fB[jp] = f;
   __nv_bfloat16 *row = Bop + ((size_t)(jp / FB_BN) * FB_BROWS + (jp % FB_BN)) * 64;  // slice 1; slice q at +(q-1)*32 rows
-  for (int q = 0; q < FB_S; ++q)
-    for (int c = 2 * k; c < 64; ++c) row[(size_t)q * FB_BN * 64 + c] = __float2bfloat16_rn(0.f);
-  for (int r = 0; r < k; ++r) {
-    const double2 w = W[(size_t)r * ldw + j];
+  for (int v = lane; v < 2 * k; v += 32) {
+    const double2 w = W[(size_t)(v >> 1) * ldw + j];
     // Re out: Re A Re W - Im A Im W; Im out: Re A Im W + Im A Re W
-    write_slices(im ? w.y : w.x, f, row + 2 * r, FB_BN * 64);
-    write_slices(im ? w.x : -w.y, f, row + 2 * r + 1, FB_BN * 64);
+    const double x = (v & 1) ? (im ? w.x : -w.y) : (im ? w.y : w.x);
+    int d[FB_S];
+    digits7(x, f, d);
+#pragma unroll
+    for (int q = 0; q < FB_S; ++q) row[(size_t)q * FB_BN * 64 + v] = __int2bfloat16_rn(d[q]);
   }
+  for (int c = 2 * k + lane; c < 64; c += 32)
+    for (int q = 0; q < FB_S; ++q) row[(size_t)q * FB_BN * 64 + c] = __float2bfloat16_rn(0.f);
 }
 
 // Exact bit pattern offset of a float holding an integer of magnitude below
@@ -449,10 +491,10 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
   // operand rows have pitch ldk; each update fills its rows up to the pitch
-  k_slice_A<<<(unsigned)((rows + 127) / 128), 128, 0, st>>>(A, rows, rows, k, k2p, (int)ldk,
-                                                            static_cast<__nv_bfloat16 *>(L.A16), L.eA);
-  k_slice_B<<<(unsigned)((cols + 127) / 128), 128, 0, st>>>(W, h->ldm, cols, k,
-                                                            static_cast<__nv_bfloat16 *>(L.B16), L.fB);
+  k_slice_A<<<(unsigned)((rows + 3) / 4), 128, 0, st>>>(A, rows, rows, k, k2p, (int)ldk,
+                                                        static_cast<__nv_bfloat16 *>(L.A16), L.eA);
+  k_slice_B<<<(unsigned)((cols + 3) / 4), 128, 0, st>>>(W, h->ldm, cols, k, static_cast<__nv_bfloat16 *>(L.B16),
+                                                        L.fB);
   CUtensorMap ma, mb, md;
   cudaError_t e;
   if ((e = make_map_bf16(&ma, L.A16, h->a16_rows, kop, ldk, FB_BM)) != cudaSuccess) return e;

@@ -17,15 +17,13 @@
 //   k_score         F = sum over frequencies, first candidate with F < F_best
 //                   (main.cpp:418-429).
 //   k_acc_factor    accept step: K, its LU and z = D (Einc_s + K^-1 w).
-//   k_acc_W         W = [D K^-1 M[s, 0:N], z] (k x (N+1)); k_acc_W32: the
-//                   same solves in FP32 for the complex64 form.
+//   k_acc_W         W = [D K^-1 M[s, 0:N], z] (k x (N+1)).
 //   k_acc_gather    A = M[:, s] ((N+E) x k, column-major).
 //   k_rank_update   M -= A W (replaces update_C_inv's zgemm, pngfopt.hpp:350-358,
 //                   and compute_R_matrix(0)).
 #include <cuda_runtime.h>
 
 #include <cmath>
-#include <type_traits>
 #include <vector>
 
 #include "pngf_internal.h"
@@ -764,84 +762,6 @@ __global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int 
   }
 }
 
-// The complex64 form's W: the same solves as k_acc_W in FP32 with the FP64
-// LU rounded to complex64 (T itself is complex64 there, and the rank-k
-// update that consumes W runs in complex FP32 on the tensor cores). GB300's
-// FP64 pipe is narrow: in FP64 these k^2 (N+1) complex operations dominate the
-// complex64 accept; in FP32 they cost a few microseconds.
-__device__ __forceinline__ float2 fcfnma(float2 a, float2 b, float2 c) {  // a - b*c
-  return make_float2(fmaf(b.y, c.y, fmaf(-b.x, c.x, a.x)), fmaf(-b.y, c.x, fmaf(-b.x, c.y, a.y)));
-}
-
-template <typename TM>
-__global__ void __launch_bounds__(64) k_acc_W32(const SV<TM> M, long n, const int *__restrict__ gs,
-                                                const signed char *__restrict__ gd, int k,
-                                                const double2 *__restrict__ LU, const int *__restrict__ gpiv,
-                                                const double2 *__restrict__ z, double2 *__restrict__ W, long ldw) {
-  extern __shared__ float2 fsm[];
-  float2 *K = fsm;                          // k x k
-  float2 *X = K + (size_t)k * k;            // k x bw, column j at X[j*k ..]
-  const int bw = blockDim.x;
-  __shared__ int s[kMaxK];
-  __shared__ int piv[kMaxK];
-  __shared__ signed char d[kMaxK];
-  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) K[idx] = make_float2((float)LU[idx].x, (float)LU[idx].y);
-  for (int q = threadIdx.x; q < k; q += blockDim.x) {
-    s[q] = gs[q];
-    piv[q] = gpiv[q];
-    d[q] = gd[q];
-  }
-  __syncthreads();
-  const long j0 = (long)blockIdx.x * bw;
-  for (int idx = threadIdx.x; idx < k * bw; idx += blockDim.x) {
-    const int r = idx / bw, jj = idx % bw;
-    const long j = j0 + jj;
-    const double2 v = j < n ? M.t(s[r], j) : make_double2(0.0, 0.0);
-    X[(size_t)jj * k + r] = make_float2((float)v.x, (float)v.y);
-  }
-  __syncthreads();
-  const long j = j0 + threadIdx.x;
-  float2 *x = X + (size_t)threadIdx.x * k;
-  if (j < n) {
-    for (int q = 0; q < k; ++q) {
-      const int p = piv[q];
-      if (p != q) {
-        const float2 t = x[q];
-        x[q] = x[p];
-        x[p] = t;
-      }
-    }
-    for (int q = 0; q < k; ++q) {
-      const float2 xq = x[q];
-      for (int i = q + 1; i < k; ++i) x[i] = fcfnma(x[i], K[i + q * k], xq);
-    }
-    for (int q = k - 1; q >= 0; --q) {
-      const float2 u = K[q + q * k];
-      const float den = fmaf(u.x, u.x, u.y * u.y);
-      const float2 xq = make_float2(fmaf(x[q].x, u.x, x[q].y * u.y) / den, fmaf(x[q].y, u.x, -x[q].x * u.y) / den);
-      x[q] = xq;
-      for (int i = 0; i < q; ++i) x[i] = fcfnma(x[i], K[i + q * k], xq);
-    }
-  }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < k * bw; idx += blockDim.x) {
-    const int r = idx / bw, jj = idx % bw;
-    const long jw = j0 + jj;
-    if (jw < ldw) {
-      double2 v;
-      if (jw < n) {
-        const float2 xf = X[(size_t)jj * k + r];
-        v = d[r] < 0 ? make_double2(-xf.x, -xf.y) : make_double2(xf.x, xf.y);
-      } else if (jw == n) {
-        v = z[r];
-      } else {
-        v = make_double2(0.0, 0.0);
-      }
-      W[(size_t)r * ldw + jw] = v;
-    }
-  }
-}
-
 // A[i + r*lda] = M[i][s_r], i < N+E.
 template <typename TM>
 __global__ void k_acc_gather(const SV<TM> M, long n, long rows, const int *__restrict__ gs, int k,
@@ -1082,17 +1002,10 @@ static cudaError_t accept_prologue(const SV<TM> &v, long n, int E, long ldm, con
   if (e != cudaSuccess) return e;
   k_acc_factor<TM><<<1, 256, smf, stream>>>(v, n, Einc, d_s, d_d, k, LU, piv, z, status);
   const int wc = k <= 64 ? 64 : 32;  // columns per CTA, so that K and the block fit in shared memory
-  if (std::is_same<TM, float2>::value) {  // complex64 form: W in FP32 (see k_acc_W32)
-    const size_t smw = sizeof(float2) * ((size_t)k * k + (size_t)k * wc);
-    e = cudaFuncSetAttribute(k_acc_W32<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
-    if (e != cudaSuccess) return e;
-    k_acc_W32<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, LU, piv, z, W, ldm);
-  } else {
-    const size_t smw = sizeof(double2) * ((size_t)k * k + (size_t)k * wc);
-    e = cudaFuncSetAttribute(k_acc_W<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
-    if (e != cudaSuccess) return e;
-    k_acc_W<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, LU, piv, z, W, ldm);
-  }
+  const size_t smw = sizeof(double2) * ((size_t)k * k + (size_t)k * wc);
+  e = cudaFuncSetAttribute(k_acc_W<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
+  if (e != cudaSuccess) return e;
+  k_acc_W<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, LU, piv, z, W, ldm);
   k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(v, n, rows, d_s, k, A, rows);
   return cudaGetLastError();
 }
