@@ -417,6 +417,7 @@ int pngf_destroy(pngf_handle *ph) {
     dfree(L.piv);
     dfree(L.Aop);
     dfree(L.Bop);
+    dfree(L.V);
     dfree(L.A16);
     dfree(L.B16);
     dfree(L.eA);
@@ -549,7 +550,8 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
                                 cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming) != cudaSuccess))
       return fail(PNGF_ERR_CUDA);
     if ((rc = dalloc(h, &L.A, (size_t)rows * h->acc_cap)) || (rc = dalloc(h, &L.W, (size_t)h->acc_cap * h->ldm)) ||
-        (rc = dalloc(h, &L.LU, (size_t)h->acc_cap * h->acc_cap)) || (rc = dalloc(h, &L.piv, (size_t)h->acc_cap)) ||
+        (rc = dalloc(h, &L.LU, (size_t)h->acc_cap * h->acc_cap)) || (rc = dalloc(h, &L.V, (size_t)h->acc_cap * h->acc_cap)) ||
+        (rc = dalloc(h, &L.piv, (size_t)h->acc_cap)) ||
         (rc = dalloc(h, &L.z, (size_t)h->acc_cap)))
       return fail(rc);
     if (c64) {

@@ -42,6 +42,7 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 
@@ -182,16 +183,24 @@ __global__ void k_slice_A(const double2 *__restrict__ A, long lda, long rows, lo
     for (int p = 0; p < FB_S; ++p) tile[core_off(r, p * k2p + v, FB_BM)] = __float2bfloat16_rn(0.f);
 }
 
-// B_op for output column j' (j' = 2j: real part, 2j+1: imaginary, of M[:, j];
-// W is k x ldw, row-major complex). Column tile c = j' / 32 is a 224 x k2p
+__device__ __forceinline__ double2 ld_c(const double2 *p) { return *p; }
+__device__ __forceinline__ double2 ld_c(const float2 *p) {
+  const float2 v = *p;
+  return make_double2(v.x, v.y);
+}
+
+// B_op for output column j' (j' = 2j: real part, 2j+1: imaginary, of column
+// j of the product; W is k x ldw, row-major complex, row c taken from row
+// rowidx[c] of W when rowidx is given). Column tile c = j' / 32 is a 224 x k2p
 // tile (same layout as A's) in which the 7 slices of its 32 output columns
 // are stacked along N: slice q of column j' is row (q - 1) * 32 + j' % 32,
 // its 2k K entries then zeros. A tile's MMA with A-slice p then takes the rows
 // of slices 1 .. 8 - p in one instruction (N = (8 - p) * 32) and lands slice q
 // in TMEM columns of level p + q. Columns from ncols2 up to the end of the
 // last tile are zeros. One warp per output column, lanes over the values.
-__global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, long bcols, int k, int k2p,
-                          __nv_bfloat16 *__restrict__ Bop, int *__restrict__ fB) {
+template <typename TIN>
+__global__ void k_slice_B(const TIN *__restrict__ W, long ldw, const int *__restrict__ rowidx, long ncols2, long bcols,
+                          int k, int k2p, __nv_bfloat16 *__restrict__ Bop, int *__restrict__ fB) {
   const long jp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (jp >= bcols) return;
@@ -206,14 +215,15 @@ __global__ void k_slice_B(const double2 *__restrict__ W, long ldw, long ncols2, 
   const bool im = jp & 1;
   unsigned long long mb = 0;
   for (int c = lane; c < k; c += 32) {
-    const double2 w = W[(size_t)c * ldw + j];
+    const double2 w = ld_c(W + (size_t)(rowidx ? rowidx[c] : c) * ldw + j);
     mb = max(mb, max(abs_bits(w.x), abs_bits(w.y)));
   }
   for (int o = 16; o; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
   const int f = scale_exp_bits(mb);
   if (lane == 0) fB[jp] = f;
   for (int v = lane; v < 2 * k; v += 32) {
-    const double2 w = W[(size_t)(v >> 1) * ldw + j];
+    const int c = v >> 1;
+    const double2 w = ld_c(W + (size_t)(rowidx ? rowidx[c] : c) * ldw + j);
     // Re out: Re A Re W - Im A Im W; Im out: Re A Im W + Im A Re W
     const double x = (v & 1) ? (im ? w.x : -w.y) : (im ? w.y : w.x);
     int d[FB_S];
@@ -533,24 +543,34 @@ size_t f64tc_b_cols() { return FB_MAX_K2P; }
 
 long f64tc_b_rows(long n) { return (2 * (n + 1) + FB_BN - 1) / FB_BN * FB_BROWS; }
 
-cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W) {
-  const long n = h->n, rows = n + h->E;
-  const long cols = 2 * (n + 1);
+namespace {
+
+// D[i, j] -= sum_c A[i, c] B[c, j] (complex, FP64-accurate) for i < drows
+// and complex columns j < dcols2 / 2, with k <= f64tc_max_k(): D row-major
+// doubles with pitch ldd, A column-major (lda), B row-major complex (ldb;
+// complex64 when b32), its row c taken from row browidx[c] when given. On
+// the lane's operand scratch and stream.
+cudaError_t f64tc_gemm(Handle *h, int f, int k, double *D, long drows, long dcols2, long ldd, const double2 *A,
+                       long lda, const void *B, bool b32, long ldb, const int *browidx, bool timed) {
   if (k < 1 || k > f64tc_max_k()) return cudaErrorInvalidValue;
   const int k2p = (2 * k + 15) / 16 * 16;
-  const int nrb = (int)((rows + FB_BM - 1) / FB_BM), ncb = (int)((cols + FB_BN - 1) / FB_BN);
+  const int nrb = (int)((drows + FB_BM - 1) / FB_BM), ncb = (int)((dcols2 + FB_BN - 1) / FB_BN);
   const long arows = (long)nrb * FB_BM, bcols = (long)ncb * FB_BN;
   // the operand buffers hold a16_rows x f64tc_op_cols() and b16_rows x f64tc_b_cols() elements
   if (arows > h->a16_rows || (long)ncb * FB_BROWS > h->b16_rows) return cudaErrorInvalidValue;
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
-  k_slice_A<<<(unsigned)((arows + 3) / 4), 128, 0, st>>>(A, rows, rows, arows, k, k2p,
-                                                         static_cast<__nv_bfloat16 *>(L.A16), L.eA);
-  k_slice_B<<<(unsigned)((bcols + 3) / 4), 128, 0, st>>>(W, h->ldm, cols, bcols, k, k2p,
-                                                         static_cast<__nv_bfloat16 *>(L.B16), L.fB);
+  __nv_bfloat16 *A16 = static_cast<__nv_bfloat16 *>(L.A16), *B16 = static_cast<__nv_bfloat16 *>(L.B16);
+  k_slice_A<<<(unsigned)((arows + 3) / 4), 128, 0, st>>>(A, lda, drows, arows, k, k2p, A16, L.eA);
+  if (b32)
+    k_slice_B<float2><<<(unsigned)((bcols + 3) / 4), 128, 0, st>>>(static_cast<const float2 *>(B), ldb, browidx,
+                                                                    dcols2, bcols, k, k2p, B16, L.fB);
+  else
+    k_slice_B<double2><<<(unsigned)((bcols + 3) / 4), 128, 0, st>>>(static_cast<const double2 *>(B), ldb, browidx,
+                                                                     dcols2, bcols, k, k2p, B16, L.fB);
   CUtensorMap md;
   cudaError_t e;
-  if ((e = make_map_f64(&md, reinterpret_cast<const double *>(M), rows, cols, 2 * h->ldm)) != cudaSuccess) return e;
+  if ((e = make_map_f64(&md, D, drows, dcols2, ldd)) != cudaSuccess) return e;
   if (g_num_sms == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
@@ -575,16 +595,37 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
       cudaSuccess)
     return e;
   const int ntiles = nrb * ncb;
-  const int grid = ntiles < g_num_sms ? ntiles : g_num_sms;
-  cudaEvent_t t0 = timing_mark(h, st);
-  k_tc_update_f64<<<grid, FB_THREADS, smem, st>>>(static_cast<const __nv_bfloat16 *>(L.A16),
-                                                  static_cast<const __nv_bfloat16 *>(L.B16), md, (int)rows, (int)cols,
-                                                  ncb, ntiles, k2p, nb, nd, L.eA, L.fB, h->d_tc_err);
-  const double cells = (double)rows * (double)(n + 1);
-  timing_close(h, t0, T_UPDATE, 8.0 * k * cells,
-               2.0 * 16.0 * cells + 2.0 * FB_S * k2p * ((double)rows + (double)cols), 0.0, st);
+  const int grid = persistent_grid(h, ntiles, g_num_sms);
+  cudaEvent_t t0 = timed ? timing_mark(h, st) : nullptr;
+  k_tc_update_f64<<<grid, FB_THREADS, smem, st>>>(A16, B16, md, (int)drows, (int)dcols2, ncb, ntiles, k2p, nb, nd,
+                                                  L.eA, L.fB, h->d_tc_err);
+  if (timed) {
+    const double cells = (double)drows * (double)(dcols2 / 2);
+    timing_close(h, t0, T_UPDATE, 8.0 * k * cells,
+                 2.0 * 16.0 * cells + 2.0 * FB_S * k2p * ((double)drows + (double)dcols2), 0.0, st);
+  }
   h->nlaunch += 3;
   return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W) {
+  const long n = h->n, rows = n + h->E;
+  return f64tc_gemm(h, f, k, reinterpret_cast<double *>(M), rows, 2 * (n + 1), 2 * h->ldm, A, rows, W, false, h->ldm,
+                    nullptr, true);
+}
+
+cudaError_t launch_f64tc_wgemm(Handle *h, int f, int k, const double2 *Vneg, const void *X, bool x32, long ldx,
+                               const int *d_s, double2 *W) {
+  // W[:, 0:N] -= Vneg X[s, 0:N], the inner dimension in pieces of at most f64tc_max_k()
+  for (int c0 = 0; c0 < k; c0 += f64tc_max_k()) {
+    const int kc = std::min(k - c0, f64tc_max_k());
+    const cudaError_t e = f64tc_gemm(h, f, kc, reinterpret_cast<double *>(W), k, 2 * h->n, 2 * h->ldm,
+                                     Vneg + (size_t)c0 * k, k, X, x32, ldx, d_s + c0, false);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 }  // namespace pngf

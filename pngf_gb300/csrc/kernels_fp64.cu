@@ -762,6 +762,69 @@ __global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int 
   }
 }
 
+// Vneg = -D K^-1 (k x k, column-major: Vneg[r + c*k]) from K's LU (LU[i +
+// q*k]: unit L below the diagonal, U on and above) and its row interchanges:
+// one warp per column c solves K x = e_c (the substitutions of k_acc_W, with
+// U's diagonal inverted once). INV_COLS columns per CTA share the LU, staged in
+// shared memory so that the sequential steps never wait on global memory.
+constexpr int INV_COLS = 4;
+constexpr int kMaxTcW = 96;  // edges per accept on the tensor-core W path (the LU fits shared memory)
+__global__ void __launch_bounds__(32 * INV_COLS) k_acc_inverse(const double2 *__restrict__ LU,
+                                                               const int *__restrict__ gpiv,
+                                                               const signed char *__restrict__ gd, int k,
+                                                               double2 *__restrict__ Vneg) {
+  extern __shared__ double2 ism[];
+  double2 *K = ism;                            // k x k
+  double2 *rdiag = K + (size_t)k * k;          // 1 / U[q][q]
+  double2 *xs = rdiag + k;                     // INV_COLS x k
+  __shared__ int piv[kMaxK];
+  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) K[idx] = LU[idx];
+  for (int q = threadIdx.x; q < k; q += blockDim.x) {
+    piv[q] = gpiv[q];
+    rdiag[q] = crecip(LU[q + (size_t)q * k]);
+  }
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int c = blockIdx.x * INV_COLS + w;
+  if (c >= k) return;
+  double2 *x = xs + (size_t)w * k;
+  for (int i = lane; i < k; i += 32) x[i] = make_double2(i == c ? 1.0 : 0.0, 0.0);
+  __syncwarp();
+  if (lane == 0)
+    for (int q = 0; q < k; ++q) {
+      const int p = piv[q];
+      if (p != q) {
+        const double2 t = x[q];
+        x[q] = x[p];
+        x[p] = t;
+      }
+    }
+  __syncwarp();
+  for (int q = 0; q < k; ++q) {
+    const double2 xq = x[q];
+    for (int i = q + 1 + lane; i < k; i += 32) x[i] = cfnma(x[i], K[i + (size_t)q * k], xq);
+    __syncwarp();
+  }
+  for (int q = k - 1; q >= 0; --q) {
+    const double2 xq = cmul(x[q], rdiag[q]);
+    __syncwarp();
+    if (lane == 0) x[q] = xq;
+    for (int i = lane; i < q; i += 32) x[i] = cfnma(x[i], K[i + (size_t)q * k], xq);
+    __syncwarp();
+  }
+  for (int r = lane; r < k; r += 32) {
+    const double2 v = x[r];
+    Vneg[r + (size_t)c * k] = gd[r] < 0 ? v : make_double2(-v.x, -v.y);
+  }
+}
+
+// W[r][j] = z_r for j = N, 0 elsewhere (j < ldw): the start of the tensor-core W.
+__global__ void k_W_init(double2 *__restrict__ W, long ldw, long n, const double2 *__restrict__ z, int k) {
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int r = blockIdx.y;
+  if (j < ldw && r < k) W[(size_t)r * ldw + j] = j == n ? z[r] : make_double2(0.0, 0.0);
+}
+
 // A[i + r*lda] = M[i][s_r], i < N+E.
 template <typename TM>
 __global__ void k_acc_gather(const SV<TM> M, long n, long rows, const int *__restrict__ gs, int k,
@@ -1010,6 +1073,32 @@ static cudaError_t accept_prologue(const SV<TM> &v, long n, int E, long ldm, con
   return cudaGetLastError();
 }
 
+// Accept prologue with W on the tensor cores: K's LU and z, Vneg = -D K^-1,
+// W = [D K^-1 T[s, 0:N], z] as Vneg times the rows s of the state with the
+// FP64-accurate tensor-core product, A = [T; R][:, s]. For the FP64 layout and
+// the complex64 one without deferred updates (whose rows are read as stored).
+template <typename TM>
+static cudaError_t accept_prologue_tc(Handle *h, int f, const SV<TM> &v, const void *X, bool x32,
+                                      const double2 *Einc, const int *d_s, const signed char *d_d, int k) {
+  const long n = h->n, rows = n + h->E;
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
+  const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
+  cudaError_t e = cudaFuncSetAttribute(k_acc_factor<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+  if (e != cudaSuccess) return e;
+  k_acc_factor<TM><<<1, 256, smf, st>>>(v, n, Einc, d_s, d_d, k, L.LU, L.piv, L.z, h->d_acc_status);
+  const size_t smi = sizeof(double2) * ((size_t)k * k + k + (size_t)INV_COLS * k);
+  if ((e = cudaFuncSetAttribute(k_acc_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smi)) != cudaSuccess)
+    return e;
+  k_acc_inverse<<<(unsigned)((k + INV_COLS - 1) / INV_COLS), 32 * INV_COLS, smi, st>>>(L.LU, L.piv, d_d, k, L.V);
+  k_W_init<<<dim3((unsigned)((h->ldm + 255) / 256), (unsigned)k), 256, 0, st>>>(L.W, h->ldm, n, L.z, k);
+  h->nlaunch += 3;
+  if ((e = launch_f64tc_wgemm(h, f, k, L.V, X, x32, h->ldm, d_s, L.W)) != cudaSuccess) return e;
+  k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, st>>>(v, n, rows, d_s, k, L.A, rows);
+  h->nlaunch += 1;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k, int layout) {
   Freq &q = h->f[f];
   const long n = h->n, rows = n + h->E;
@@ -1017,6 +1106,16 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
   cudaError_t e;
+  if (h->f64tc && layout == PNGF_PREC_C64 && h->defer_cap == 0 && k <= kMaxTcW) {
+    if ((e = accept_prologue_tc<float2>(h, f, view32(h, f), q.T32, true, q.Einc, d_s, d_d, k)) != cudaSuccess)
+      return e;
+    return launch_c64_update(h, f, k);
+  }
+  if (h->f64tc && layout != PNGF_PREC_C64 && k <= f64tc_max_k()) {
+    if ((e = accept_prologue_tc<double2>(h, f, view64(h, f), q.M64, false, q.Einc, d_s, d_d, k)) != cudaSuccess)
+      return e;
+    return launch_f64tc_update(h, f, k, q.M64, L.A, L.W);
+  }
   if (layout == PNGF_PREC_C64) {
     e = accept_prologue<float2>(view32(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, L.LU, L.piv, L.z, L.A, L.W,
                                 h->d_acc_status, st);

@@ -63,6 +63,7 @@ struct Lane {
   double2 *A = nullptr;           // (N+E) x acc_cap, column-major (ld = N+E)
   double2 *W = nullptr;           // acc_cap x ldm row-major
   double2 *LU = nullptr;          // acc_cap^2
+  double2 *V = nullptr;           // acc_cap^2: -D K^-1 (column-major), the tensor-core W
   double2 *z = nullptr;           // acc_cap
   int *piv = nullptr;             // acc_cap
   float *Aop = nullptr;           // complex64 update operands: aop_rows x kt_cap fp32, K-major
@@ -263,7 +264,20 @@ size_t f64tc_b_cols();   // row pitch of the B slices (elements)
 long f64tc_b_rows(long n);  // rows of the B slices: 7 per output column, 32-column tiles stacked
 // M -= A W for M ((N+E) x ldm complex128), A ((N+E) x k column-major), W (k x ldm),
 // with frequency f's lane scratch and stream.
+// Grid of a persistent update kernel (one CTA per SM) over ntiles tiles: with
+// several frequency lanes it leaves kReservedSMs SMs free, so that the other
+// lanes' single-CTA kernels (capacitance LU, explicit inverse) run beside it
+// instead of waiting for it to end.
+constexpr int kReservedSMs = 8;
+inline int persistent_grid(const Handle *h, int ntiles, int nsm) {
+  const int g = h->lanes.size() > 1 && nsm > 2 * kReservedSMs ? nsm - kReservedSMs : nsm;
+  return ntiles < g ? ntiles : g;
+}
 cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W);
+// W[:, 0:N] -= Vneg X[s, 0:N] on the tensor cores (FP64-accurate): Vneg k x k
+// column-major, X rows s of the state (complex64 when x32, pitch ldx).
+cudaError_t launch_f64tc_wgemm(Handle *h, int f, int k, const double2 *Vneg, const void *X, bool x32, long ldx,
+                               const int *d_s, double2 *W);
 // Commits P and the tile map on the device for candidate c of the batch.
 cudaError_t launch_commit(Handle *h, int c);
 // The accept kernels on caller-supplied buffers (no handle): scratch LU (k^2),

@@ -43,18 +43,20 @@ def torch_net(params, C, x, target, mask):
     return out.detach().numpy(), float(loss), np.concatenate(grads)
 
 
-def test_network_matches_torch_cpu(cases, built_lib):
+# (tiles_x, tiles_y, channels, batch): square maps in one band of the tiled
+# kernels, a wide map cut into several bands (25 wide: 5-row bands), and a
+# channel count the tiled kernels do not take (the general kernels).
+@pytest.mark.parametrize("tx,ty,C,B", [(7, 7, 32, 3), (25, 13, 16, 5), (9, 7, 12, 2)])
+def test_network_matches_torch_cpu(tx, ty, C, B, cases, built_lib):
     from pngf_gb300 import lib
-    h = lib.Handle(7, 7, [30e9], max_flips=1)
-    C = 32
+    h = lib.Handle(tx, ty, [30e9], max_flips=1)
     p = lib.Proposal(h, channels=C, seed=3)
     rng = np.random.default_rng(0)
     params = (rng.standard_normal(p.num_params()) * 0.2).astype(np.float32)
     p.set_params(params)
-    B = 3
-    x = rng.standard_normal((B, 3, 7, 7)).astype(np.float32)
-    target = rng.standard_normal((B, 7, 7)).astype(np.float32)
-    mask = (rng.random((B, 7, 7)) < 0.6).astype(np.float32)
+    x = rng.standard_normal((B, 3, ty, tx)).astype(np.float32)
+    target = rng.standard_normal((B, ty, tx)).astype(np.float32)
+    mask = (rng.random((B, ty, tx)) < 0.6).astype(np.float32)
     out, grad, loss = p.forward_backward(x, target, mask)
     out_t, loss_t, grad_t = torch_net(params, C, x, target, mask)
     np.testing.assert_allclose(out, out_t, rtol=1e-4, atol=1e-4 * np.abs(out_t).max())
