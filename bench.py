@@ -265,6 +265,31 @@ def run_form(a, precision, Gs, rank, local, dist, defer_rank=0):
     return out
 
 
+def isolated_update(a, precision, G0, local, decisions=6):
+    """The accept update alone: a one-frequency handle (one stream, nothing
+    sharing the GPU with its launches), a few DBS decisions from the same
+    design; returns the update kernel's mean launch time and bytes."""
+    import torch
+    from pngf_gb300 import lib
+    h = lib.Handle(a.tiles, a.tiles, FREQS[:1], precision=precision, max_flips=1, device=local)
+    h.load_G(0, G0, None)
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0)
+    h.autotune()
+    d.step()
+    torch.cuda.synchronize()
+    h.timing_enable(True)
+    for _ in range(decisions):
+        d.step()
+    torch.cuda.synchronize()
+    tm = h.timing()
+    d.close()
+    h.close()
+    torch.cuda.empty_cache()
+    nl = max(1, tm["update_launches"])
+    return {"launch_ms": tm["update_ms"] / nl, "bytes_per_launch": tm["update_bytes"] / nl,
+            "flop_per_launch": tm["update_flop"] / nl, "launches": tm["update_launches"]}
+
+
 def autotune_on(h, mode_single=True):
     """Autotunes a handle's kernel forms on a throwaway random design (seed
     99), outside any timed region; the forms stay with the handle."""
@@ -514,6 +539,8 @@ def gpu_arm(a, world, rank, local):
     if "c64d" in forms:  # complex64 with the rank-k updates deferred to rank 192
         r32d = run_form(a, lib.PREC_C64, Gs, rank, local, dist, defer_rank=192)
         c64d_red = reduce_form(r32d, dist)
+    iso64 = isolated_update(a, lib.PREC_FP64, Gs[0], local) if r64 is not None and rank == 0 else None
+    iso32 = isolated_update(a, lib.PREC_C64, Gs[0], local) if r32 is not None and rank == 0 else None
     conv = None
     if not a.no_converge and rank == 0:
         conv = converge_compare(a.tiles, FREQS, lambda h: [h.load_G(f, G, None) for f, G in enumerate(Gs)], a.seed,
@@ -565,6 +592,11 @@ def gpu_arm(a, world, rank, local):
         "aggregate_gbs_over_accept_time": tm["update_bytes"] / (tm["accept_ms"] * 1e-3) / 1e9
         if tm["accept_ms"] > 0 else None,
     }
+    if iso64:  # the same kernel with the GPU to itself
+        g = iso64["bytes_per_launch"] / (iso64["launch_ms"] * 1e-3) / 1e9
+        roofline["isolated"] = {"what": "one-frequency handle, %d DBS decisions, one stream" % 6,
+                                "launch_ms": iso64["launch_ms"], "achieved": g, "frac": g / peaks["hbm_gbs"],
+                                "launches": iso64["launches"]}
     eval_s = tm["eval_ms"] * 1e-3
     line = {
         "metric": "DBS flip evals/s, 21x21 tiles x 5 frequencies, plain FP64 form",
@@ -647,6 +679,11 @@ def gpu_arm(a, world, rank, local):
             r32, c64_red, "T in complex64, rank-k update on tcgen05 tensor cores (kind::tf32, 3xTF32 split products, "
                           "FP32 accumulation in TMEM) at every accept; capacitance LU, y, R, Eobj, objective and accept "
                           "test in FP64; same workload and steps")
+        if iso32:
+            g = iso32["bytes_per_launch"] / (iso32["launch_ms"] * 1e-3) / 1e9
+            line["c64_form"]["roofline"]["isolated"] = {
+                "what": "one-frequency handle, 6 DBS decisions, one stream", "launch_ms": iso32["launch_ms"],
+                "achieved": g, "frac": g / peaks["hbm_gbs"], "launches": iso32["launches"]}
     if r32d is not None:
         line["c64_deferred_form"] = c64_block(
             r32d, c64d_red, "the complex64 form with the T part of each accept appended to pending rank-k factors "
