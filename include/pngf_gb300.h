@@ -263,8 +263,10 @@ typedef struct pngf_tune {
   int cands_per_cta[PNGF_TUNE_MAX];
   double eval_us[PNGF_TUNE_MAX];     /* device time of one batch; -1 = form does not apply */
   int batch;                         /* candidates in the timed batch (every tile once) */
-  int update_form;                   /* chosen complex64 update tile form */
-  int update_forms;
+  int update_form;                   /* chosen complex64 update tile form for accepts (entry 0 or 1) */
+  int update_forms;                  /* complex64: 4 entries, the two tile widths timed at the accept rank
+                                        (min(k_max, 24)), then at the build chunk's rank (48); the widths
+                                        chosen for each rank class are kept by the handle */
   int update_cols[PNGF_TUNE_MAX];    /* FP32 output columns per update tile */
   double update_us[PNGF_TUNE_MAX];   /* device time of one rank-update; -1 = not timed */
 } pngf_tune;

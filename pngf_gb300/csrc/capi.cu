@@ -1045,8 +1045,10 @@ int pngf_timing_get(pngf_handle *ph, pngf_timing *out) {
 // (T, y and R are then left unchanged) and keeps the fastest.
 static int tune_update(Handle *h, pngf_tune *out) {
   if (h->cfg.precision != PNGF_PREC_C64) return PNGF_OK;
+  // widths for accepts (rank <= kAccTuneRank) and for build chunks / flushes
   const int widths[2] = {128, 64};
-  const int k = std::min(h->kmax, 24);
+  const int ks[2] = {std::min(h->kmax, kAccTuneRank), kC64BuildChunk};
+  const int k = std::max(ks[0], ks[1]);
   const long rows = h->n + h->E;
   int rc = lanes_fork(h);  // frequency 0's lane runs the timed updates
   if (rc) return rc;
@@ -1063,33 +1065,37 @@ static int tune_update(Handle *h, pngf_tune *out) {
   const bool timing = h->timing;
   h->timing = false;
   const int reps = 3;
-  double best = 1e300;
-  int bi = 0;
+  double best[2] = {1e300, 1e300};
+  int bi[2] = {0, 0};
   cudaError_t e = cudaSuccess;
-  for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
-    h->c64_cols = widths[i];
-    out->update_cols[i] = widths[i];
-    out->update_us[i] = -1.0;
-    if ((e = launch_c64_update(h, 0, k)) != cudaSuccess) break;  // warm-up
-    cudaEventRecord(a, st);
-    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_c64_update(h, 0, k);
-    cudaEventRecord(b, st);
-    if (e == cudaSuccess) e = cudaEventSynchronize(b);
-    float ms = 0.f;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
-    out->update_us[i] = 1e3 * ms / reps;
-    if (out->update_us[i] < best) {
-      best = out->update_us[i];
-      bi = i;
+  // entries 0, 1: the widths at the accept rank; 2, 3: at the build chunk rank
+  for (int kc = 0; kc < 2 && e == cudaSuccess; ++kc)
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+      const int ent = 2 * kc + i;
+      h->c64_cols = h->c64_cols_build = widths[i];
+      out->update_cols[ent] = widths[i];
+      out->update_us[ent] = -1.0;
+      if ((e = launch_c64_update(h, 0, ks[kc])) != cudaSuccess) break;  // warm-up
+      cudaEventRecord(a, st);
+      for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_c64_update(h, 0, ks[kc]);
+      cudaEventRecord(b, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(b);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+      out->update_us[ent] = 1e3 * ms / reps;
+      if (out->update_us[ent] < best[kc]) {
+        best[kc] = out->update_us[ent];
+        bi[kc] = i;
+      }
     }
-  }
   h->timing = timing;
   h->nlaunch = nl0;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  h->c64_cols = widths[bi];
-  out->update_form = bi;
-  out->update_forms = 2;
+  h->c64_cols = widths[bi[0]];
+  h->c64_cols_build = widths[bi[1]];
+  out->update_form = bi[0];
+  out->update_forms = 4;
   if (e != cudaSuccess) return cuda_check(h, e, "autotune (update)");
   if ((rc = lanes_join(h))) return rc;
   int tc = 0;

@@ -49,7 +49,7 @@ using namespace tc;
 template <int BN> struct C64Tile {
   static constexpr uint32_t B_BYTES = BN * TC_BK * 4;  // one K stage of B
   static constexpr uint32_t STAGE = A_BYTES + B_BYTES;
-  static constexpr int ST = BN == 128 ? 2 : 4;         // operand stages
+  static constexpr int ST = BN == 128 ? 3 : 6;         // operand stages (the ring hides L2 latency)
   static constexpr uint32_t DTILE = (BN / 32) * TC_DBOX;  // a 128 x BN tile of T
   static constexpr size_t SMEM = 1024 + ST * STAGE + 2 * DTILE + 256;
   // Instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
@@ -597,7 +597,7 @@ cudaError_t launch_c64_tc(Handle *h, int f, int Kt, int rank) {
   if (e != cudaSuccess) return e;
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
-  const int bn = h->c64_cols == 64 ? 64 : 128;
+  const int bn = (rank > kAccTuneRank ? h->c64_cols_build : h->c64_cols) == 64 ? 64 : 128;
   const int dcols = (int)(2 * n);
   CUtensorMap ma, mb, md;
   if ((e = make_map(&ma, L.Aop, h->aop_rows, Kt, h->kt_cap, TC_BM)) != cudaSuccess) return e;

@@ -307,6 +307,10 @@ __global__ void k_edge_lists(Geo g, int ncand, const int *__restrict__ tiles, co
 // cooperative LU of K (column-major, leading dimension ld) in shared memory
 
 // Returns 0 on success, j+1 if pivot j is exactly zero (LAPACK's info).
+// Per column j, warp 0 finds the pivot, swaps the rows and scales the column
+// (warp shuffles and __syncwarp only), then the whole CTA applies the rank-1
+// update of the trailing block: two CTA barriers per column. Every element
+// sees the same operations in the same order as in k_eval_warp.
 __device__ int cta_lu(double2 *K, int ld, int k, int *piv, double *red_v, int *red_i) {
   const int tid = threadIdx.x, nt = blockDim.x;
   __shared__ int s_info;
@@ -329,19 +333,17 @@ __device__ int cta_lu(double2 *K, int ld, int k, int *piv, double *red_v, int *r
         red_v[0] = bv;
         if (bv == 0.0 && s_info == 0) s_info = j + 1;
       }
-    }
-    __syncthreads();
-    const int p = piv[j];
-    if (p != j)
-      for (int c = tid; c < k; c += nt) {
-        const double2 t = K[j + c * ld];
-        K[j + c * ld] = K[p + c * ld];
-        K[p + c * ld] = t;
+      if (bi != j)
+        for (int c = tid; c < k; c += 32) {
+          const double2 t = K[j + c * ld];
+          K[j + c * ld] = K[bi + c * ld];
+          K[bi + c * ld] = t;
+        }
+      __syncwarp();
+      if (bv != 0.0) {
+        const double2 r = crecip(K[j + j * ld]);
+        for (int i = j + 1 + tid; i < k; i += 32) K[i + j * ld] = cmul(K[i + j * ld], r);
       }
-    __syncthreads();
-    if (red_v[0] != 0.0) {
-      const double2 r = crecip(K[j + j * ld]);
-      for (int i = j + 1 + tid; i < k; i += nt) K[i + j * ld] = cmul(K[i + j * ld], r);
     }
     __syncthreads();
     const int m = k - j - 1;
@@ -355,31 +357,35 @@ __device__ int cta_lu(double2 *K, int ld, int k, int *piv, double *red_v, int *r
   return s_info;
 }
 
-// Solves K x = b in place (b in shared memory) with the LU from cta_lu.
+// Solves K x = b in place (b in shared memory) with the LU from cta_lu: warp
+// 0 alone (the vector is short), then a CTA barrier.
 __device__ void cta_lu_solve(const double2 *K, int ld, int k, const int *piv, double2 *b) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  if (tid == 0)
-    for (int j = 0; j < k; ++j) {
-      const int p = piv[j];
-      if (p != j) {
-        const double2 t = b[j];
-        b[j] = b[p];
-        b[p] = t;
+  const int tid = threadIdx.x;
+  if (tid < 32) {
+    if (tid == 0)
+      for (int j = 0; j < k; ++j) {
+        const int p = piv[j];
+        if (p != j) {
+          const double2 t = b[j];
+          b[j] = b[p];
+          b[p] = t;
+        }
       }
+    __syncwarp();
+    for (int j = 0; j < k; ++j) {  // unit lower
+      const double2 bj = b[j];
+      for (int i = j + 1 + tid; i < k; i += 32) b[i] = cfnma(b[i], K[i + j * ld], bj);
+      __syncwarp();
     }
+    for (int j = k - 1; j >= 0; --j) {  // upper
+      if (tid == 0) b[j] = cdiv(b[j], K[j + j * ld]);
+      __syncwarp();
+      const double2 bj = b[j];
+      for (int i = tid; i < j; i += 32) b[i] = cfnma(b[i], K[i + j * ld], bj);
+      __syncwarp();
+    }
+  }
   __syncthreads();
-  for (int j = 0; j < k; ++j) {  // unit lower
-    const double2 bj = b[j];
-    for (int i = j + 1 + tid; i < k; i += nt) b[i] = cfnma(b[i], K[i + j * ld], bj);
-    __syncthreads();
-  }
-  for (int j = k - 1; j >= 0; --j) {  // upper
-    if (tid == 0) b[j] = cdiv(b[j], K[j + j * ld]);
-    __syncthreads();
-    const double2 bj = b[j];
-    for (int i = tid; i < j; i += nt) b[i] = cfnma(b[i], K[i + j * ld], bj);
-    __syncthreads();
-  }
 }
 
 // Shared prologue of evaluation and accept: gathers K = I + T[s,s] D and

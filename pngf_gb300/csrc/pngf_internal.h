@@ -22,6 +22,7 @@ constexpr int kInitChunk = 96;
 constexpr int kC64BuildChunk = 48;
 // Largest pending rank of deferred complex64 updates.
 constexpr int kMaxDeferRank = 256;
+constexpr int kAccTuneRank = 24;  // updates of rank <= this use c64_cols, larger ones c64_cols_build
 
 // Forms of the candidate kernel the autotuner chooses from: warps working on
 // one (candidate, frequency) and candidates per CTA. Index 0 is the default.
@@ -100,6 +101,7 @@ struct Handle {
   int init_chunk = kInitChunk;
   int eval_variant = 0;                     // index into kEvalForms (set by the autotuner)
   int c64_cols = 128;                       // output tile width of the complex64 update (64 or 128)
+  int c64_cols_build = 128;                 // the same for ranks above kAccTuneRank (build chunks, flushes)
   int defer_cap = 0;                        // C64: pending rank at which deferred updates are flushed (0 = off)
   int defer_rp = 0;                         //   rank pending now (same at every frequency)
   bool defer_now = false;                   //   accepts being launched are deferred (DBS accepts, not builds)

@@ -81,7 +81,9 @@ def test_autotune_keeps_state(prec, cases, built_lib):
     assert t["eval"][t["eval_form"]]["us"] > 0
     assert all(e["us"] > 0 for e in t["eval"])  # kmax = 24: every form applies
     if prec == 1:
-        assert len(t["update"]) == 2 and all(u["us"] > 0 for u in t["update"])
+        # two widths at the accept rank, then the same two at the build chunk's rank
+        assert len(t["update"]) == 4 and all(u["us"] > 0 for u in t["update"])
+        assert [u["cols"] for u in t["update"]] == [128, 64, 128, 64] and t["update_form"] in (0, 1)
     for f in range(len(Gs)):
         assert np.array_equal(bits(h.get_M(f)[0]), bits(before[f]))
     cands = [[t_] for t_ in range(a * a) if t_ != ((a - 1) // 2) * (a + 1)]
