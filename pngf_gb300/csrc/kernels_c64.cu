@@ -403,29 +403,31 @@ __global__ void k_merge_M(const float2 *__restrict__ T32, const double2 *__restr
 constexpr int DR_MAX_ROWS = 8;
 
 // out[r][j] = sum_{l in P} X[r][P_l] H[P_l][j], one warp per column j (lanes
-// walk P, so the reads of column j of G are contiguous).
-__global__ void k_rows_PH(const double2 *__restrict__ X, int nr, long n, const int *__restrict__ Pidx, int np,
+// walk P, so the reads of column j of G are contiguous). NR rows exactly, so
+// that no FP64 instruction is issued for absent rows.
+template <int NR>
+__global__ void k_rows_PH(const double2 *__restrict__ X, long n, const int *__restrict__ Pidx, int np,
                           const double2 *__restrict__ G, double2 *__restrict__ out) {
+  constexpr int nr = NR;
   const long j = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (j >= n) return;
-  double2 acc[DR_MAX_ROWS];
+  double2 acc[NR];
 #pragma unroll
-  for (int r = 0; r < DR_MAX_ROWS; ++r) acc[r] = make_double2(0.0, 0.0);
+  for (int r = 0; r < NR; ++r) acc[r] = make_double2(0.0, 0.0);
   for (int q = lane; q < np; q += 32) {
     const int l = Pidx[q];
     double2 hv = G[(size_t)j * n + l];
     if (l == j) hv.x -= 1.0;
 #pragma unroll
-    for (int r = 0; r < DR_MAX_ROWS; ++r)
-      if (r < nr) {
-        const double2 x = X[(size_t)r * n + l];
-        acc[r].x += x.x * hv.x - x.y * hv.y;
-        acc[r].y += x.x * hv.y + x.y * hv.x;
-      }
+    for (int r = 0; r < NR; ++r) {
+      const double2 x = X[(size_t)r * n + l];
+      acc[r].x += x.x * hv.x - x.y * hv.y;
+      acc[r].y += x.x * hv.y + x.y * hv.x;
+    }
   }
 #pragma unroll
-  for (int r = 0; r < DR_MAX_ROWS; ++r) {
+  for (int r = 0; r < NR; ++r) {
     for (int o = 16; o; o >>= 1) {
       acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, o);
       acc[r].y += __shfl_xor_sync(0xffffffffu, acc[r].y, o);
@@ -452,30 +454,31 @@ __global__ void k_rows_residual(const double2 *__restrict__ X, const double2 *__
 // X[r][j] -= Rk[r][j] - sum_{l in P} Rk[r][P_l] T[P_l][j]: 32 columns per CTA
 // (lane = column, so each warp reads 256 contiguous bytes of a row of T), the
 // sum over P split across the CTA's 8 warps and reduced in shared memory.
-__global__ void __launch_bounds__(256) k_rows_refine(double2 *__restrict__ X, const double2 *__restrict__ Rk, int nr,
-                                                     long n, const int *__restrict__ Pidx, int np,
+template <int NR>
+__global__ void __launch_bounds__(256) k_rows_refine(double2 *__restrict__ X, const double2 *__restrict__ Rk, long n,
+                                                     const int *__restrict__ Pidx, int np,
                                                      const float2 *__restrict__ T32, long ldm) {
-  __shared__ double2 part[8][DR_MAX_ROWS][32];
+  constexpr int nr = NR;
+  __shared__ double2 part[8][NR][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const long j = (long)blockIdx.x * 32 + lane;
-  double2 acc[DR_MAX_ROWS];
+  double2 acc[NR];
 #pragma unroll
-  for (int r = 0; r < DR_MAX_ROWS; ++r) acc[r] = make_double2(0.0, 0.0);
+  for (int r = 0; r < NR; ++r) acc[r] = make_double2(0.0, 0.0);
   if (j < n)
     for (int q = w; q < np; q += 8) {
       const int l = Pidx[q];
       const float2 tf = T32[(size_t)l * ldm + j];
       const double2 t = make_double2(tf.x, tf.y);
 #pragma unroll
-      for (int r = 0; r < DR_MAX_ROWS; ++r)
-        if (r < nr) {
-          const double2 rv = Rk[(size_t)r * n + l];
-          acc[r].x += rv.x * t.x - rv.y * t.y;
-          acc[r].y += rv.x * t.y + rv.y * t.x;
-        }
+      for (int r = 0; r < NR; ++r) {
+        const double2 rv = Rk[(size_t)r * n + l];
+        acc[r].x += rv.x * t.x - rv.y * t.y;
+        acc[r].y += rv.x * t.y + rv.y * t.x;
+      }
     }
 #pragma unroll
-  for (int r = 0; r < DR_MAX_ROWS; ++r) part[w][r][lane] = acc[r];
+  for (int r = 0; r < NR; ++r) part[w][r][lane] = acc[r];
   __syncthreads();
   if (w == 0 && j < n)
     for (int r = 0; r < nr; ++r) {
@@ -570,9 +573,26 @@ cudaError_t launch_drift_rows(Handle *h, int f, const int *d_rows, int nr, const
   if (nr < 1 || nr > DR_MAX_ROWS) return cudaErrorInvalidValue;
   const unsigned g1 = (unsigned)((n + 255) / 256), gw = (unsigned)((n * 32 + 255) / 256);
   k_rows_load<<<g1, 256, 0, h->stream>>>(q.T32, h->ldm, d_rows, nr, n, X);
-  k_rows_PH<<<gw, 256, 0, h->stream>>>(X, nr, n, d_P, np, q.G, PH);
-  k_rows_residual<<<g1, 256, 0, h->stream>>>(X, PH, q.G, d_rows, nr, n, Rk);
-  k_rows_refine<<<(unsigned)((n + 31) / 32), 256, 0, h->stream>>>(X, Rk, nr, n, d_P, np, q.T32, h->ldm);
+  const unsigned gr = (unsigned)((n + 31) / 32);
+  switch (nr) {
+#define PNGF_DRIFT_ROWS(NRV)                                                                     \
+  case NRV:                                                                                      \
+    k_rows_PH<NRV><<<gw, 256, 0, h->stream>>>(X, n, d_P, np, q.G, PH);                           \
+    k_rows_residual<<<g1, 256, 0, h->stream>>>(X, PH, q.G, d_rows, nr, n, Rk);                   \
+    k_rows_refine<NRV><<<gr, 256, 0, h->stream>>>(X, Rk, n, d_P, np, q.T32, h->ldm);             \
+    break;
+    PNGF_DRIFT_ROWS(1)
+    PNGF_DRIFT_ROWS(2)
+    PNGF_DRIFT_ROWS(3)
+    PNGF_DRIFT_ROWS(4)
+    PNGF_DRIFT_ROWS(5)
+    PNGF_DRIFT_ROWS(6)
+    PNGF_DRIFT_ROWS(7)
+    PNGF_DRIFT_ROWS(8)
+#undef PNGF_DRIFT_ROWS
+    default:
+      return cudaErrorInvalidValue;
+  }
   k_rows_compare<<<g1, 256, 0, h->stream>>>(q.T32, h->ldm, d_rows, nr, n, X, d_out);
   h->nlaunch += 5;
   return cudaGetLastError();

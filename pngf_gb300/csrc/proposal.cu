@@ -246,38 +246,45 @@ __global__ void __launch_bounds__(CT_THREADS) k_conv_tile(const float *__restric
 }
 
 // Partial weight gradients: dwp[s][o][i][k] = sum over the s-th of CT_WS
-// slices of the B x H x W pixels of dz[b][o][p] x[b][i][p + d(k)], and the
-// bias term (k = 9, sum dz) from the blocks of input channel 0. One block per
-// (input channel, group of CO_T output channels, pixel slice); a fixed-order
-// block reduction, then k_conv_wsum adds the slices in order (deterministic).
+// slices of the batch of sum_p dz[b][o][p] x[b][i][p + d(k)], and the bias
+// term (k = 9, sum dz) from the blocks of input channel 0. One block per
+// (input channel, group of CO_T output channels, batch slice); each thread
+// takes pixels p = tid, tid + 256, ..., works out which of its taps fall
+// inside the map once per pixel, and walks the slice's images; a fixed-order block
+// reduction, then k_conv_wsum adds the slices in order (deterministic).
 constexpr int CT_WS = 4;
 template <int CO_T>
 __global__ void __launch_bounds__(256) k_conv_wgrad(const float *__restrict__ x, const float *__restrict__ dz,
                                                     float *__restrict__ dwp, int B, int Ci, int Co, int H, int W) {
   const int i = blockIdx.x, o0 = blockIdx.y * CO_T, sl = blockIdx.z;
-  const int HW = H * W, np = B * HW;
-  const int p0 = (int)(((long)np * sl) / CT_WS), p1 = (int)(((long)np * (sl + 1)) / CT_WS);
+  const int HW = H * W;
+  const int b0 = (int)(((long)B * sl) / CT_WS), b1 = (int)(((long)B * (sl + 1)) / CT_WS);
   float acc[CO_T][10];
 #pragma unroll
   for (int c = 0; c < CO_T; ++c)
 #pragma unroll
     for (int k = 0; k < 10; ++k) acc[c][k] = 0.f;
-  for (int idx = p0 + threadIdx.x; idx < p1; idx += blockDim.x) {
-    const int bb = idx / HW, p = idx - bb * HW;
+  for (int p = threadIdx.x; p < HW; p += 256) {  // this thread's pixels
     const int py = p / W, px = p - py * W;
-    const float *xc = x + ((size_t)bb * Ci + i) * HW;
-    float xv[9];
+    unsigned valid = 0;  // bit k: tap k inside the map
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       const int yy = py + k / 3 - 1, xx = px + k % 3 - 1;
-      xv[k] = (yy >= 0 && yy < H && xx >= 0 && xx < W) ? xc[yy * W + xx] : 0.f;
+      if (yy >= 0 && yy < H && xx >= 0 && xx < W) valid |= 1u << k;
     }
+    for (int bb = b0; bb < b1; ++bb) {
+      const float *xc = x + ((size_t)bb * Ci + i) * HW;
+      const float *dzb = dz + ((size_t)bb * Co + o0) * HW;
+      float xv[9];
 #pragma unroll
-    for (int c = 0; c < CO_T; ++c) {
-      const float g = dz[((size_t)bb * Co + o0 + c) * HW + p];
+      for (int k = 0; k < 9; ++k) xv[k] = (valid >> k) & 1u ? xc[p + (k / 3 - 1) * W + (k % 3 - 1)] : 0.f;
 #pragma unroll
-      for (int k = 0; k < 9; ++k) acc[c][k] = fmaf(g, xv[k], acc[c][k]);
-      acc[c][9] += g;
+      for (int c = 0; c < CO_T; ++c) {
+        const float g = dzb[(size_t)c * HW + p];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[c][k] = fmaf(g, xv[k], acc[c][k]);
+        acc[c][9] += g;
+      }
     }
   }
   __shared__ float red[8][CO_T * 10];
@@ -490,7 +497,9 @@ int prop_alloc_batch(pngf_prop *p, int B) {
 }
 
 // Whether the tiled kernels take this network (map width and channels).
-bool tiled_ok(const pngf_prop *p) { return p->W <= CT_MAXW && p->C <= CT_MAXC && p->C % 8 == 0; }
+bool tiled_ok(const pngf_prop *p) {
+  return p->W <= CT_MAXW && p->C <= CT_MAXC && p->C % 8 == 0;
+}
 
 int tile_rows(const pngf_prop *p) { return std::max(1, std::min(p->H, CT_BAND / p->W)); }
 
