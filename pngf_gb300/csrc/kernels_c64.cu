@@ -235,42 +235,65 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 }
 
 // A_op rows i < n: 3xTF32 segments of the interleaved real form of A[i, :].
-__global__ void k_build_Aop(const double2 *__restrict__ A, long lda, long n, int k, int Kt, long ldk,
-                            float *__restrict__ Aop) {
-  const long i = (long)blockIdx.y;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || c >= Kt) return;
-  float v = 0.f;
-  const int k2 = 2 * k;
-  if (c < 3 * k2) {
-    const int seg = c / k2, w = c - seg * k2, r = w >> 1;
-    const double2 a = A[(size_t)r * lda + i];
-    const float x = (float)((w & 1) ? a.y : a.x);
-    const float hi = to_tf32(x);
-    v = seg == 2 ? to_tf32(x - hi) : hi;
+// One block per 32 rows: A's 32 x k block is read column-coalesced into shared
+// memory, then the rows of A_op are written along K.
+constexpr int BO_ROWS = 32;   // A_op rows per block
+constexpr int BO_COLS = 16;   // complex columns of W per block (32 rows of B_op)
+__global__ void __launch_bounds__(256) k_build_Aop(const double2 *__restrict__ A, long lda, long n, int k, int Kt,
+                                                   long ldk, float *__restrict__ Aop) {
+  extern __shared__ double2 bsm[];  // k x (BO_ROWS + 1)
+  const long i0 = (long)blockIdx.x * BO_ROWS;
+  for (int idx = threadIdx.x; idx < k * BO_ROWS; idx += blockDim.x) {
+    const int r = idx / BO_ROWS, ii = idx - r * BO_ROWS;
+    bsm[r * (BO_ROWS + 1) + ii] = i0 + ii < n ? A[(size_t)r * lda + i0 + ii] : make_double2(0.0, 0.0);
   }
-  Aop[(size_t)i * ldk + c] = v;
+  __syncthreads();
+  const int k2 = 2 * k;
+  for (int idx = threadIdx.x; idx < BO_ROWS * Kt; idx += blockDim.x) {
+    const int ii = idx / Kt, c = idx - ii * Kt;
+    const long i = i0 + ii;
+    if (i >= n) break;
+    float v = 0.f;
+    if (c < 3 * k2) {
+      const int seg = c / k2, w = c - seg * k2, r = w >> 1;
+      const double2 a = bsm[r * (BO_ROWS + 1) + ii];
+      const float x = (float)((w & 1) ? a.y : a.x);
+      const float hi = to_tf32(x);
+      v = seg == 2 ? to_tf32(x - hi) : hi;
+    }
+    Aop[(size_t)i * ldk + c] = v;
+  }
 }
 
 // B_op rows j' < 2n: output column j' = 2j (real part) or 2j+1 (imaginary).
-__global__ void k_build_Bop(const double2 *__restrict__ W, long ldw, long n, int k, int Kt, long ldk,
-                            float *__restrict__ Bop) {
-  const long jp = (long)blockIdx.y;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (jp >= 2 * n || c >= Kt) return;
-  float v = 0.f;
-  const int k2 = 2 * k;
-  if (c < 3 * k2) {
-    const int seg = c / k2, w = c - seg * k2, r = w >> 1;
-    const double2 wv = W[(size_t)r * ldw + (jp >> 1)];
-    double b;
-    if ((jp & 1) == 0) b = (w & 1) ? -wv.y : wv.x;  // Re out: Re A Re W - Im A Im W
-    else b = (w & 1) ? wv.x : wv.y;                 // Im out: Re A Im W + Im A Re W
-    const float x = (float)b;
-    const float hi = to_tf32(x);
-    v = seg == 1 ? to_tf32(x - hi) : hi;
+// One block per 16 columns of W (32 rows of B_op), staged like k_build_Aop.
+__global__ void __launch_bounds__(256) k_build_Bop(const double2 *__restrict__ W, long ldw, long n, int k, int Kt,
+                                                   long ldk, float *__restrict__ Bop) {
+  extern __shared__ double2 bsm[];  // k x (BO_COLS + 1)
+  const long j0 = (long)blockIdx.x * BO_COLS;
+  for (int idx = threadIdx.x; idx < k * BO_COLS; idx += blockDim.x) {
+    const int r = idx / BO_COLS, jj = idx - r * BO_COLS;
+    bsm[r * (BO_COLS + 1) + jj] = j0 + jj < n ? W[(size_t)r * ldw + j0 + jj] : make_double2(0.0, 0.0);
   }
-  Bop[(size_t)jp * ldk + c] = v;
+  __syncthreads();
+  const int k2 = 2 * k;
+  for (int idx = threadIdx.x; idx < 2 * BO_COLS * Kt; idx += blockDim.x) {
+    const int jl = idx / Kt, c = idx - jl * Kt;
+    const long jp = 2 * j0 + jl;
+    if (jp >= 2 * n) break;
+    float v = 0.f;
+    if (c < 3 * k2) {
+      const int seg = c / k2, w = c - seg * k2, r = w >> 1;
+      const double2 wv = bsm[r * (BO_COLS + 1) + (jl >> 1)];
+      double b;
+      if ((jp & 1) == 0) b = (w & 1) ? -wv.y : wv.x;  // Re out: Re A Re W - Im A Im W
+      else b = (w & 1) ? wv.x : wv.y;                 // Im out: Re A Im W + Im A Re W
+      const float x = (float)b;
+      const float hi = to_tf32(x);
+      v = seg == 1 ? to_tf32(x - hi) : hi;
+    }
+    Bop[(size_t)jp * ldk + c] = v;
+  }
 }
 
 // Deferred updates: appends the T part of an accept to the pending factors,
@@ -676,9 +699,11 @@ cudaError_t launch_c64_update(Handle *h, int f, int k) {
   cudaStream_t st = lane_stream(h, f);
   cudaError_t e = launch_side_update(h, f, k);  // FP64 side: y and R/Eobj
   if (e != cudaSuccess) return e;
-  const dim3 ga((unsigned)((Kt + 127) / 128), (unsigned)n), gb((unsigned)((Kt + 127) / 128), (unsigned)(2 * n));
-  k_build_Aop<<<ga, 128, 0, st>>>(L.A, rows, n, k, Kt, h->kt_cap, L.Aop);
-  k_build_Bop<<<gb, 128, 0, st>>>(L.W, h->ldm, n, k, Kt, h->kt_cap, L.Bop);
+  const size_t sma = sizeof(double2) * (size_t)k * (BO_ROWS + 1), smb = sizeof(double2) * (size_t)k * (BO_COLS + 1);
+  if ((e = cudaFuncSetAttribute(k_build_Aop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma)) != cudaSuccess)
+    return e;
+  k_build_Aop<<<(unsigned)((n + BO_ROWS - 1) / BO_ROWS), 256, sma, st>>>(L.A, rows, n, k, Kt, h->kt_cap, L.Aop);
+  k_build_Bop<<<(unsigned)((n + BO_COLS - 1) / BO_COLS), 256, smb, st>>>(L.W, h->ldm, n, k, Kt, h->kt_cap, L.Bop);
   h->nlaunch += 2;
   return launch_c64_tc(h, f, Kt, k);
 }

@@ -393,30 +393,32 @@ __global__ void k_to_bf16(const float *__restrict__ w, __nv_bfloat16 *__restrict
   if (i < n) wb[i] = __float2bfloat16_rn(w[i]);
 }
 
-// Channel 1 of the features: per tile, mean log |T_ee| over its edges (frequency 0).
+// Channel 1 of the features: per tile, mean log |T_ee| over its edges
+// (frequency 0). One warp per tile, lanes over its edges (their diagonal
+// entries load concurrently), the sum reduced in a fixed order.
 template <typename TM>
 __global__ void k_tile_sensitivity(const TM *__restrict__ T, long ldt, int tiles_x, int tiles_y, int cells_x,
                                    int cells_y, int ex_xsz, int ey_xsz, long nx, float *__restrict__ out) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (int)(((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (t >= tiles_x * tiles_y) return;
   const int ty = t / tiles_x, tx = t - ty * tiles_x;
+  const int nxe = (cells_y + 1) * cells_x, nye = cells_y * (cells_x + 1);
   double s = 0.0;
-  int cnt = 0;
-  for (int jj = 0; jj <= cells_y; ++jj)
-    for (int ii = 0; ii < cells_x; ++ii) {
-      const long e = (long)(tx * cells_x + ii) + (long)(ty * cells_y + jj) * ex_xsz;
-      const TM v = T[(size_t)e * ldt + e];
-      s += log(hypot((double)v.x, (double)v.y) + 1e-300);
-      ++cnt;
+  for (int q = lane; q < nxe + nye; q += 32) {
+    long e;
+    if (q < nxe) {
+      const int jj = q / cells_x, ii = q - jj * cells_x;
+      e = (long)(tx * cells_x + ii) + (long)(ty * cells_y + jj) * ex_xsz;
+    } else {
+      const int r = q - nxe, jj = r / (cells_x + 1), ii = r - jj * (cells_x + 1);
+      e = nx + (long)(tx * cells_x + ii) + (long)(ty * cells_y + jj) * ey_xsz;
     }
-  for (int jj = 0; jj < cells_y; ++jj)
-    for (int ii = 0; ii <= cells_x; ++ii) {
-      const long e = nx + (long)(tx * cells_x + ii) + (long)(ty * cells_y + jj) * ey_xsz;
-      const TM v = T[(size_t)e * ldt + e];
-      s += log(hypot((double)v.x, (double)v.y) + 1e-300);
-      ++cnt;
-    }
-  out[t] = (float)(s / cnt);
+    const TM v = T[(size_t)e * ldt + e];
+    s += log(hypot((double)v.x, (double)v.y) + 1e-300);
+  }
+  for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[t] = (float)(s / (nxe + nye));
 }
 
 }  // namespace
@@ -816,11 +818,11 @@ static int prop_features(pngf_prop *p, int slot, float *feat) {
   if (!h->prepared) return prop_err(p, PNGF_ERR_STATE, "handle not prepared");
   const int HW = p->map_sz;
   if (h->cfg.precision == PNGF_PREC_FP64)
-    k_tile_sensitivity<double2><<<(HW + 127) / 128, 128, 0, h->stream>>>(
+    k_tile_sensitivity<double2><<<(HW + 3) / 4, 128, 0, h->stream>>>(
         h->f[0].M64, h->ldm, h->cfg.tiles_x, h->cfg.tiles_y, h->cfg.cells_x, h->cfg.cells_y, h->ex_xsz, h->ey_xsz,
         h->nx, p->d_sens);
   else
-    k_tile_sensitivity<float2><<<(HW + 127) / 128, 128, 0, h->stream>>>(
+    k_tile_sensitivity<float2><<<(HW + 3) / 4, 128, 0, h->stream>>>(
         h->f[0].T32, h->ldm, h->cfg.tiles_x, h->cfg.tiles_y, h->cfg.cells_x, h->cfg.cells_y, h->ex_xsz, h->ey_xsz,
         h->nx, p->d_sens);
   std::vector<float> sens(HW), f(3 * HW);
