@@ -150,6 +150,9 @@ static int ensure_cand_cap(Handle *h, int ncand) {
   dfree(h->d_perf);
   dfree(h->d_F);
   dfree(h->d_status);
+  dfree(h->d_eval_LU);
+  dfree(h->d_eval_piv);
+  dfree(h->d_eval_z);
   if (h->h_tiles) cudaFreeHost(h->h_tiles);
   if (h->h_nflip) cudaFreeHost(h->h_nflip);
   h->h_tiles = h->h_nflip = nullptr;
@@ -160,7 +163,10 @@ static int ensure_cand_cap(Handle *h, int ncand) {
       (rc = dalloc(h, &h->d_ed, (size_t)cap * h->kmax)) || (rc = dalloc(h, &h->d_ek, (size_t)cap)) ||
       (rc = dalloc(h, &h->d_new_eobj, (size_t)cap * nf * h->E)) || (rc = dalloc(h, &h->d_Ff, (size_t)cap * nf)) ||
       (rc = dalloc(h, &h->d_perf, (size_t)cap * nf * 3)) || (rc = dalloc(h, &h->d_F, (size_t)cap)) ||
-      (rc = dalloc(h, &h->d_status, (size_t)cap * nf)))
+      (rc = dalloc(h, &h->d_status, (size_t)cap * nf)) ||
+      (rc = dalloc(h, &h->d_eval_LU, (size_t)cap * nf * h->kmax * h->kmax)) ||
+      (rc = dalloc(h, &h->d_eval_piv, (size_t)cap * nf * h->kmax)) ||
+      (rc = dalloc(h, &h->d_eval_z, (size_t)cap * nf * h->kmax)))
     return rc;
   PNGF_CUDA(h, cudaMallocHost(&h->h_tiles, sizeof(int) * (size_t)cap * h->cfg.max_flips));
   PNGF_CUDA(h, cudaMallocHost(&h->h_nflip, sizeof(int) * (size_t)cap));
@@ -329,9 +335,11 @@ int accept_cand_async(Handle *h, int c, int k, bool check_now) {
   // flush them to T when another accept might not fit
   h->defer_now = h->defer_cap > 0;
   h->defer_flush = h->defer_now && h->defer_rp + k + h->kmax > h->defer_cap;
+  h->acc_cand = c;  // the accept starts from the factorization its evaluation left
   for (int f = 0; f < h->cfg.num_freq && rc == PNGF_OK; ++f)
     rc = cuda_check(h, launch_accept_edges(h, f, h->d_es + (size_t)c * h->kmax, h->d_ed + (size_t)c * h->kmax, k,
                                            h->cfg.precision), "accept");
+  h->acc_cand = -1;
   h->defer_now = false;
   if (rc) return rc;
   if ((rc = lanes_join(h))) return rc;
@@ -439,6 +447,9 @@ int pngf_destroy(pngf_handle *ph) {
   dfree(h->d_F);
   dfree(h->d_first);
   dfree(h->d_status);
+  dfree(h->d_eval_LU);
+  dfree(h->d_eval_piv);
+  dfree(h->d_eval_z);
   dfree(h->d_acc_s);
   dfree(h->d_acc_d);
   dfree(h->d_acc_status);

@@ -428,13 +428,22 @@ __device__ int cta_capacitance(const SV<TM> &M, long n, const double2 *__restric
 // ---------------------------------------------------------------------------
 // evaluation
 
+// Where the candidate kernels leave each (candidate, frequency)'s factored
+// capacitance matrix for the accept: LU (kmax x kmax, column-major, leading
+// dimension kmax), row interchanges and z, at slot c * nf + f.
+struct LuOut {
+  double2 *LU;
+  int *piv;
+  double2 *z;
+};
+
 template <typename TM, int NT>
 __global__ void __launch_bounds__(NT) k_eval(const SV<TM> *__restrict__ Ms, const double2 *const *__restrict__ Eincs,
                                               long n, int E, int kmax, const int *__restrict__ es,
                                               const signed char *__restrict__ ed, const int *__restrict__ ek,
                                               const FreqConst *__restrict__ fconst, ObjConst oc, int nf,
                                               double2 *__restrict__ new_eobj, double *__restrict__ Ff,
-                                              double *__restrict__ perf, int *__restrict__ status) {
+                                              double *__restrict__ perf, int *__restrict__ status, LuOut lo) {
   extern __shared__ double2 smem[];
   const int c = blockIdx.x, f = blockIdx.y;
   const int tid = threadIdx.x;
@@ -462,6 +471,18 @@ __global__ void __launch_bounds__(NT) k_eval(const SV<TM> *__restrict__ Ms, cons
   }
   __syncthreads();
   const int info = cta_capacitance(M, n, Eincs[f], s, d, k, K, ld, vec, einc, piv, red);
+  if (lo.LU) {  // the factorization, for an accept of this candidate
+    const size_t cf = (size_t)c * nf + f;
+    double2 *LUo = lo.LU + cf * kmax * kmax;
+    for (int idx = tid; idx < k * k; idx += blockDim.x) {
+      const int i = idx % k, q = idx / k;
+      LUo[i + (size_t)q * kmax] = K[i + q * ld];
+    }
+    for (int q = tid; q < k; q += blockDim.x) {
+      lo.piv[cf * kmax + q] = piv[q];
+      lo.z[cf * kmax + q] = vec[q];
+    }
+  }
   // newEobj = Eobj - R[:,s] z, one warp per objective row.
   const int w = tid / 32, lane = tid % 32;
   for (int e = w; e < E; e += blockDim.x / 32) {
@@ -501,7 +522,7 @@ __global__ void __launch_bounds__(32 * WPC)
                 int ncand, const int *__restrict__ es, const signed char *__restrict__ ed,
                 const int *__restrict__ ek, const FreqConst *__restrict__ fconst, ObjConst oc, int nf,
                 double2 *__restrict__ new_eobj, double *__restrict__ Ff, double *__restrict__ perf,
-                int *__restrict__ status) {
+                int *__restrict__ status, LuOut lo) {
   extern __shared__ double2 smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * WPC + warp, f = blockIdx.y;
@@ -608,6 +629,13 @@ __global__ void __launch_bounds__(32 * WPC)
   }
   double2 z = cadd(einc_l, w);
   if (d_l < 0) z = make_double2(-z.x, -z.y);
+  if (lo.LU && lane < k) {  // the factorization, for an accept of this candidate
+    const size_t cf = (size_t)c * nf + f;
+    double2 *LUo = lo.LU + cf * kmax * kmax;
+    for (int q = 0; q < k; ++q) LUo[lane + (size_t)q * kmax] = K[lane + q * ld];
+    lo.piv[cf * kmax + lane] = piv_l;
+    lo.z[cf * kmax + lane] = z;
+  }
   // newEobj = Eobj - R[:,s] z, reduced across the warp as k_eval does.
   double2 eo[PNGF_MAX_EOBJ];
   for (int e = 0; e < E; ++e) {
@@ -769,13 +797,13 @@ __global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int 
 }
 
 // Vneg = -D K^-1 (k x k, column-major: Vneg[r + c*k]) from K's LU (LU[i +
-// q*k]: unit L below the diagonal, U on and above) and its row interchanges:
+// q*ldlu]: unit L below the diagonal, U on and above) and its row interchanges:
 // one warp per column c solves K x = e_c (the substitutions of k_acc_W, with
 // U's diagonal inverted once). INV_COLS columns per CTA share the LU, staged in
 // shared memory so that the sequential steps never wait on global memory.
 constexpr int INV_COLS = 4;
 constexpr int kMaxTcW = 96;  // edges per accept on the tensor-core W path (the LU fits shared memory)
-__global__ void __launch_bounds__(32 * INV_COLS) k_acc_inverse(const double2 *__restrict__ LU,
+__global__ void __launch_bounds__(32 * INV_COLS) k_acc_inverse(const double2 *__restrict__ LU, int ldlu,
                                                                const int *__restrict__ gpiv,
                                                                const signed char *__restrict__ gd, int k,
                                                                double2 *__restrict__ Vneg) {
@@ -784,10 +812,10 @@ __global__ void __launch_bounds__(32 * INV_COLS) k_acc_inverse(const double2 *__
   double2 *rdiag = K + (size_t)k * k;          // 1 / U[q][q]
   double2 *xs = rdiag + k;                     // INV_COLS x k
   __shared__ int piv[kMaxK];
-  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) K[idx] = LU[idx];
+  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) K[idx] = LU[(idx % k) + (size_t)(idx / k) * ldlu];
   for (int q = threadIdx.x; q < k; q += blockDim.x) {
     piv[q] = gpiv[q];
-    rdiag[q] = crecip(LU[q + (size_t)q * k]);
+    rdiag[q] = crecip(LU[q + (size_t)q * ldlu]);
   }
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1002,7 +1030,7 @@ template <typename TM, int NT> static cudaError_t launch_eval_cta(Handle *h, int
   k_eval<TM, NT><<<dim3(ncand, nf), NT, sm, h->stream>>>(
       static_cast<const SV<TM> *>(h->d_views), reinterpret_cast<const double2 *const *>(h->d_Eincs), h->n, h->E,
       h->kmax, h->d_es, h->d_ed, h->d_ek, h->d_fconst, obj_const(h), nf, h->d_new_eobj, h->d_Ff, h->d_perf,
-      h->d_status);
+      h->d_status, LuOut{h->d_eval_LU, h->d_eval_piv, h->d_eval_z});
   return cudaGetLastError();
 }
 
@@ -1014,7 +1042,7 @@ template <typename TM, int WPC> static cudaError_t launch_eval_warp(Handle *h, i
   k_eval_warp<TM, WPC><<<dim3((ncand + WPC - 1) / WPC, nf), 32 * WPC, sm, h->stream>>>(
       static_cast<const SV<TM> *>(h->d_views), reinterpret_cast<const double2 *const *>(h->d_Eincs), h->n, h->E,
       h->kmax, ncand, h->d_es, h->d_ed, h->d_ek, h->d_fconst, obj_const(h), nf, h->d_new_eobj, h->d_Ff, h->d_perf,
-      h->d_status);
+      h->d_status, LuOut{h->d_eval_LU, h->d_eval_piv, h->d_eval_z});
   return cudaGetLastError();
 }
 
@@ -1079,7 +1107,8 @@ static cudaError_t accept_prologue(const SV<TM> &v, long n, int E, long ldm, con
   return cudaGetLastError();
 }
 
-// Accept prologue with W on the tensor cores: K's LU and z, Vneg = -D K^-1,
+// Accept prologue with W on the tensor cores: K's LU and z (those the candidate
+// kernel left, for a candidate of the evaluated batch), Vneg = -D K^-1,
 // W = [D K^-1 T[s, 0:N], z] as Vneg times the rows s of the state with the
 // FP64-accurate tensor-core product, A = [T; R][:, s]. For the FP64 layout and
 // the complex64 one without deferred updates (whose rows are read as stored).
@@ -1089,16 +1118,30 @@ static cudaError_t accept_prologue_tc(Handle *h, int f, const SV<TM> &v, const v
   const long n = h->n, rows = n + h->E;
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
-  const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
-  cudaError_t e = cudaFuncSetAttribute(k_acc_factor<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
-  if (e != cudaSuccess) return e;
-  k_acc_factor<TM><<<1, 256, smf, st>>>(v, n, Einc, d_s, d_d, k, L.LU, L.piv, L.z, h->d_acc_status);
+  cudaError_t e;
+  const double2 *LU = L.LU, *z = L.z;
+  const int *piv = L.piv;
+  int ldlu = k;
+  if (h->acc_cand >= 0) {  // a candidate of the evaluated batch: its kernel left K's LU and z
+    const size_t cf = (size_t)h->acc_cand * h->cfg.num_freq + f, km = (size_t)h->kmax;
+    LU = h->d_eval_LU + cf * km * km;
+    piv = h->d_eval_piv + cf * km;
+    z = h->d_eval_z + cf * km;
+    ldlu = h->kmax;
+  } else {
+    const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
+    if ((e = cudaFuncSetAttribute(k_acc_factor<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf)) !=
+        cudaSuccess)
+      return e;
+    k_acc_factor<TM><<<1, 256, smf, st>>>(v, n, Einc, d_s, d_d, k, L.LU, L.piv, L.z, h->d_acc_status);
+    h->nlaunch += 1;
+  }
   const size_t smi = sizeof(double2) * ((size_t)k * k + k + (size_t)INV_COLS * k);
   if ((e = cudaFuncSetAttribute(k_acc_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smi)) != cudaSuccess)
     return e;
-  k_acc_inverse<<<(unsigned)((k + INV_COLS - 1) / INV_COLS), 32 * INV_COLS, smi, st>>>(L.LU, L.piv, d_d, k, L.V);
-  k_W_init<<<dim3((unsigned)((h->ldm + 255) / 256), (unsigned)k), 256, 0, st>>>(L.W, h->ldm, n, L.z, k);
-  h->nlaunch += 3;
+  k_acc_inverse<<<(unsigned)((k + INV_COLS - 1) / INV_COLS), 32 * INV_COLS, smi, st>>>(LU, ldlu, piv, d_d, k, L.V);
+  k_W_init<<<dim3((unsigned)((h->ldm + 255) / 256), (unsigned)k), 256, 0, st>>>(L.W, h->ldm, n, z, k);
+  h->nlaunch += 2;
   if ((e = launch_f64tc_wgemm(h, f, k, L.V, X, x32, h->ldm, d_s, L.W)) != cudaSuccess) return e;
   k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, st>>>(v, n, rows, d_s, k, L.A, rows);
   h->nlaunch += 1;

@@ -128,6 +128,10 @@ struct Handle {
   double *d_F = nullptr;                        // ncand
   int *d_first = nullptr;
   int *d_status = nullptr;                      // per-candidate LU status
+  double2 *d_eval_LU = nullptr;                 // ncand x nf x kmax^2: each candidate's factored K (for its accept)
+  int *d_eval_piv = nullptr;                    // ncand x nf x kmax
+  double2 *d_eval_z = nullptr;                  // ncand x nf x kmax
+  int acc_cand = -1;                            // candidate of the evaluated batch being accepted, else -1
   int batch_n = 0;
   int launched_n = 0;      // batch enqueued by eval_launch, not yet collected
   int staged_n = 0;        // batch staged by eval_stage
