@@ -792,11 +792,13 @@ static int prepare_impl(Handle *h, bool fp64) {
   // frequencies build independently, one lane (stream + scratch) each
   int rc = lanes_fork(h);
   if (rc) return rc;
+  h->building = true;
   for (int f = 0; f < h->cfg.num_freq && rc == PNGF_OK; ++f) {
     rc = stage_in(h, f, true, true);
     if (rc == PNGF_OK) rc = build(f);
     stage_out(h, f);
   }
+  h->building = false;
   const int rj = lanes_join(h);
   if (rc) return rc;
   if (rj) return rj;

@@ -132,6 +132,7 @@ struct Handle {
   int *d_eval_piv = nullptr;                    // ncand x nf x kmax
   double2 *d_eval_z = nullptr;                  // ncand x nf x kmax
   int acc_cand = -1;                            // candidate of the evaluated batch being accepted, else -1
+  bool building = false;                        // inside a build of the state (prepare / refresh)
   int batch_n = 0;
   int launched_n = 0;      // batch enqueued by eval_launch, not yet collected
   int staged_n = 0;        // batch staged by eval_stage
@@ -270,13 +271,14 @@ size_t f64tc_b_cols();   // row pitch of the B slices (elements)
 long f64tc_b_rows(long n);  // rows of the B slices: 7 per output column, 32-column tiles stacked
 // M -= A W for M ((N+E) x ldm complex128), A ((N+E) x k column-major), W (k x ldm),
 // with frequency f's lane scratch and stream.
-// Grid of a persistent update kernel (one CTA per SM) over ntiles tiles: with
-// several frequency lanes it leaves kReservedSMs SMs free, so that the other
-// lanes' single-CTA kernels (capacitance LU, explicit inverse) run beside it
-// instead of waiting for it to end.
+// Grid of a persistent update kernel (one CTA per SM) over ntiles tiles:
+// during a build with several frequency lanes it leaves kReservedSMs SMs
+// free, so that the other lanes' single-CTA capacitance LUs run beside it
+// instead of waiting for it to end (an accept of an evaluated candidate has
+// no LU to run: it starts from the evaluation's).
 constexpr int kReservedSMs = 8;
 inline int persistent_grid(const Handle *h, int ntiles, int nsm) {
-  const int g = h->lanes.size() > 1 && nsm > 2 * kReservedSMs ? nsm - kReservedSMs : nsm;
+  const int g = h->building && h->lanes.size() > 1 && nsm > 2 * kReservedSMs ? nsm - kReservedSMs : nsm;
   return ntiles < g ? ntiles : g;
 }
 cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W);
