@@ -61,6 +61,10 @@ def parse():
     ap.add_argument("--tiles", type=int, default=21)
     ap.add_argument("--mode", choices=["single", "sym"], default="single")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--batch", type=int, default=-16,
+                    help="DBS speculative batch of the timed runs and of the plain convergence run: < 0 adaptive "
+                         "(-batch draws after an accept, doubling after a batch without one), 0 = the whole "
+                         "remaining hat, > 0 fixed; every size keeps the reference's evaluation order")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", default="fp64,c64,c64d", help="precision forms to run; the first is the headline")
     ap.add_argument("--nfreq", type=int, default=5, help="use the first NFREQ of the five frequencies")
@@ -233,7 +237,7 @@ def run_form(a, precision, Gs, rank, local, dist, defer_rank=0):
     for f, G in enumerate(Gs):
         h.load_G(f, G, None)
     d = lib.Dbs(h, mode=lib.DBS_SINGLE if a.mode == "single" else lib.DBS_SYMMETRIC, init=lib.INIT_RANDOM,
-                seed=a.seed + rank, batch=0)
+                seed=a.seed + rank, batch=a.batch)
     tune = h.autotune()  # kernel forms for this instance; the state is left unchanged
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t_setup
@@ -302,7 +306,7 @@ def autotune_on(h, mode_single=True):
 
 
 def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), train_evals=1500, train_steps=600,
-                     topk=64, state_only=0):
+                     topk=64, state_only=0, batch=0):
     """Wall time to the converged objective: plain FP64 DBS (reference order,
     run until the hat is empty) against the proposal + complex64 form, whose
     network is trained only on plain complex64 runs from other seeds. The
@@ -318,7 +322,7 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
     tune64 = autotune_on(h)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, batch=0)
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, batch=batch)
     torch.cuda.synchronize()
     t_prep = time.perf_counter() - t0
     s = d.run()
@@ -544,7 +548,7 @@ def gpu_arm(a, world, rank, local):
     conv = None
     if not a.no_converge and rank == 0:
         conv = converge_compare(a.tiles, FREQS, lambda h: [h.load_G(f, G, None) for f, G in enumerate(Gs)], a.seed,
-                                local)
+                                local, batch=a.batch)
     del Gs
     grp = group_bench(a, local) if (not a.no_group and rank == 0) else None
     if rank != 0:

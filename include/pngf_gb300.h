@@ -265,7 +265,7 @@ typedef struct pngf_tune {
   int batch;                         /* candidates in the timed batch (every tile once) */
   int update_form;                   /* chosen complex64 update tile form for accepts (entry 0 or 1) */
   int update_forms;                  /* complex64: 4 entries, the two tile widths timed at the accept rank
-                                        (min(k_max, 24)), then at the build chunk's rank (48); the widths
+                                        (min(k_max, 24)), then at the build chunk's rank (96); the widths
                                         chosen for each rank class are kept by the handle */
   int update_cols[PNGF_TUNE_MAX];    /* FP32 output columns per update tile */
   double update_us[PNGF_TUNE_MAX];   /* device time of one rank-update; -1 = not timed */
@@ -292,7 +292,8 @@ typedef struct pngf_dbs_params {
   int seed;       /* MagicHat rng_seed (magichat.hpp:53-75); 0 is rejected */
   int run_index;
   long max_evals; /* stop after this many evaluations; 0 = run to convergence */
-  int batch;      /* speculative candidates per launch (0 = whole remaining hat) */
+  int batch;      /* speculative candidates per launch: > 0 fixed; 0 = the whole remaining hat; < 0 adaptive,
+                     -batch draws after an accept, doubling after each batch without an accept */
   int drift_every;   /* PNGF_PREC_C64: drift check every this many accepts (0 = never) */
   double drift_tol;  /* ... and rebuild M from G in FP64 when the drift exceeds this */
 } pngf_dbs_params;

@@ -89,6 +89,7 @@ struct pngf_dbs {
   // the batch being evaluated: hat state at its start, its draws, staging
   Hat pend_hat{1, 1};
   int pend_last = -1;
+  int adapt_B = 0;  // adaptive batch size (batch < 0)
   std::vector<Cand> pend;
   bool pend_exhausted = false;
   std::vector<int> tiles, nflip;
@@ -263,7 +264,10 @@ int batch_draw(pngf_dbs *d, bool *have) {
   }
   d->pend_hat = d->hat;
   d->pend_last = d->last_tried;
-  int B = d->p.batch > 0 ? d->p.batch : std::max(1, d->hat.left());
+  // batch > 0: fixed; 0: the whole remaining hat; < 0: adaptive, -batch draws
+  // after an accept, doubling after every batch without one
+  if (d->p.batch < 0 && d->adapt_B <= 0) d->adapt_B = -d->p.batch;
+  int B = d->p.batch > 0 ? d->p.batch : d->p.batch < 0 ? d->adapt_B : std::max(1, d->hat.left());
   B = (int)std::min<long>(B, budget);
   d->pend.clear();
   d->pend_exhausted = false;
@@ -337,8 +341,10 @@ int batch_finish(pngf_dbs *d, int *accepted, bool sync_accept) {
     }
     d->hat.reset();
     if (accepted) *accepted = 1;
+    d->adapt_B = -d->p.batch;
     return drift_after_accept(d);
   }
+  if (d->p.batch < 0) d->adapt_B = (int)std::min<long>(2L * d->adapt_B, 1L << 20);
   if (d->pend_exhausted) d->converged = d->done = true;
   return PNGF_OK;
 }

@@ -19,7 +19,7 @@ constexpr int kInitChunk = 96;
 // Edges per chunk when a complex64 state is built directly in complex64: the
 // factor and W solve cost O(k^3) and O(k^2 N) in FP64, the tensor-core update
 // O(1) passes over T, so mid-sized chunks are cheapest.
-constexpr int kC64BuildChunk = 48;
+constexpr int kC64BuildChunk = 96;
 // Largest pending rank of deferred complex64 updates.
 constexpr int kMaxDeferRank = 256;
 constexpr int kAccTuneRank = 24;  // updates of rank <= this use c64_cols, larger ones c64_cols_build

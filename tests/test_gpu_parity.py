@@ -51,9 +51,11 @@ def test_dbs_matches_reference(name, cases, built_lib):
     compare_log(d, h, golden_log(name), s)
 
 
-@pytest.mark.parametrize("batch", [1, 5])
+@pytest.mark.parametrize("batch", [1, 5, -2, -16])
 def test_dbs_batch_size_does_not_change_sequence(batch, cases, built_lib):
-    """Speculative batches of any size replay the hat to the reference's order."""
+    """Speculative batches of any size replay the hat to the reference's order
+    (negative: adaptive, |batch| draws after an accept, doubling after each
+    batch without one)."""
     c = cases["single_7x7_f2_seed1"]
     Gs, gobj = case_G(c, built_lib)
     h, d, s = gpu_dbs(c, Gs, gobj, batch=batch)
