@@ -499,7 +499,7 @@ def c5_run(a, local):
     torch.cuda.set_device(local)
     t0 = time.perf_counter()
     out = converge_compare(41, FREQS_C5, lambda h: [h.load_G_synth(f, seed=1) for f in range(len(FREQS_C5))],
-                           a.seed, local, train_evals=3000, train_steps=1000)
+                           a.seed, local, train_evals=3000, train_steps=1000, batch=a.batch)
     print(json.dumps({"metric": "wall time to converged objective, 41x41 tiles x 4 frequencies, proposal + "
                                 "complex64 vs plain FP64", "c5": out, "total_s": time.perf_counter() - t0}),
           flush=True)
@@ -623,7 +623,9 @@ def gpu_arm(a, world, rank, local):
             "candidates_per_pass": a.tiles * a.tiles if a.mode == "single" else None,
             "precision": "fp64", "parallelism": "one DBS instance per GPU" if world > 1 else "single GPU",
             "l2": "inputs larger than L2: M is %.2f GB per frequency" % ((n + 3) * r64["ldm"] * 16 / 1e9),
-            "step": "one DBS decision (speculative batch of the remaining hat, first improving draw accepted)",
+            "step": "one DBS decision (speculative batches of draws in hat order until the first improving one, "
+                    "which is accepted; batch %s)" % ("adaptive from %d" % -a.batch if a.batch < 0 else
+                                                       "whole remaining hat" if a.batch == 0 else str(a.batch)),
             "value_timing": "sum of CUDA-event spans of the hot-path launch groups on the handle's stream",
         },
         "e2e": {"value": evals_t / wall_m, "unit": "flip_evals/s",
