@@ -269,14 +269,18 @@ typedef struct pngf_tune {
                                         chosen for each rank class are kept by the handle */
   int update_cols[PNGF_TUNE_MAX];    /* FP32 output columns per update tile */
   double update_us[PNGF_TUNE_MAX];   /* device time of one rank-update; -1 = not timed */
+  int eval_form_small;               /* chosen candidate-kernel form for batches of at most 64 candidates */
+  int batch_small;                   /* candidates in the small timed batch (the first 64 of the pass) */
+  double eval_us_small[PNGF_TUNE_MAX]; /* device time of the small batch per form; -1 = form does not apply */
 } pngf_tune;
-/* Times every applicable form of the candidate kernel (and, for
- * PNGF_PREC_C64, of the update tile) at the current design, keeps the fastest
- * for this handle and reports the times. Call after pngf_prepare; the last
- * evaluated batch is discarded and M is left unchanged. */
+/* Times every applicable form of the candidate kernel on a pass over every
+ * tile and on the first 64 candidates of it (and, for PNGF_PREC_C64, the
+ * update forms), keeps the fastest for each batch class for this handle and
+ * reports the times. Call after pngf_prepare; the last evaluated batch is
+ * discarded and M is left unchanged. */
 int pngf_autotune(pngf_handle *h, pngf_tune *out);
-/* Selects a candidate-kernel form by index (PNGF_ERR_UNSUPPORTED if it does
- * not apply to this handle). */
+/* Selects a candidate-kernel form by index for every batch size
+ * (PNGF_ERR_UNSUPPORTED if it does not apply to this handle). */
 int pngf_set_eval_form(pngf_handle *h, int form);
 
 /* ---- DBS driver (host, native): pngf-opt/main.cpp:181-459 ---- */

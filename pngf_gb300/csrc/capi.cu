@@ -1126,7 +1126,7 @@ int pngf_set_eval_form(pngf_handle *ph, int form) {
   Handle *h = H(ph);
   if (!h) return PNGF_ERR_ARG;
   if (!eval_variant_ok(h, form)) return set_error(h, PNGF_ERR_UNSUPPORTED, "candidate-kernel form does not apply");
-  h->eval_variant = form;
+  h->eval_variant = h->eval_variant_small = form;
   return PNGF_OK;
 }
 
@@ -1147,36 +1147,47 @@ int pngf_autotune(pngf_handle *ph, pngf_tune *out) {
     return set_error(h, PNGF_ERR_CUDA, "event creation failed");
   }
   const int reps = 5;
-  double best = 1e300;
-  int bestv = 0;
-  out->eval_forms = kEvalVariants;
-  out->batch = nc;
   const long nl0 = h->nlaunch;
   cudaError_t e = cudaSuccess;
-  for (int v = 0; v < kEvalVariants && e == cudaSuccess; ++v) {
-    out->warps_per_cand[v] = kEvalForms[v].warps_per_cand;
-    out->cands_per_cta[v] = kEvalForms[v].cands_per_cta;
-    out->eval_us[v] = -1.0;
-    if (!eval_variant_ok(h, v)) continue;
-    h->eval_variant = v;
-    if ((e = launch_eval(h, nc, 0.0)) != cudaSuccess) break;  // warm-up
-    cudaEventRecord(a, h->stream);
-    for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_eval(h, nc, 0.0);
-    cudaEventRecord(b, h->stream);
-    if (e == cudaSuccess) e = cudaEventSynchronize(b);
-    float ms = 0.f;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
-    out->eval_us[v] = 1e3 * ms / reps;
-    if (out->eval_us[v] < best) {
-      best = out->eval_us[v];
-      bestv = v;
+  // every form on the whole pass, then on the first kSmallBatch candidates of
+  // it (the batches adaptive and proposal-driven decisions launch)
+  const int nsmall = std::min(nc, kSmallBatch);
+  int bestv[2] = {0, 0};
+  h->eval_variant_small = -1;
+  for (int pass = 0; pass < 2 && e == cudaSuccess; ++pass) {
+    const int nb = pass == 0 ? nc : nsmall;
+    double *us = pass == 0 ? out->eval_us : out->eval_us_small;
+    double best = 1e300;
+    for (int v = 0; v < kEvalVariants && e == cudaSuccess; ++v) {
+      out->warps_per_cand[v] = kEvalForms[v].warps_per_cand;
+      out->cands_per_cta[v] = kEvalForms[v].cands_per_cta;
+      us[v] = -1.0;
+      if (!eval_variant_ok(h, v)) continue;
+      h->eval_variant = h->eval_variant_small = v;
+      if ((e = launch_eval(h, nb, 0.0)) != cudaSuccess) break;  // warm-up
+      cudaEventRecord(a, h->stream);
+      for (int r = 0; r < reps && e == cudaSuccess; ++r) e = launch_eval(h, nb, 0.0);
+      cudaEventRecord(b, h->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(b);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+      us[v] = 1e3 * ms / reps;
+      if (us[v] < best) {
+        best = us[v];
+        bestv[pass] = v;
+      }
     }
   }
+  out->eval_forms = kEvalVariants;
+  out->batch = nc;
+  out->batch_small = nsmall;
   h->nlaunch = nl0;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
-  h->eval_variant = bestv;
-  out->eval_form = bestv;
+  h->eval_variant = bestv[0];
+  h->eval_variant_small = bestv[1];
+  out->eval_form = bestv[0];
+  out->eval_form_small = bestv[1];
   h->batch_valid = false;
   if (e != cudaSuccess) return cuda_check(h, e, "autotune");
   return tune_update(h, out);

@@ -1052,7 +1052,8 @@ bool eval_variant_ok(const Handle *h, int v) {
 }
 
 template <typename TM> static cudaError_t launch_eval_t(Handle *h, int ncand) {
-  switch (eval_variant_ok(h, h->eval_variant) ? h->eval_variant : 0) {
+  const int v = ncand <= kSmallBatch && h->eval_variant_small >= 0 ? h->eval_variant_small : h->eval_variant;
+  switch (eval_variant_ok(h, v) ? v : 0) {
     case 1: return launch_eval_cta<TM, 64>(h, ncand);
     case 2: return launch_eval_cta<TM, 256>(h, ncand);
     case 3: return launch_eval_warp<TM, 2>(h, ncand);

@@ -22,6 +22,7 @@ constexpr int kInitChunk = 96;
 constexpr int kC64BuildChunk = 96;
 // Largest pending rank of deferred complex64 updates.
 constexpr int kMaxDeferRank = 256;
+constexpr int kSmallBatch = 64;  // candidate batches up to this size use the small-batch kernel form
 constexpr int kAccTuneRank = 24;  // updates of rank <= this use c64_cols, larger ones c64_cols_build
 
 // Forms of the candidate kernel the autotuner chooses from: warps working on
@@ -100,6 +101,7 @@ struct Handle {
   bool f64tc = false;                       // FP64 updates of up to f64tc_max_k() edges on tensor cores
   int init_chunk = kInitChunk;
   int eval_variant = 0;                     // index into kEvalForms (set by the autotuner)
+  int eval_variant_small = -1;              // the same for batches of at most kSmallBatch candidates (-1: eval_variant)
   int c64_cols = 128;                       // output tile width of the complex64 update (64 or 128)
   int c64_cols_build = 128;                 // the same for ranks above kAccTuneRank (build chunks, flushes)
   int defer_cap = 0;                        // C64: pending rank at which deferred updates are flushed (0 = off)

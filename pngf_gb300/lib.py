@@ -70,13 +70,16 @@ class Tune(C.Structure):
     _fields_ = [("eval_form", C.c_int), ("eval_forms", C.c_int), ("warps_per_cand", C.c_int * TUNE_MAX),
                 ("cands_per_cta", C.c_int * TUNE_MAX), ("eval_us", C.c_double * TUNE_MAX), ("batch", C.c_int),
                 ("update_form", C.c_int), ("update_forms", C.c_int), ("update_cols", C.c_int * TUNE_MAX),
-                ("update_us", C.c_double * TUNE_MAX)]
+                ("update_us", C.c_double * TUNE_MAX), ("eval_form_small", C.c_int), ("batch_small", C.c_int),
+                ("eval_us_small", C.c_double * TUNE_MAX)]
 
     def as_dict(self):
         ne, nu = self.eval_forms, self.update_forms
         return {"eval_form": self.eval_form, "batch": self.batch,
                 "eval": [{"warps_per_cand": self.warps_per_cand[i], "cands_per_cta": self.cands_per_cta[i],
                           "us": self.eval_us[i]} for i in range(ne)],
+                "eval_form_small": self.eval_form_small, "batch_small": self.batch_small,
+                "eval_small": [{"us": self.eval_us_small[i]} for i in range(ne)],
                 "update_form": self.update_form,
                 "update": [{"cols": self.update_cols[i], "us": self.update_us[i]} for i in range(nu)]}
 

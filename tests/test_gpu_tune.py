@@ -80,6 +80,8 @@ def test_autotune_keeps_state(prec, cases, built_lib):
     assert 0 <= t["eval_form"] < len(t["eval"]) and t["batch"] == a * a
     assert t["eval"][t["eval_form"]]["us"] > 0
     assert all(e["us"] > 0 for e in t["eval"])  # kmax = 24: every form applies
+    assert t["batch_small"] == min(64, a * a) and 0 <= t["eval_form_small"] < len(t["eval_small"])
+    assert all(e["us"] > 0 for e in t["eval_small"])
     if prec == 1:
         # two widths at the accept rank, then the same two at the build chunk's rank
         assert len(t["update"]) == 4 and all(u["us"] > 0 for u in t["update"])
