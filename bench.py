@@ -66,6 +66,8 @@ def parse():
                          "(-batch draws after an accept, doubling after a batch without one), 0 = the whole "
                          "remaining hat, > 0 fixed; every size keeps the reference's evaluation order")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--device-loop", type=int, default=0,
+                    help="1: DBS decisions without an accept run on the device (one CUDA graph with a WHILE node)")
     ap.add_argument("--forms", default="fp64,c64,c64d", help="precision forms to run; the first is the headline")
     ap.add_argument("--nfreq", type=int, default=5, help="use the first NFREQ of the five frequencies")
     ap.add_argument("--no-converge", action="store_true",
@@ -237,7 +239,7 @@ def run_form(a, precision, Gs, rank, local, dist, defer_rank=0):
     for f, G in enumerate(Gs):
         h.load_G(f, G, None)
     d = lib.Dbs(h, mode=lib.DBS_SINGLE if a.mode == "single" else lib.DBS_SYMMETRIC, init=lib.INIT_RANDOM,
-                seed=a.seed + rank, batch=a.batch)
+                seed=a.seed + rank, batch=a.batch, device_loop=bool(a.device_loop))
     tune = h.autotune()  # kernel forms for this instance; the state is left unchanged
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t_setup
@@ -306,7 +308,7 @@ def autotune_on(h, mode_single=True):
 
 
 def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), train_evals=1500, train_steps=600,
-                     topk=64, state_only=0, batch=0):
+                     topk=64, state_only=0, batch=0, device_loop=False):
     """Wall time to the converged objective: plain FP64 DBS (reference order,
     run until the hat is empty) against the proposal + complex64 form, whose
     network is trained only on plain complex64 runs from other seeds. The
@@ -322,7 +324,7 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
     tune64 = autotune_on(h)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, batch=batch)
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, batch=batch, device_loop=device_loop)
     torch.cuda.synchronize()
     t_prep = time.perf_counter() - t0
     s = d.run()
@@ -499,7 +501,8 @@ def c5_run(a, local):
     torch.cuda.set_device(local)
     t0 = time.perf_counter()
     out = converge_compare(41, FREQS_C5, lambda h: [h.load_G_synth(f, seed=1) for f in range(len(FREQS_C5))],
-                           a.seed, local, train_evals=3000, train_steps=1000, batch=a.batch)
+                           a.seed, local, train_evals=3000, train_steps=1000, batch=a.batch,
+                           device_loop=bool(a.device_loop))
     print(json.dumps({"metric": "wall time to converged objective, 41x41 tiles x 4 frequencies, proposal + "
                                 "complex64 vs plain FP64", "c5": out, "total_s": time.perf_counter() - t0}),
           flush=True)
@@ -548,7 +551,7 @@ def gpu_arm(a, world, rank, local):
     conv = None
     if not a.no_converge and rank == 0:
         conv = converge_compare(a.tiles, FREQS, lambda h: [h.load_G(f, G, None) for f, G in enumerate(Gs)], a.seed,
-                                local, batch=a.batch)
+                                local, batch=a.batch, device_loop=bool(a.device_loop))
     del Gs
     grp = group_bench(a, local) if (not a.no_group and rank == 0) else None
     if rank != 0:

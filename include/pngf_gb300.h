@@ -282,6 +282,11 @@ int pngf_autotune(pngf_handle *h, pngf_tune *out);
 /* Selects a candidate-kernel form by index for every batch size
  * (PNGF_ERR_UNSUPPORTED if it does not apply to this handle). */
 int pngf_set_eval_form(pngf_handle *h, int form);
+/* Failure test hook: records `code` in the handle's tensor-core error flag as
+ * if an accept update's bounded wait had given up, without any device wait.
+ * The next call that reads the flag (the next evaluation, or the device
+ * loop's next decision) fails with PNGF_ERR_TIMEOUT and clears it. */
+int pngf_inject_update_timeout(pngf_handle *h, int code);
 
 /* ---- DBS driver (host, native): pngf-opt/main.cpp:181-459 ---- */
 
@@ -315,6 +320,8 @@ typedef struct pngf_dbs_stats {
   double drift_max;    /* largest drift seen, max |T_c64 - T| / max |T| */
   long prop_hits;      /* proposal steps whose top-k batch held an improving flip */
   long full_passes;    /* proposal steps that fell back to a full exact pass */
+  long device_launches;   /* launches of the device-resident decision loop */
+  long device_decisions;  /* decisions it took (each a batch evaluated and decided on the GPU) */
 } pngf_dbs_stats;
 
 /* Draws the initial design (rand_binary per tile, main.cpp:187-208), forces
@@ -324,6 +331,17 @@ int pngf_dbs_begin(pngf_handle *h, const pngf_dbs_params *p, pngf_dbs **out);
 /* One DBS decision: evaluate draws in hat order until the first improving
  * flip (accepting it, main.cpp:429-456) or until the hat is empty. */
 int pngf_dbs_step(pngf_dbs *d, int *accepted);
+/* Device-resident decisions (no reference counterpart): the hat's random
+ * stream (std::mt19937 with std::uniform_int_distribution, restated for the
+ * device and checked here against this C++ library's) lives on the GPU, and
+ * one CUDA graph with a WHILE node draws, evaluates and decides batch after
+ * batch without returning to the host until an accept, the end of the run,
+ * or 1024 decisions; accepts then run on the host path. Flips, objectives and
+ * log equal those of the host driver. Call before the first pngf_dbs_step;
+ * not with learned proposals or in a group. enable = 0 turns it off again
+ * (before the first step). PNGF_ERR_UNSUPPORTED when the library's stream
+ * differs from the restatement. */
+int pngf_dbs_set_device_loop(pngf_dbs *d, int enable);
 int pngf_dbs_stats_get(const pngf_dbs *d, pngf_dbs_stats *out);
 /* Log of every evaluation in reference order (Logger::record_flip,
  * logger.hpp:64-73): tile index tx+ty*tiles_x, accept bit, F, F_best and per

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpngf_gb300.so")
 
-SOURCES = ["kernels_fp64.cu", "kernels_c64.cu", "kernels_f64tc.cu", "capi.cu", "dbs.cpp", "gfile.cpp", "noalloc.cu",
+SOURCES = ["kernels_fp64.cu", "kernels_c64.cu", "kernels_f64tc.cu", "capi.cu", "dbs.cpp", "dbs_device.cu", "gfile.cpp", "noalloc.cu",
            "proposal.cu", "synth.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "-I" + os.path.join(ROOT, "include")]

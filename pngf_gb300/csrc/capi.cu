@@ -92,11 +92,6 @@ static void timing_collect(Handle *h) {
   h->pending.clear();
 }
 
-#define PNGF_CUDA(h, call)                                   \
-  do {                                                       \
-    const int _rc = cuda_check((h), (call), #call);          \
-    if (_rc != PNGF_OK) return _rc;                          \
-  } while (0)
 
 template <typename T> static int dalloc(Handle *h, T **p, size_t count) {
   *p = nullptr;
@@ -171,6 +166,21 @@ static int ensure_cand_cap(Handle *h, int ncand) {
   PNGF_CUDA(h, cudaMallocHost(&h->h_tiles, sizeof(int) * (size_t)cap * h->cfg.max_flips));
   PNGF_CUDA(h, cudaMallocHost(&h->h_nflip, sizeof(int) * (size_t)cap));
   h->cand_cap = cap;
+  return PNGF_OK;
+}
+
+int reserve_candidates(Handle *h, int ncand) { return ensure_cand_cap(h, ncand); }
+
+int adopt_device_batch(Handle *h, int ncand, int c, const int *tiles_c, int nflip_c) {
+  if (c < 0 || c >= ncand || ncand > h->cand_cap || nflip_c < 0 || nflip_c > h->cfg.max_flips)
+    return set_error(h, PNGF_ERR_STATE, "device batch out of range");
+  const int mf = h->cfg.max_flips;
+  h->batch_tiles.assign((size_t)ncand * mf, 0);
+  h->batch_nflip.assign(ncand, 0);
+  for (int i = 0; i < nflip_c; ++i) h->batch_tiles[(size_t)c * mf + i] = tiles_c[i];
+  h->batch_nflip[c] = nflip_c;
+  h->batch_n = ncand;
+  h->batch_valid = true;
   return PNGF_OK;
 }
 
@@ -1121,6 +1131,14 @@ static int tune_update(Handle *h, pngf_tune *out) {
 }
 
 extern "C" {
+
+int pngf_inject_update_timeout(pngf_handle *ph, int code) {
+  Handle *h = H(ph);
+  if (!h || code == 0) return PNGF_ERR_ARG;
+  PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
+  PNGF_CUDA(h, cudaMemcpy(h->d_tc_err, &code, sizeof(int), cudaMemcpyHostToDevice));
+  return PNGF_OK;
+}
 
 int pngf_set_eval_form(pngf_handle *ph, int form) {
   Handle *h = H(ph);

@@ -12,7 +12,9 @@
 //
 // MagicHat (pngf-opt/magichat.hpp:32-111) uses std::mt19937 and
 // std::uniform_int_distribution<>; its draws depend on the C++ library, so
-// this driver stays in C++ and uses the same two standard components.
+// this driver stays in C++ and uses the same two standard components. The
+// device-resident form of the loop (dbs_device.cu, pngf_dbs_set_device_loop)
+// restates them (hat_rng.h) and is checked against them before it starts.
 #include <algorithm>
 #include <cstdio>
 #include <fstream>
@@ -33,7 +35,25 @@ class Hat {
     dis_ = std::uniform_int_distribution<>(0, entries - 1);
     for (int i = 0; i < entries; ++i) entry_[i] = i;
   }
-  int rand_binary() { return gen_() & 1; }
+  int rand_binary() {
+    ++binary_draws_;
+    return gen_() & 1;
+  }
+  long binary_draws() const { return binary_draws_; }
+  // Whether the restated stream m (hat_rng.h), taken to this hat's engine
+  // state, reproduces its bounded draws over every range a hat uses.
+  bool restated_matches(const pngf::MtState &m0) const {
+    std::mt19937 g = gen_;
+    std::uniform_int_distribution<> d;
+    pngf::MtState m = m0;
+    int used = 0;
+    for (int i = 0; i < 4096; ++i) {
+      const int range = 1 + (int)((i * 7919L) % total_);
+      d.param(std::uniform_int_distribution<int>::param_type(0, range - 1));
+      if (d(g) != (int)pngf::mt_below(&m, (uint32_t)range, &used)) return false;
+    }
+    return true;
+  }
   int draw() {
     if (left_ <= 0) return -1;
     dis_.param(std::uniform_int_distribution<int>::param_type(0, left_ - 1));
@@ -51,6 +71,7 @@ class Hat {
 
  private:
   int total_, left_;
+  long binary_draws_ = 0;
   std::vector<int> entry_;
   std::mt19937 gen_;
   std::uniform_int_distribution<> dis_;
@@ -93,6 +114,9 @@ struct pngf_dbs {
   std::vector<Cand> pend;
   bool pend_exhausted = false;
   std::vector<int> tiles, nflip;
+  // device-resident decisions (pngf_dbs_set_device_loop)
+  pngf::DevLoop *dev = nullptr;
+  long dev_launches = 0, dev_decisions = 0;
 };
 
 extern "C" {
@@ -104,46 +128,18 @@ long pngf_prop_num_samples(const pngf_prop *p);
 
 namespace {
 
+pngf::HatGeom hat_geom(const pngf_dbs *d) {
+  return pngf::HatGeom{d->h->cfg.tiles_x, d->h->cfg.tiles_y, d->qx, d->mid_x, d->mid_y,
+                       d->p.mode == PNGF_DBS_SYMMETRIC ? 1 : 0};
+}
+
 // Draws the next valid candidate (main.cpp:343-392); false when the hat is empty.
 bool next_candidate(pngf_dbs *d, Cand *c) {
-  const int xsz = d->h->cfg.tiles_x, ysz = d->h->cfg.tiles_y;
-  const bool sym = d->p.mode == PNGF_DBS_SYMMETRIC;
+  const pngf::HatGeom g = hat_geom(d);
   while (true) {
     const int r = d->hat.draw();
     if (r < 0) return false;
-    int tx, ty;
-    if (sym) {
-      ty = r / d->qx;
-      tx = r - ty * d->qx;
-    } else {
-      ty = r / xsz;
-      tx = r - ty * xsz;
-    }
-    if (r == d->last_tried) continue;
-    if (tx == d->mid_x && ty == d->mid_y) continue;      // source tile
-    if (tx == d->mid_x - 1 && ty == d->mid_y) continue;  // metal next to the source
-    if (!sym && tx == d->mid_x + 1 && ty == d->mid_y) continue;
-    d->last_tried = r;
-    c->log_index = tx + ty * xsz;
-    if (!sym) {
-      c->nflip = 1;
-      c->tiles[0] = tx + ty * xsz;
-    } else if (tx == d->mid_x) {
-      c->nflip = 2;
-      c->tiles[0] = tx + ty * xsz;
-      c->tiles[1] = tx + ((ysz - 1) - ty) * xsz;
-    } else if (ty == d->mid_y) {
-      c->nflip = 2;
-      c->tiles[0] = tx + ty * xsz;
-      c->tiles[1] = ((xsz - 1) - tx) + ty * xsz;
-    } else {
-      c->nflip = 4;
-      c->tiles[0] = tx + ty * xsz;
-      c->tiles[1] = ((xsz - 1) - tx) + ty * xsz;
-      c->tiles[2] = tx + ((ysz - 1) - ty) * xsz;
-      c->tiles[3] = ((xsz - 1) - tx) + ((ysz - 1) - ty) * xsz;
-    }
-    return true;
+    if (pngf::hat_candidate(g, r, &d->last_tried, &c->log_index, &c->nflip, c->tiles)) return true;
   }
 }
 
@@ -349,15 +345,84 @@ int batch_finish(pngf_dbs *d, int *accepted, bool sync_accept) {
   return PNGF_OK;
 }
 
+// One DBS decision on the device-resident loop: decisions without an accept
+// run on the GPU; an accept is performed here as on the host path.
+int device_step(pngf_dbs *d, int *accepted) {
+  pngf::Handle *h = d->h;
+  pngf::DevLoopLog lg{d->lg_tile, d->lg_acc, d->lg_F, d->lg_Fb, d->lg_perf};
+  while (!d->done) {
+    pngf::DevLoopResult r{};
+    int rc = pngf::devloop_run(h, d->dev, &r, &lg);
+    if (rc) return rc;
+    d->evals = r.evals;
+    d->accepts = r.accepts;
+    d->launched = r.launched;
+    d->F_best = r.F_best;
+    d->converged = r.converged != 0;
+    d->done = r.done != 0;
+    ++d->dev_launches;
+    d->dev_decisions += r.decisions;
+    if (r.err == 2) {
+      d->done = true;
+      cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->stream);
+      return pngf::set_error(h, PNGF_ERR_TIMEOUT,
+                             "tensor-core update gave up waiting (code " + std::to_string(r.tc_code) + ")");
+    }
+    if (r.err) {
+      d->done = true;
+      return pngf::set_error(h, PNGF_ERR_ARG, "invalid candidate produced by the driver");
+    }
+    if (r.accepted) {
+      // not waited for: the next launch's decide kernel reads the tensor-core
+      // error flag before it decides
+      if ((rc = pngf::adopt_device_batch(h, r.nc, r.j, r.tiles, r.nflip)) ||
+          (rc = pngf::accept_cand_async(h, r.j, r.k, false)))
+        return rc;
+      if (accepted) *accepted = 1;
+      const double fb = d->F_best;
+      if ((rc = drift_after_accept(d))) return rc;
+      if (!(d->F_best == fb) && (rc = pngf::devloop_set_fbest(h, d->dev, d->F_best))) return rc;
+      return PNGF_OK;
+    }
+  }
+  return PNGF_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int pngf_dbs_set_device_loop(pngf_dbs *d, int enable) {
+  if (!d) return PNGF_ERR_ARG;
+  pngf::Handle *h = d->h;
+  if (d->evals > 0 || d->launched > 0 || d->done)
+    return pngf::set_error(h, PNGF_ERR_STATE, "the device loop is chosen before the first step");
+  if (!enable) {
+    pngf::devloop_destroy(d->dev);
+    d->dev = nullptr;
+    return PNGF_OK;
+  }
+  if (d->dev) return PNGF_OK;
+  if (d->prop)
+    return pngf::set_error(h, PNGF_ERR_UNSUPPORTED, "learned proposals run on the host driver");
+  pngf::MtState m;
+  pngf::mt_seed(&m, (uint32_t)d->p.seed);
+  for (long i = 0; i < d->hat.binary_draws(); ++i) pngf::mt_next(&m);
+  if (!d->hat.restated_matches(m))
+    return pngf::set_error(h, PNGF_ERR_UNSUPPORTED,
+                           "this C++ library's MagicHat stream differs from the device restatement");
+  pngf::DevLoopConfig cfg{hat_geom(d), d->hat_entries, d->p.batch, d->p.max_evals, (unsigned)d->p.seed,
+                          d->hat.binary_draws(), d->F_best};
+  return pngf::devloop_create(h, cfg, &d->dev);
+}
 
 int pngf_dbs_set_proposal(pngf_dbs *d, pngf_prop *p, int topk, int train_every, int train_steps, int train_batch,
                           float lr) {
   if (!d) return PNGF_ERR_ARG;
   if (p && d->p.mode != PNGF_DBS_SINGLE)
     return pngf::set_error(d->h, PNGF_ERR_UNSUPPORTED, "proposals apply to single-tile candidates");
+  if (p && d->dev)
+    return pngf::set_error(d->h, PNGF_ERR_UNSUPPORTED, "learned proposals run on the host driver");
   d->prop = p;
   d->topk = topk;
   d->train_every = train_every;
@@ -427,6 +492,7 @@ int pngf_dbs_step(pngf_dbs *d, int *accepted) {
   if (!d) return PNGF_ERR_ARG;
   if (accepted) *accepted = 0;
   if (d->prop && d->topk > 0) return d->done ? PNGF_OK : proposal_step(d, accepted);
+  if (d->dev) return device_step(d, accepted);
   while (!d->done) {
     bool have = false;
     int rc = batch_draw(d, &have);
@@ -455,6 +521,8 @@ int pngf_dbs_stats_get(const pngf_dbs *d, pngf_dbs_stats *out) {
   out->drift_max = d->drift_max;
   out->prop_hits = d->prop_hits;
   out->full_passes = d->full_passes;
+  out->device_launches = d->dev_launches;
+  out->device_decisions = d->dev_decisions;
   return PNGF_OK;
 }
 
@@ -500,6 +568,7 @@ int pngf_dbs_save_log(const pngf_dbs *d, const char *path) {
 }
 
 int pngf_dbs_end(pngf_dbs *d) {
+  if (d) pngf::devloop_destroy(d->dev);
   delete d;
   return PNGF_OK;
 }
@@ -598,6 +667,8 @@ int pngf_group_create(pngf_dbs *const *members, int count, int use_graphs, pngf_
     if (!members[i]) return PNGF_ERR_ARG;
     if (members[i]->prop && members[i]->topk > 0)
       return pngf::set_error(members[i]->h, PNGF_ERR_UNSUPPORTED, "proposal-driven runs are stepped on their own");
+    if (members[i]->dev)
+      return pngf::set_error(members[i]->h, PNGF_ERR_UNSUPPORTED, "device-loop runs are stepped on their own");
     for (int j = 0; j < i; ++j)
       if (members[j]->h == members[i]->h)
         return pngf::set_error(members[i]->h, PNGF_ERR_ARG, "two group members share a handle");

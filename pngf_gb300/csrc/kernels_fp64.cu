@@ -225,7 +225,7 @@ __device__ __forceinline__ int flipped_parity(const int *tl, int nf, int t) {
 
 // One warp per candidate. Output: es[c*kmax + q], ed[...], ek[c]; ek = -1 on
 // an invalid tile index or flip count.
-__global__ void k_edge_lists(Geo g, int ncand, const int *__restrict__ tiles, const int *__restrict__ nflip,
+__global__ void k_edge_lists(Geo g, int ncand, Gate gt, const int *__restrict__ tiles, const int *__restrict__ nflip,
                              const int *__restrict__ tile_map, const signed char *__restrict__ P,
                              int *__restrict__ es, signed char *__restrict__ ed, int *__restrict__ ek) {
   extern __shared__ int sh[];
@@ -235,7 +235,7 @@ __global__ void k_edge_lists(Geo g, int ncand, const int *__restrict__ tiles, co
   const int slots = g.max_flips * ((g.cells_x) * (g.cells_y + 1) + (g.cells_x + 1) * g.cells_y);
   int *cg = sh + w * 2 * slots;          // candidate edge index per slot (-1 = none)
   int *cd = cg + slots;                  // sign per slot
-  if (c >= ncand) return;
+  if (!gt.open(&ncand) || c >= ncand) return;
   const int nfl = nflip[c];
   const int *tl = tiles + (size_t)c * g.max_flips;
   bool bad = nfl < 0 || nfl > g.max_flips;
@@ -443,9 +443,12 @@ __global__ void __launch_bounds__(NT) k_eval(const SV<TM> *__restrict__ Ms, cons
                                               const signed char *__restrict__ ed, const int *__restrict__ ek,
                                               const FreqConst *__restrict__ fconst, ObjConst oc, int nf,
                                               double2 *__restrict__ new_eobj, double *__restrict__ Ff,
-                                              double *__restrict__ perf, int *__restrict__ status, LuOut lo) {
+                                              double *__restrict__ perf, int *__restrict__ status, LuOut lo,
+                                              Gate gt) {
   extern __shared__ double2 smem[];
   const int c = blockIdx.x, f = blockIdx.y;
+  int ncand = gridDim.x;
+  if (!gt.open(&ncand) || c >= ncand) return;
   const int tid = threadIdx.x;
   const int ld = kmax;  // K is kmax x kmax
   double2 *K = smem;
@@ -522,11 +525,11 @@ __global__ void __launch_bounds__(32 * WPC)
                 int ncand, const int *__restrict__ es, const signed char *__restrict__ ed,
                 const int *__restrict__ ek, const FreqConst *__restrict__ fconst, ObjConst oc, int nf,
                 double2 *__restrict__ new_eobj, double *__restrict__ Ff, double *__restrict__ perf,
-                int *__restrict__ status, LuOut lo) {
+                int *__restrict__ status, LuOut lo, Gate gt) {
   extern __shared__ double2 smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * WPC + warp, f = blockIdx.y;
-  if (c >= ncand) return;
+  if (!gt.open(&ncand) || c >= ncand) return;
   const int ld = kmax | 1;
   double2 *K = smem + (size_t)warp * ld * kmax;
   const SV<TM> M = Ms[f];
@@ -1007,13 +1010,14 @@ cudaError_t launch_init_M(Handle *h, int f) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const int *d_nflip) {
+cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const int *d_nflip, Gate gt) {
   const Geo g = make_geo(h);
   const int slots = g.max_flips * ((g.cells_x) * (g.cells_y + 1) + (g.cells_x + 1) * g.cells_y);
   const int warps = 4;
   const size_t sm = sizeof(int) * 2 * slots * warps;
-  k_edge_lists<<<(ncand + warps - 1) / warps, 32 * warps, sm, h->stream>>>(g, ncand, d_tiles, d_nflip, h->d_tile_map,
-                                                                          h->d_P, h->d_es, h->d_ed, h->d_ek);
+  k_edge_lists<<<(ncand + warps - 1) / warps, 32 * warps, sm, h->stream>>>(g, ncand, gt, d_tiles, d_nflip,
+                                                                          h->d_tile_map, h->d_P, h->d_es, h->d_ed,
+                                                                          h->d_ek);
   h->nlaunch += 1;
   return cudaGetLastError();
 }
@@ -1022,7 +1026,7 @@ static size_t eval_smem(int kmax) {
   return sizeof(double2) * ((size_t)kmax * kmax + 2 * kmax) + sizeof(int) * kmax + kmax + 16;
 }
 
-template <typename TM, int NT> static cudaError_t launch_eval_cta(Handle *h, int ncand) {
+template <typename TM, int NT> static cudaError_t launch_eval_cta(Handle *h, int ncand, Gate gt) {
   const int nf = h->cfg.num_freq;
   const size_t sm = eval_smem(h->kmax);
   cudaError_t e = cudaFuncSetAttribute(k_eval<TM, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -1030,11 +1034,11 @@ template <typename TM, int NT> static cudaError_t launch_eval_cta(Handle *h, int
   k_eval<TM, NT><<<dim3(ncand, nf), NT, sm, h->stream>>>(
       static_cast<const SV<TM> *>(h->d_views), reinterpret_cast<const double2 *const *>(h->d_Eincs), h->n, h->E,
       h->kmax, h->d_es, h->d_ed, h->d_ek, h->d_fconst, obj_const(h), nf, h->d_new_eobj, h->d_Ff, h->d_perf,
-      h->d_status, LuOut{h->d_eval_LU, h->d_eval_piv, h->d_eval_z});
+      h->d_status, LuOut{h->d_eval_LU, h->d_eval_piv, h->d_eval_z}, gt);
   return cudaGetLastError();
 }
 
-template <typename TM, int WPC> static cudaError_t launch_eval_warp(Handle *h, int ncand) {
+template <typename TM, int WPC> static cudaError_t launch_eval_warp(Handle *h, int ncand, Gate gt) {
   const int nf = h->cfg.num_freq;
   const size_t sm = sizeof(double2) * (size_t)WPC * (h->kmax | 1) * h->kmax;
   cudaError_t e = cudaFuncSetAttribute(k_eval_warp<TM, WPC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -1042,7 +1046,7 @@ template <typename TM, int WPC> static cudaError_t launch_eval_warp(Handle *h, i
   k_eval_warp<TM, WPC><<<dim3((ncand + WPC - 1) / WPC, nf), 32 * WPC, sm, h->stream>>>(
       static_cast<const SV<TM> *>(h->d_views), reinterpret_cast<const double2 *const *>(h->d_Eincs), h->n, h->E,
       h->kmax, ncand, h->d_es, h->d_ed, h->d_ek, h->d_fconst, obj_const(h), nf, h->d_new_eobj, h->d_Ff, h->d_perf,
-      h->d_status, LuOut{h->d_eval_LU, h->d_eval_piv, h->d_eval_z});
+      h->d_status, LuOut{h->d_eval_LU, h->d_eval_piv, h->d_eval_z}, gt);
   return cudaGetLastError();
 }
 
@@ -1051,24 +1055,28 @@ bool eval_variant_ok(const Handle *h, int v) {
   return kEvalForms[v].cands_per_cta == 1 || h->kmax <= 32;
 }
 
-template <typename TM> static cudaError_t launch_eval_t(Handle *h, int ncand) {
-  const int v = ncand <= kSmallBatch && h->eval_variant_small >= 0 ? h->eval_variant_small : h->eval_variant;
+template <typename TM> static cudaError_t launch_eval_t(Handle *h, int v, int ncand, Gate gt) {
   switch (eval_variant_ok(h, v) ? v : 0) {
-    case 1: return launch_eval_cta<TM, 64>(h, ncand);
-    case 2: return launch_eval_cta<TM, 256>(h, ncand);
-    case 3: return launch_eval_warp<TM, 2>(h, ncand);
-    case 4: return launch_eval_warp<TM, 4>(h, ncand);
-    case 5: return launch_eval_warp<TM, 8>(h, ncand);
-    default: return launch_eval_cta<TM, 128>(h, ncand);
+    case 1: return launch_eval_cta<TM, 64>(h, ncand, gt);
+    case 2: return launch_eval_cta<TM, 256>(h, ncand, gt);
+    case 3: return launch_eval_warp<TM, 2>(h, ncand, gt);
+    case 4: return launch_eval_warp<TM, 4>(h, ncand, gt);
+    case 5: return launch_eval_warp<TM, 8>(h, ncand, gt);
+    default: return launch_eval_cta<TM, 128>(h, ncand, gt);
   }
 }
 
+cudaError_t launch_eval_form(Handle *h, int form, int ncand, Gate gt) {
+  const cudaError_t e = h->cfg.precision == PNGF_PREC_FP64 ? launch_eval_t<double2>(h, form, ncand, gt)
+                                                           : launch_eval_t<float2>(h, form, ncand, gt);
+  h->nlaunch += 1;
+  return e;
+}
+
 cudaError_t launch_eval(Handle *h, int ncand, double F_best, const double *d_fbest) {
-  cudaError_t e;
-  if (h->cfg.precision == PNGF_PREC_FP64)
-    e = launch_eval_t<double2>(h, ncand);
-  else
-    e = launch_eval_t<float2>(h, ncand);
+  const int v = ncand <= kSmallBatch && h->eval_variant_small >= 0 ? h->eval_variant_small : h->eval_variant;
+  cudaError_t e = h->cfg.precision == PNGF_PREC_FP64 ? launch_eval_t<double2>(h, v, ncand, Gate{})
+                                                     : launch_eval_t<float2>(h, v, ncand, Gate{});
   if (e != cudaSuccess) return e;
   k_score<<<1, 256, 0, h->stream>>>(ncand, h->cfg.num_freq, h->d_Ff, F_best, d_fbest, h->d_F, h->d_first);
   h->nlaunch += 2;

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/pngf_gb300.h"
+#include "hat_rng.h"
 
 namespace pngf {
 
@@ -32,6 +33,24 @@ struct EvalForm {
 };
 constexpr int kEvalVariants = 6;
 constexpr EvalForm kEvalForms[kEvalVariants] = {{4, 1}, {2, 1}, {8, 1}, {1, 2}, {1, 4}, {1, 8}};
+
+// Batch gate of the edge-list and candidate kernels. With nc set, the batch
+// size is read from *nc on the device (the launch grid covers the largest
+// batch) and the launch does nothing unless lo < *nc <= hi: a CUDA graph can
+// then replay one launch per kernel form for whatever batch the device drew.
+struct Gate {
+  const int *nc = nullptr;
+  int lo = 0, hi = 0;
+#ifdef __CUDACC__
+  __device__ __forceinline__ bool open(int *ncand) const {
+    if (!nc) return true;
+    const int n = *nc;
+    if (n <= lo || n > hi) return false;
+    *ncand = n;
+    return true;
+  }
+#endif
+};
 
 struct FreqConst {   // per-frequency scalars used by the objective
   double2 vinc, ln1, ln2;
@@ -189,6 +208,12 @@ void timing_close(Handle *h, cudaEvent_t start, int cat, double x1, double x2, d
 
 int set_error(Handle *h, int code, const std::string &msg);
 int cuda_check(Handle *h, cudaError_t e, const char *what);
+// Returns the library status of a failed CUDA call from the enclosing function.
+#define PNGF_CUDA(h, call)                          \
+  do {                                              \
+    const int _rc = cuda_check((h), (call), #call); \
+    if (_rc != PNGF_OK) return _rc;                 \
+  } while (0)
 
 // Host copy of one evaluated batch.
 struct EvalOut {
@@ -217,15 +242,56 @@ int accept_cand(Handle *h, int c, int k);
 // error flag is then reported by the next eval_collect).
 int accept_cand_async(Handle *h, int c, int k, bool check_now);
 
+// Makes room for batches of ncand candidates (device buffers only).
+int reserve_candidates(Handle *h, int ncand);
+// Marks the batch the device-resident loop evaluated (ncand candidates, left
+// in the handle's device buffers) as the evaluated batch, so that candidate
+// c (its tiles given for the host copy of the design) can be accepted.
+int adopt_device_batch(Handle *h, int ncand, int c, const int *tiles_c, int nflip_c);
+
+// ---- device-resident DBS decisions (dbs_device.cu) ----
+struct DevLoopConfig {
+  HatGeom geo;
+  int hat_entries;
+  int batch;             // pngf_dbs_params.batch
+  long long max_evals;   // 0 = no budget
+  unsigned seed;         // MagicHat seed
+  long engine_used;      // engine outputs pngf_dbs_begin consumed (rand_binary)
+  double F_best;
+};
+struct DevLoopResult {
+  long long evals, accepts, launched;
+  double F_best;
+  int converged, done;
+  int err;      // 1: an invalid candidate; 2: a tensor-core accept update gave up waiting (tc_code)
+  int tc_code;
+  int accepted, nc, j, k, nflip, tiles[4];  // the accept the host is to perform
+  int decisions;                             // decisions taken by this launch
+};
+struct DevLoopLog {  // rows appended by devloop_run
+  std::vector<int> &tile, &acc;
+  std::vector<double> &F, &Fb, &perf;
+};
+struct DevLoop;
+int devloop_create(Handle *h, const DevLoopConfig &cfg, DevLoop **out);
+// Runs decisions on the device until an accept, the end of the run or a
+// launch limit; appends the log rows and reports the state.
+int devloop_run(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log);
+// New F_best after the host changed it (drift refresh).
+int devloop_set_fbest(Handle *h, DevLoop *L, double F_best);
+void devloop_destroy(DevLoop *L);
+
 // ---- kernels (kernels_fp64.cu) ----
 // Builds M for P = 0 from G and the objective rows; computes Einc and the
 // port constants (on the frequency's lane stream).
 cudaError_t launch_init_M(Handle *h, int f);
 // Per-candidate flipped-edge lists (sorted, deduplicated) from tile lists.
-cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const int *d_nflip);
+cudaError_t launch_edge_lists(Handle *h, int ncand, const int *d_tiles, const int *d_nflip, Gate gt = Gate{});
 // Candidate evaluation + objective at every frequency, then the score
 // against F_best (read from d_fbest when it is not null).
 cudaError_t launch_eval(Handle *h, int ncand, double F_best, const double *d_fbest = nullptr);
+// The candidate kernel alone in form kEvalForms[form], gated (no score).
+cudaError_t launch_eval_form(Handle *h, int form, int ncand, Gate gt);
 // Whether kEvalForms[v] applies to the handle (warp forms need kmax <= 32).
 bool eval_variant_ok(const Handle *h, int v);
 // Objective of the current design (from M's Eobj entries) into d_F[0].

@@ -52,7 +52,7 @@ class DbsStats(C.Structure):
     _fields_ = [("evals", C.c_long), ("accepts", C.c_long), ("launched", C.c_long), ("converged", C.c_int),
                 ("F_init", C.c_double), ("F_best", C.c_double), ("drift_checks", C.c_long),
                 ("refreshes", C.c_long), ("drift_max", C.c_double), ("prop_hits", C.c_long),
-                ("full_passes", C.c_long)]
+                ("full_passes", C.c_long), ("device_launches", C.c_long), ("device_decisions", C.c_long)]
 
 
 class Timing(C.Structure):
@@ -130,6 +130,8 @@ def load():
         "pngf_timing_get": (I, [P, P]),
         "pngf_dbs_begin": (I, [P, P, P]),
         "pngf_dbs_step": (I, [P, P]),
+        "pngf_dbs_set_device_loop": (I, [P, I]),
+        "pngf_inject_update_timeout": (I, [P, I]),
         "pngf_dbs_stats_get": (I, [P, P]),
         "pngf_dbs_log": (I, [P, L_, P, P, P, P, P, P]),
         "pngf_dbs_save_log": (I, [P, C.c_char_p]),
@@ -338,18 +340,28 @@ class Handle:
     def set_eval_form(self, form):
         self._chk(self.L.pngf_set_eval_form(self.h, form), "pngf_set_eval_form")
 
+    def inject_update_timeout(self, code=21):
+        """Failure test hook: the tensor-core error flag as a timed-out update leaves it."""
+        self._chk(self.L.pngf_inject_update_timeout(self.h, code), "pngf_inject_update_timeout")
+
 
 class Dbs:
     """The native DBS driver over a prepared-able handle (G loaded)."""
 
     def __init__(self, handle: Handle, mode=DBS_SYMMETRIC, init=INIT_RANDOM, seed=1, max_evals=0, batch=0,
-                 run_index=0, drift_every=0, drift_tol=0.0):
+                 run_index=0, drift_every=0, drift_tol=0.0, device_loop=False):
         self.hd = handle
         self.max_evals = max_evals
         p = DbsParams(mode, init, seed, run_index, max_evals, batch, drift_every, drift_tol)
         d = C.c_void_p()
         handle._chk(handle.L.pngf_dbs_begin(handle.h, C.byref(p), C.byref(d)), "pngf_dbs_begin")
         self.d = d
+        if device_loop:
+            self.set_device_loop(True)
+
+    def set_device_loop(self, enable=True):
+        """Decisions without an accept run on the GPU (pngf_dbs_set_device_loop)."""
+        self.hd._chk(self.hd.L.pngf_dbs_set_device_loop(self.d, 1 if enable else 0), "pngf_dbs_set_device_loop")
 
     def step(self):
         a = C.c_int()
