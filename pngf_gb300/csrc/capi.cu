@@ -258,6 +258,7 @@ int eval_stage(Handle *h, const int *tiles, const int *nflip, int ncand, double 
 }
 
 int eval_enqueue(Handle *h) {
+  pngf::TraceRange trace_("pngf evaluate");
   const int ncand = h->staged_n, mf = h->cfg.max_flips, nf = h->cfg.num_freq;
   if (ncand <= 0) return set_error(h, PNGF_ERR_STATE, "no staged batch");
   PNGF_CUDA(h, cudaMemcpyAsync(h->d_tiles, h->h_tiles, sizeof(int) * (size_t)ncand * mf, cudaMemcpyHostToDevice,
@@ -333,6 +334,7 @@ int eval_batch(Handle *h, const int *tiles, const int *nflip, int ncand, double 
 int accept_cand(Handle *h, int c, int k) { return accept_cand_async(h, c, k, true); }
 
 int accept_cand_async(Handle *h, int c, int k, bool check_now) {
+  pngf::TraceRange trace_("pngf accept");
   if (!h->batch_valid) return set_error(h, PNGF_ERR_STATE, "no evaluated batch to accept from");
   if (c < 0 || c >= h->batch_n) return set_error(h, PNGF_ERR_ARG, "candidate index outside the last batch");
   if (k < 0 || k > h->kmax) return set_error(h, PNGF_ERR_ARG, "invalid flipped-edge count");
@@ -829,6 +831,7 @@ static int prepare_impl(Handle *h, bool fp64) {
 }
 
 int pngf_prepare(pngf_handle *ph) {
+  pngf::TraceRange trace_("pngf_prepare");
   Handle *h = H(ph);
   if (!h) return PNGF_ERR_ARG;
   return prepare_impl(h, !(h->cfg.precision == PNGF_PREC_C64 && h->cfg.c64_build == PNGF_BUILD_C64));
@@ -890,6 +893,7 @@ int pngf_get_M(pngf_handle *ph, int f, double *M, long ld, double *einc) {
 
 int pngf_eval_candidates(pngf_handle *ph, const int *tiles, const int *nflip, int ncand, double *new_eobj,
                          double *F) {
+  pngf::TraceRange trace_("pngf_eval_candidates");
   Handle *h = H(ph);
   if (!h || !tiles || !nflip) return PNGF_ERR_ARG;
   EvalOut o;
@@ -904,6 +908,7 @@ int pngf_eval_candidates(pngf_handle *ph, const int *tiles, const int *nflip, in
 
 int pngf_eval_candidates_device(pngf_handle *ph, const int *d_tiles, const int *d_nflip, int ncand,
                                 double *d_new_eobj, double *d_F, double F_best, int *d_first) {
+  pngf::TraceRange trace_("pngf_eval_candidates_device");
   Handle *h = H(ph);
   if (!h || !d_tiles || !d_nflip || ncand <= 0) return PNGF_ERR_ARG;
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "not prepared");
@@ -927,6 +932,7 @@ int pngf_eval_candidates_device(pngf_handle *ph, const int *d_tiles, const int *
 }
 
 int pngf_accept(pngf_handle *ph, int cand) {
+  pngf::TraceRange trace_("pngf_accept");
   Handle *h = H(ph);
   if (!h) return PNGF_ERR_ARG;
   if (!h->batch_valid) return set_error(h, PNGF_ERR_STATE, "pngf_accept without a preceding evaluation");
@@ -1029,6 +1035,7 @@ int pngf_drift_check(pngf_handle *ph, int nrows, double *max_rel) {
 }
 
 int pngf_drift_check_freq(pngf_handle *ph, int f, int nrows, double *max_rel) {
+  pngf::TraceRange trace_("pngf_drift_check");
   Handle *h = H(ph);
   if (!h || !max_rel) return PNGF_ERR_ARG;
   if (f < 0 || f >= h->cfg.num_freq) return set_error(h, PNGF_ERR_ARG, "frequency index out of range");
@@ -1036,6 +1043,7 @@ int pngf_drift_check_freq(pngf_handle *ph, int f, int nrows, double *max_rel) {
 }
 
 int pngf_refresh(pngf_handle *ph) {
+  pngf::TraceRange trace_("pngf_refresh");
   Handle *h = H(ph);
   if (!h) return PNGF_ERR_ARG;
   return prepare_impl(h, true);
@@ -1149,6 +1157,7 @@ int pngf_set_eval_form(pngf_handle *ph, int form) {
 }
 
 int pngf_autotune(pngf_handle *ph, pngf_tune *out) {
+  pngf::TraceRange trace_("pngf_autotune");
   Handle *h = H(ph);
   if (!h || !out) return PNGF_ERR_ARG;
   if (!h->prepared) return set_error(h, PNGF_ERR_STATE, "pngf_prepare has not been called for this design");

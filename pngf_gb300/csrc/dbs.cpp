@@ -489,6 +489,7 @@ int pngf_dbs_begin(pngf_handle *ph, const pngf_dbs_params *p, pngf_dbs **out) {
 }
 
 int pngf_dbs_step(pngf_dbs *d, int *accepted) {
+  pngf::TraceRange trace_("pngf_dbs_step");
   if (!d) return PNGF_ERR_ARG;
   if (accepted) *accepted = 0;
   if (d->prop && d->topk > 0) return d->done ? PNGF_OK : proposal_step(d, accepted);
@@ -695,6 +696,7 @@ int pngf_group_create(pngf_dbs *const *members, int count, int use_graphs, pngf_
 }
 
 int pngf_group_step(pngf_group *g, int *active) {
+  pngf::TraceRange trace_("pngf_group_step");
   if (!g) return PNGF_ERR_ARG;
   const size_t nm = g->m.size();
   std::vector<char> on(nm, 0);

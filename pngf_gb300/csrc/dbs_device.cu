@@ -422,6 +422,7 @@ int devloop_set_fbest(Handle *h, DevLoop *L, double F_best) {
 }
 
 int devloop_run(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log) {
+  pngf::TraceRange trace_("pngf device decisions");
   uintptr_t key[kKeyLen];
   capture_key(h, key);
   int rc;

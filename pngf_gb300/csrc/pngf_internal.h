@@ -5,10 +5,20 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/pngf_gb300.h"
 #include "hat_rng.h"
 
 namespace pngf {
+
+// NVTX range over a host call (tracing; no cost without a tool attached).
+struct TraceRange {
+  explicit TraceRange(const char *name) { nvtxRangePushA(name); }
+  ~TraceRange() { nvtxRangePop(); }
+  TraceRange(const TraceRange &) = delete;
+  TraceRange &operator=(const TraceRange &) = delete;
+};
 
 // Largest capacitance matrix a launch handles (edges flipped at once). The
 // candidate kernel keeps K (kmax^2 complex128) in shared memory.

@@ -901,6 +901,7 @@ long pngf_prop_num_samples(const pngf_prop *p) { return p ? std::min(p->samples,
 
 // Adam steps on random minibatches of the stored samples; *loss = mean loss.
 int pngf_prop_train(pngf_prop *p, int steps, int batch, float lr, float *loss) {
+  pngf::TraceRange trace_("pngf_prop_train");
   if (!p || steps < 0 || batch < 1) return PNGF_ERR_ARG;
   const long have = std::min(p->samples, p->max_samples);
   if (have == 0) return prop_err(p, PNGF_ERR_STATE, "no training samples");
