@@ -548,8 +548,8 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
   }
   // Tensor-core operands: rows padded to the 128-row tile, zero outside what
   // each update writes. Complex64 updates (accepts and build chunks); FP64
-  // updates of up to f64tc_max_k() edges (and the FP64 build of M) on the
-  // tensor cores unless PNGF_F64_SIMT.
+  // updates (and the FP64 build of M) on the tensor cores, in pieces of
+  // f64tc_max_k() edges, unless PNGF_F64_SIMT.
   if (c64) {
     h->kt_cap = (6 * std::max(std::max(kmax, kInitChunk), defer_cap) + 31) / 32 * 32;
     h->aop_rows = (n + 127) / 128 * 128;

@@ -612,8 +612,17 @@ cudaError_t f64tc_gemm(Handle *h, int f, int k, double *D, long drows, long dcol
 
 cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W) {
   const long n = h->n, rows = n + h->E;
-  return f64tc_gemm(h, f, k, reinterpret_cast<double *>(M), rows, 2 * (n + 1), 2 * h->ldm, A, rows, W, false, h->ldm,
-                    nullptr, true);
+  // the inner dimension in pieces of at most f64tc_max_k(): each piece's
+  // product is exact and rounded once into M (as a K-blocked DGEMM rounds
+  // once per block); A and W are copies, so later pieces see the same operands
+  for (int c0 = 0; c0 < k; c0 += f64tc_max_k()) {
+    const int kc = std::min(k - c0, f64tc_max_k());
+    const cudaError_t e = f64tc_gemm(h, f, kc, reinterpret_cast<double *>(M), rows, 2 * (n + 1), 2 * h->ldm,
+                                     A + (size_t)c0 * rows, rows, W + (size_t)c0 * h->ldm, false, h->ldm, nullptr,
+                                     true);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_f64tc_wgemm(Handle *h, int f, int k, const double2 *Vneg, const void *X, bool x32, long ldx,

@@ -1169,6 +1169,10 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
       return e;
     return launch_c64_update(h, f, k);
   }
+  // FP64: W from K's explicit inverse only up to f64tc_max_k() edges; above,
+  // its error grows with cond(K) beyond that of the triangular solves
+  // (which the larger accepts keep), while the update itself runs on the
+  // tensor cores in pieces either way
   if (h->f64tc && layout != PNGF_PREC_C64 && k <= f64tc_max_k()) {
     if ((e = accept_prologue_tc<double2>(h, f, view64(h, f), q.M64, false, q.Einc, d_s, d_d, k)) != cudaSuccess)
       return e;
@@ -1184,7 +1188,7 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   e = accept_prologue<double2>(view64(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, L.LU, L.piv, L.z, L.A, L.W,
                                h->d_acc_status, st);
   if (e != cudaSuccess) return e;
-  if (h->f64tc && k <= f64tc_max_k()) {
+  if (h->f64tc) {  // W by FP64 solves, the update on the tensor cores
     h->nlaunch += 3;
     return launch_f64tc_update(h, f, k, q.M64, L.A, L.W);
   }

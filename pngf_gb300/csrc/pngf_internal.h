@@ -127,7 +127,7 @@ struct Handle {
   long aop_rows = 0, bop_rows = 0;
   int *d_tc_err = nullptr;     // set by bounded waits in the tensor-core kernels
   long a16_rows = 0, b16_rows = 0;
-  bool f64tc = false;                       // FP64 updates of up to f64tc_max_k() edges on tensor cores
+  bool f64tc = false;                       // FP64 updates on tensor cores (pieces of f64tc_max_k() edges)
   int init_chunk = kInitChunk;
   int eval_variant = 0;                     // index into kEvalForms (set by the autotuner)
   int eval_variant_small = -1;              // the same for batches of at most kSmallBatch candidates (-1: eval_variant)
