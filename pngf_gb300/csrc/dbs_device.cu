@@ -166,7 +166,9 @@ __global__ void __launch_bounds__(kLoopThreads)
     }
     return;
   }
+  // every thread reads what thread 0 updates at the end before the first barrier
   const double Fb = v.F_best;
+  const int row0 = v.log_n;
   if (tid == 0) {
     s_first = INT_MAX;
     s_bad = 0;
@@ -191,7 +193,7 @@ __global__ void __launch_bounds__(kLoopThreads)
     }
     return;
   }
-  const int row0 = v.log_n, pw = 3 * nf, rb = log_rec_bytes(nf);
+  const int pw = 3 * nf, rb = log_rec_bytes(nf);
   for (int i = tid; i < rows; i += blockDim.x) {
     unsigned char *r = logrec + (size_t)(row0 + i) * rb;
     reinterpret_cast<int *>(r)[0] = logidx[i];
