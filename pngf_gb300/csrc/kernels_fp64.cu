@@ -735,8 +735,8 @@ __global__ void __launch_bounds__(256) k_acc_factor(const SV<TM> M, long n,
 template <typename TM>
 __global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int *__restrict__ gs,
                                               const signed char *__restrict__ gd, int k, const double2 *__restrict__ LU,
-                                              const int *__restrict__ gpiv, const double2 *__restrict__ z,
-                                              double2 *__restrict__ W, long ldw) {
+                                              int ldlu, const int *__restrict__ gpiv,
+                                              const double2 *__restrict__ z, double2 *__restrict__ W, long ldw) {
   extern __shared__ double2 smem[];
   double2 *K = smem;                         // k x k
   double2 *X = K + (size_t)k * k;            // k x bw, column j at X[j*k ..]
@@ -744,7 +744,7 @@ __global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int 
   __shared__ int s[kMaxK];
   __shared__ int piv[kMaxK];
   __shared__ signed char d[kMaxK];
-  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) K[idx] = LU[idx];
+  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) K[idx] = LU[idx % k + (size_t)(idx / k) * ldlu];
   for (int q = threadIdx.x; q < k; q += blockDim.x) {
     s[q] = gs[q];
     piv[q] = gpiv[q];
@@ -1101,17 +1101,29 @@ cudaError_t launch_current_objective(Handle *h) {
 template <typename TM>
 static cudaError_t accept_prologue(const SV<TM> &v, long n, int E, long ldm, const double2 *Einc, const int *d_s,
                                    const signed char *d_d, int k, double2 *LU, int *piv, double2 *z, double2 *A,
-                                   double2 *W, int *status, cudaStream_t stream) {
+                                   double2 *W, int *status, cudaStream_t stream, const LuOut *given = nullptr,
+                                   int ld_given = 0) {
   const long rows = n + E;
-  const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
-  cudaError_t e = cudaFuncSetAttribute(k_acc_factor<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
-  if (e != cudaSuccess) return e;
-  k_acc_factor<TM><<<1, 256, smf, stream>>>(v, n, Einc, d_s, d_d, k, LU, piv, z, status);
+  const double2 *lu = LU, *zz = z;
+  const int *pv = piv;
+  int ldlu = k;
+  cudaError_t e;
+  if (given) {  // the factorization the candidate kernel left (leading dimension ld_given)
+    lu = given->LU;
+    pv = given->piv;
+    zz = given->z;
+    ldlu = ld_given;
+  } else {
+    const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
+    e = cudaFuncSetAttribute(k_acc_factor<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
+    if (e != cudaSuccess) return e;
+    k_acc_factor<TM><<<1, 256, smf, stream>>>(v, n, Einc, d_s, d_d, k, LU, piv, z, status);
+  }
   const int wc = k <= 64 ? 64 : 32;  // columns per CTA, so that K and the block fit in shared memory
   const size_t smw = sizeof(double2) * ((size_t)k * k + (size_t)k * wc);
   e = cudaFuncSetAttribute(k_acc_W<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
   if (e != cudaSuccess) return e;
-  k_acc_W<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, LU, piv, z, W, ldm);
+  k_acc_W<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, lu, ldlu, pv, zz, W, ldm);
   k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(v, n, rows, d_s, k, A, rows);
   return cudaGetLastError();
 }
@@ -1178,15 +1190,23 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
       return e;
     return launch_f64tc_update(h, f, k, q.M64, L.A, L.W);
   }
+  // a candidate of the evaluated batch: start from the factorization its kernel left
+  LuOut ev{};
+  const LuOut *given = nullptr;
+  if (h->acc_cand >= 0) {
+    const size_t cf = (size_t)h->acc_cand * h->cfg.num_freq + f, km = (size_t)h->kmax;
+    ev = LuOut{h->d_eval_LU + cf * km * km, h->d_eval_piv + cf * km, h->d_eval_z + cf * km};
+    given = &ev;
+  }
   if (layout == PNGF_PREC_C64) {
     e = accept_prologue<float2>(view32(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, L.LU, L.piv, L.z, L.A, L.W,
-                                h->d_acc_status, st);
+                                h->d_acc_status, st, given, h->kmax);
     if (e != cudaSuccess) return e;
     h->nlaunch += 3;
     return h->defer_now ? launch_c64_defer(h, f, k) : launch_c64_update(h, f, k);
   }
   e = accept_prologue<double2>(view64(h, f), n, h->E, h->ldm, q.Einc, d_s, d_d, k, L.LU, L.piv, L.z, L.A, L.W,
-                               h->d_acc_status, st);
+                               h->d_acc_status, st, given, h->kmax);
   if (e != cudaSuccess) return e;
   if (h->f64tc) {  // W by FP64 solves, the update on the tensor cores
     h->nlaunch += 3;
