@@ -500,7 +500,9 @@ int pngf_dbs_step(pngf_dbs *d, int *accepted) {
     if (rc || !have) return rc;
     if ((rc = pngf::eval_enqueue(d->h))) return rc;
     int acc = 0;
-    if ((rc = batch_finish(d, &acc, true))) return rc;
+    // the accept is not waited for: the next batch queues behind it and its
+    // read-back carries the tensor-core status
+    if ((rc = batch_finish(d, &acc, false))) return rc;
     if (acc) {
       if (accepted) *accepted = 1;
       return PNGF_OK;
