@@ -329,7 +329,10 @@ typedef struct pngf_dbs_stats {
  * (main.cpp:241) and prepares every frequency. G must be loaded. */
 int pngf_dbs_begin(pngf_handle *h, const pngf_dbs_params *p, pngf_dbs **out);
 /* One DBS decision: evaluate draws in hat order until the first improving
- * flip (accepting it, main.cpp:429-456) or until the hat is empty. */
+ * flip (accepting it, main.cpp:429-456) or until the hat is empty. The
+ * accept's launches are queued on the handle's stream and not waited for; a
+ * tensor-core update that gave up waiting is reported (PNGF_ERR_TIMEOUT) by
+ * the next step. */
 int pngf_dbs_step(pngf_dbs *d, int *accepted);
 /* Device-resident decisions (no reference counterpart): the hat's random
  * stream (std::mt19937 with std::uniform_int_distribution, restated for the
