@@ -41,17 +41,25 @@ constexpr int TC_BK = 32;        // fp32 K elements per stage = one 128-byte swi
 constexpr uint32_t A_BYTES = TC_BM * TC_BK * 4;
 constexpr uint32_t TC_DBOX = TC_BM * 128;  // 128 rows x 32 floats of T (one TMA box)
 constexpr int TC_EPI_WARPS = 8;
+constexpr int kLongKStages = 24;  // K stages per tile (rank >= 128) from which one staged tile of T is used
 constexpr int TC_THREADS = 96 + 32 * TC_EPI_WARPS;  // producer, MMA and store warps + epilogue
 using namespace tc;
 
 // Shapes per output tile width BN (fp32 columns = the MMA N; 64 or 128,
 // picked by the autotuner): operand stages in flight and shared memory.
-template <int BN> struct C64Tile {
+// ND staged tiles of T (2: the next tile's T loads during this tile's
+// epilogue; 1: for long K, where the MMAs of a tile outlast a T load and the
+// shared memory serves a deeper operand ring instead). The operand ring takes
+// what is left of the 227 KB: 3 or 6 stages with two tiles of T, 5 or 8 with one.
+constexpr size_t kTcSmemOptin = 232448;
+template <int BN, int ND> struct C64Tile {
   static constexpr uint32_t B_BYTES = BN * TC_BK * 4;  // one K stage of B
   static constexpr uint32_t STAGE = A_BYTES + B_BYTES;
-  static constexpr int ST = BN == 128 ? 3 : 6;         // operand stages (the ring hides L2 latency)
   static constexpr uint32_t DTILE = (BN / 32) * TC_DBOX;  // a 128 x BN tile of T
-  static constexpr size_t SMEM = 1024 + ST * STAGE + 2 * DTILE + 256;
+  static constexpr int ST = (int)((kTcSmemOptin - 1024 - 256 - (size_t)ND * DTILE) / STAGE);  // operand stages
+  static constexpr size_t SMEM = 1024 + ST * STAGE + ND * DTILE + 256;
+  static_assert(ND == 1 || ND == 2, "one or two staged tiles of T");
+  static_assert(SMEM <= kTcSmemOptin && (2 * ST + 10) * 8 + 4 <= 256, "shared memory and barrier block");
   // Instruction descriptor, kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
   // (bits 7-9 and 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits
   // 17-22, M >> 4 at bits 24-28.
@@ -73,11 +81,11 @@ template <int BN> struct C64Tile {
 // columns each) read the accumulator with tcgen05.ld and update the staged
 // tile in place (thread = row; the swizzle makes these accesses conflict-free);
 // warp 2 writes each finished tile back with a TMA store and frees its slot.
-template <int BN>
+template <int BN, int ND>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_update(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                 const __grid_constant__ CUtensorMap tmD, int cols, int ncb, int ntiles, int nkb, int *err) {
-  using S = C64Tile<BN>;
+  using S = C64Tile<BN, ND>;
   constexpr int ST = S::ST;
   extern __shared__ unsigned char smem_raw[];
   unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -85,7 +93,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t sbase = smem_u32(base);
   constexpr uint32_t dbase = ST * S::STAGE;  // byte offset of slot 0 from base
   const uint32_t sD0 = sbase + dbase;
-  uint64_t *bars = reinterpret_cast<uint64_t *>(base + dbase + 2 * S::DTILE);
+  uint64_t *bars = reinterpret_cast<uint64_t *>(base + dbase + ND * S::DTILE);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2 * ST + 10);
   const uint32_t bar0 = smem_u32(bars);
   auto full = [&](int s) { return bar0 + 8 * s; };
@@ -125,8 +133,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       int g = 0, issuedD = 0;
       for (int t = t_begin; t < t_end && ok; ++t) {
         const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb;
-        const int m0 = rb * TC_BM, n0 = cb * BN, s = li & 1;
-        if (li >= 2 && !mbar_wait(d_empty(s), ((li >> 1) - 1) & 1)) { ok = false; break; }
+        const int m0 = rb * TC_BM, n0 = cb * BN, s = li % ND;
+        if (li >= ND && !mbar_wait(d_empty(s), ((li / ND) - 1) & 1)) { ok = false; break; }
         mbar_expect_tx(d_full(s), S::DTILE);
         for (int j = 0; j < BN / 32; ++j) tma_load_2d(sD0 + s * S::DTILE + j * TC_DBOX, &tmD, n0 + 32 * j, m0, d_full(s));
         ++issuedD;
@@ -142,8 +150,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       // Drain: every copy this thread issued has landed before the CTA exits.
       for (int q = g > ST ? g - ST : 0; q < g; ++q)
         if (!mbar_wait(full(q % ST), (q / ST) & 1)) atomicExch(err, 34);
-      for (int q = issuedD > 2 ? issuedD - 2 : 0; q < issuedD; ++q)
-        if (!mbar_wait(d_full(q & 1), (q >> 1) & 1)) atomicExch(err, 34);
+      for (int q = issuedD > ND ? issuedD - ND : 0; q < issuedD; ++q)
+        if (!mbar_wait(d_full(q % ND), (q / ND) & 1)) atomicExch(err, 34);
     }
   } else if (warp == 1) {
     if (lane == 0) {
@@ -174,8 +182,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (lane == 0) {
       bool ok = true;
       for (int t = t_begin; t < t_end; ++t) {
-        const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb, s = li & 1;
-        if (!mbar_wait(d_done(s), (li >> 1) & 1)) { ok = false; break; }
+        const int li = t - t_begin, rb = t / ncb, cb = t - rb * ncb, s = li % ND;
+        if (!mbar_wait(d_done(s), (li / ND) & 1)) { ok = false; break; }
         for (int j = 0; j < BN / 32; ++j)  // rows / columns past T are clipped
           if (cb * BN + 32 * j < cols) tma_store_2d(&tmD, sD0 + s * S::DTILE + j * TC_DBOX, cb * BN + 32 * j, rb * TC_BM);
         bulk_commit();
@@ -192,7 +200,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     const int r = q * 32 + lane;      // row of the tile (TMEM lane)
     bool ok = true;
     for (int t = t_begin; t < t_end; ++t) {
-      const int li = t - t_begin, b = li & 1, s = li & 1;
+      const int li = t - t_begin, b = li & 1, s = li % ND;
       ok = __all_sync(0xffffffffu, mbar_wait(acc_full(b), (li >> 1) & 1));
       if (!ok) break;
       tc_fence_after();
@@ -204,7 +212,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(acc_empty(b));  // the accumulator may be refilled
-      ok = __all_sync(0xffffffffu, mbar_wait(d_full(s), (li >> 1) & 1));
+      ok = __all_sync(0xffffffffu, mbar_wait(d_full(s), (li / ND) & 1));
       if (!ok) break;
       // Rows and columns past T hold the TMA's zero fill and a zero
       // accumulator; the store clips them.
@@ -656,19 +664,21 @@ cudaError_t launch_c64_tc(Handle *h, int f, int Kt, int rank) {
   const int ncb = (dcols + bn - 1) / bn, ntiles = ncb * (int)((n + TC_BM - 1) / TC_BM);
   const int grid = persistent_grid(h, ntiles, g_c64_sms);
   cudaEvent_t t0 = timing_mark(h, st);
-  if (bn == 64) {
-    if ((e = cudaFuncSetAttribute(k_tc_update<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)C64Tile<64>::SMEM)) != cudaSuccess)
-      return e;
-    k_tc_update<64><<<grid, TC_THREADS, C64Tile<64>::SMEM, st>>>(ma, mb, md, dcols, ncb, ntiles, Kt / TC_BK,
-                                                                  h->d_tc_err);
-  } else {
-    if ((e = cudaFuncSetAttribute(k_tc_update<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)C64Tile<128>::SMEM)) != cudaSuccess)
-      return e;
-    k_tc_update<128><<<grid, TC_THREADS, C64Tile<128>::SMEM, st>>>(ma, mb, md, dcols, ncb, ntiles, Kt / TC_BK,
-                                                                    h->d_tc_err);
-  }
+  // long K (build chunks, flushes of deferred updates): one staged tile of T
+  // and a deeper operand ring
+  const int nkb = Kt / TC_BK;
+  const bool longk = nkb >= kLongKStages;
+  auto go = [&](auto kern, size_t smem) -> cudaError_t {
+    cudaError_t r = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (r != cudaSuccess) return r;
+    kern<<<grid, TC_THREADS, smem, st>>>(ma, mb, md, dcols, ncb, ntiles, nkb, h->d_tc_err);
+    return cudaGetLastError();
+  };
+  if (bn == 64)
+    e = longk ? go(k_tc_update<64, 1>, C64Tile<64, 1>::SMEM) : go(k_tc_update<64, 2>, C64Tile<64, 2>::SMEM);
+  else
+    e = longk ? go(k_tc_update<128, 1>, C64Tile<128, 1>::SMEM) : go(k_tc_update<128, 2>, C64Tile<128, 2>::SMEM);
+  if (e != cudaSuccess) return e;
   const double cells = (double)n * (double)n;  // complex entries of T updated
   timing_close(h, t0, T_UPDATE, 8.0 * rank * cells,
                2.0 * 8.0 * cells + 4.0 * Kt * ((double)h->aop_rows + (double)h->bop_rows), 0.0, st);
