@@ -49,3 +49,35 @@ def test_null_handle_calls_are_errors(built_lib):
     assert built_lib.pngf_prepare(None) == 1
     assert built_lib.pngf_accept(None, 0) == 1
     assert built_lib.pngf_destroy(None) == 0
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Every public struct's ctypes mirror has the size and field offsets the
+    C compiler gives the header's declaration (fields appended to a struct
+    keep callers compiled against it in step with the library)."""
+    import os
+    import shutil
+    import subprocess
+
+    from conftest import ROOT
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("gcc not found")
+    structs = {"pngf_config": lib.Config, "pngf_dbs_params": lib.DbsParams, "pngf_dbs_stats": lib.DbsStats,
+               "pngf_timing": lib.Timing, "pngf_tune": lib.Tune, "pngf_group_stats": lib.GroupStats}
+    src = ['#include <stddef.h>', '#include <stdio.h>', '#include "pngf_gb300.h"', "int main(void) {"]
+    for cname, cls in structs.items():
+        src.append('  printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in cls._fields_:
+            src.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    src += ["  return 0;", "}"]
+    c = tmp_path / "layout.c"
+    c.write_text("\n".join(src) + "\n")
+    exe = str(tmp_path / "layout")
+    subprocess.run([gcc, "-std=c11", "-I" + os.path.join(ROOT, "include"), str(c), "-o", exe], check=True)
+    got = dict(line.split() for line in subprocess.run([exe], capture_output=True, text=True,
+                                                       check=True).stdout.splitlines())
+    for cname, cls in structs.items():
+        assert int(got[cname]) == C.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert int(got["%s.%s" % (cname, fname)]) == getattr(cls, fname).offset, (cname, fname)
