@@ -308,7 +308,7 @@ def autotune_on(h, mode_single=True):
 
 
 def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), train_evals=1500, train_steps=600,
-                     topk=64, state_only=0, batch=0, device_loop=False):
+                     topk=64, state_only=0, batch=0, device_loop=False, online_every=0):
     """Wall time to the converged objective: plain FP64 DBS (reference order,
     run until the hat is empty) against the proposal + complex64 form, whose
     network is trained only on plain complex64 runs from other seeds. The
@@ -359,7 +359,9 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, batch=0, drift_every=32, drift_tol=1e-4)
-    lib.dbs_set_proposal(d, prop, topk=topk, train_every=8, train_steps=20, train_batch=32, lr=1e-3)
+    # online_every > 0: 20 more training steps on the run's own exact pairs every
+    # that many proposal steps (0: the network trained beforehand is kept)
+    lib.dbs_set_proposal(d, prop, topk=topk, train_every=online_every, train_steps=20, train_batch=32, lr=1e-3)
     torch.cuda.synchronize()
     t_prep = time.perf_counter() - t0
     h.timing_enable(True)
@@ -386,7 +388,9 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
                            "reached_target": t_reach is not None,
                            "training": {"seeds": list(train_seeds), "collect_s": t_collect, "train_s": t_train,
                                         "samples": samples, "pairs": pairs, "final_loss": loss,
-                                        "steps": train_steps}}
+                                        "steps": train_steps,
+                                        "online": ("20 steps every %d proposal steps" % online_every)
+                                        if online_every > 0 else "none"}}
     out["F_target"] = F_target
     if t_reach:
         out["speedup_wall_to_objective"] = out["plain_fp64"]["wall_s"] / t_reach
@@ -502,7 +506,7 @@ def c5_run(a, local):
     t0 = time.perf_counter()
     out = converge_compare(41, FREQS_C5, lambda h: [h.load_G_synth(f, seed=1) for f in range(len(FREQS_C5))],
                            a.seed, local, train_evals=3000, train_steps=1000, batch=a.batch,
-                           device_loop=bool(a.device_loop))
+                           device_loop=bool(a.device_loop), online_every=8)
     print(json.dumps({"metric": "wall time to converged objective, 41x41 tiles x 4 frequencies, proposal + "
                                 "complex64 vs plain FP64", "c5": out, "total_s": time.perf_counter() - t0}),
           flush=True)
