@@ -13,10 +13,20 @@
 //
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address with cudaGetSymbolAddress and caches it; make
-// that first call before any stream capture. All calls share the one array
-// and it keeps the last call's contents: calls that overlap on the GPU (on
-// different streams, or from several host threads) race on it, so serialise
-// them on one stream. The status word is cleared on every call.
+// that first call before any stream capture. The cached address belongs to
+// the device's primary context: after cudaDeviceReset the module is loaded
+// again and the array may move, so this entry point must not be used across a
+// device reset. All calls share the one array and it keeps the last call's
+// contents: calls that overlap on the GPU (on different streams, or from
+// several host threads) race on it, so serialise them on one stream.
+//
+// The caller's edge list is untrusted input: the factor kernel checks every
+// index against [0, n) and every sign against +-1 before any of them
+// addresses M, and on a bad entry sets the status to PNGF_ERR_ARG; on a
+// singular K it sets PNGF_ERR_SINGULAR. In both cases the later kernels return
+// without writing, so M is left exactly as it was. The status word (the
+// caller's, or one inside the scratch array when status is NULL) is cleared
+// at the start of every call.
 #include <cuda_runtime.h>
 
 #include <mutex>
