@@ -73,6 +73,12 @@ def parse():
     ap.add_argument("--no-converge", action="store_true",
                     help="skip the wall time to convergence, plain FP64 DBS against proposal + complex64 DBS")
     ap.add_argument("--no-group", action="store_true", help="skip the many-instance group run")
+    ap.add_argument("--eval-probe", type=int, default=0,
+                    help="profiling case for the candidate kernel: N passes of every tile at every frequency on a "
+                         "state-only handle (G not kept), one JSON line; nothing else runs")
+    ap.add_argument("--eval-form", type=int, default=1, help="--eval-probe: candidate-kernel form")
+    ap.add_argument("--no-c5", action="store_true",
+                    help="skip the reduced 41x41 x 4-frequency proposal comparison of the default run")
     ap.add_argument("--c5", action="store_true",
                     help="only the learned-proposal form at 41x41 tiles x 4 frequencies against plain FP64 DBS")
     ap.add_argument("--instances", type=int, default=64, help="group run: DBS instances")
@@ -172,8 +178,34 @@ def fp64_gemm_peak_tflops():
 
 
 def make_Gs(tiles, freqs):
-    from pngf_gb300 import lib
-    return [lib.synth_G(tiles, tiles, f, seed=1) for f in freqs]
+    """The workload's inputs, from the oracle's generator (oracle/synth.c, the
+    same recipe as the library's): one synthetic G per frequency and the two
+    NF2FF rows (broadside far-field projection), so that the objective's
+    directivity term is live. Returns (Gs, rows)."""
+    from oracle import synth
+    return [synth.synth_G(tiles, tiles, f, seed=1) for f in freqs], synth.synth_gobj(tiles, tiles, seed=1)
+
+
+def ldm_of(n):
+    """Leading dimension of M on the device: N+1 rounded up to 16."""
+    return (n + 1 + 15) // 16 * 16
+
+
+METRIC = "DBS flip evals/s, 21x21 tiles x 5 frequencies, plain FP64 form"
+
+
+def workload_config(a, n, nf, world):
+    """The `config` object both arms print (identical for the same flags)."""
+    return {
+        "workload": "wideband %dx%d tiles x %d frequencies (27-33 GHz), N=%d edges, %s-tile DBS from a "
+                    "50%%-fill random design (seed %d), synthetic complex-symmetric dyadic G with broadside NF2FF "
+                    "rows" % (a.tiles, a.tiles, nf, n, a.mode, a.seed),
+        "tiles": a.tiles, "freqs_ghz": [f / 1e9 for f in FREQS], "edges": n,
+        "candidates_per_pass": a.tiles * a.tiles if a.mode == "single" else None,
+        "precision": "fp64", "parallelism": "one DBS instance per GPU" if world > 1 else "single GPU",
+        "l2": "inputs larger than L2: M is %.2f GB per frequency" % ((n + 3) * ldm_of(n) * 16 / 1e9),
+        "step": "one DBS decision (evaluations in hat order until the first improving draw, which is accepted)",
+    }
 
 
 def cpu_baseline_sample(tiles, mode, seed, freq, gpu_evals, gpu_accepts, nf, budget_s=20.0):
@@ -181,11 +213,11 @@ def cpu_baseline_sample(tiles, mode, seed, freq, gpu_evals, gpu_accepts, nf, bud
     frequencies: init, then DBS steps until ~budget_s of evaluation/accept work.
     Returns per-frequency eval and accept times and the modelled throughput on
     the GPU run's eval/accept mix at nf frequencies."""
+    from oracle import synth
     from oracle.dbs import DbsRunner
     from oracle.port import threads
-    from pngf_gb300 import lib
-    G = np.ascontiguousarray(lib.synth_G(tiles, tiles, freq, seed=1))
-    gobj = np.zeros((2, G.shape[0]), dtype=np.complex128)
+    G = synth.synth_G(tiles, tiles, freq, seed=1)
+    gobj = synth.synth_gobj(tiles, tiles, seed=1)
     t0 = time.perf_counter()
     r = DbsRunner([G], [gobj], [freq], tiles, tiles, seed, sym=(mode == "sym"), algebra="port")
     t_init = time.perf_counter() - t0
@@ -229,7 +261,7 @@ def cpu_baseline_sample(tiles, mode, seed, freq, gpu_evals, gpu_accepts, nf, bud
     }
 
 
-def run_form(a, precision, Gs, rank, local, dist, defer_rank=0):
+def run_form(a, precision, Gs, rows, rank, local, dist, defer_rank=0):
     """Runs W + K DBS decisions of one precision form; returns its counters."""
     import torch
     from pngf_gb300 import lib
@@ -237,7 +269,7 @@ def run_form(a, precision, Gs, rank, local, dist, defer_rank=0):
     h = lib.Handle(a.tiles, a.tiles, FREQS, precision=precision, max_flips=1 if a.mode == "single" else 4,
                    device=local, defer_rank=defer_rank)
     for f, G in enumerate(Gs):
-        h.load_G(f, G, None)
+        h.load_G(f, G, rows)
     d = lib.Dbs(h, mode=lib.DBS_SINGLE if a.mode == "single" else lib.DBS_SYMMETRIC, init=lib.INIT_RANDOM,
                 seed=a.seed + rank, batch=a.batch, device_loop=bool(a.device_loop))
     tune = h.autotune()  # kernel forms for this instance; the state is left unchanged
@@ -271,14 +303,14 @@ def run_form(a, precision, Gs, rank, local, dist, defer_rank=0):
     return out
 
 
-def isolated_update(a, precision, G0, local, decisions=6):
+def isolated_update(a, precision, G0, rows, local, decisions=6):
     """The accept update alone: a one-frequency handle (one stream, nothing
     sharing the GPU with its launches), a few DBS decisions from the same
     design; returns the update kernel's mean launch time and bytes."""
     import torch
     from pngf_gb300 import lib
     h = lib.Handle(a.tiles, a.tiles, FREQS[:1], precision=precision, max_flips=1, device=local)
-    h.load_G(0, G0, None)
+    h.load_G(0, G0, rows)
     d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, batch=0)
     h.autotune()
     d.step()
@@ -327,13 +359,23 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
     d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, batch=batch, device_loop=device_loop)
     torch.cuda.synchronize()
     t_prep = time.perf_counter() - t0
-    s = d.run()
+    # step by step, recording when each decision's F_best was known on the
+    # host, so that the time to first reach the target is known afterwards
+    trace = []
+    while True:
+        d.step()
+        s = d.stats()
+        trace.append((time.perf_counter() - t0, s.F_best, s.evals))
+        if s.converged or s.evals >= 10 ** 7:
+            break
     torch.cuda.synchronize()
+    F_target = s.F_best * (1.0 + 1e-3)
+    hit = next(((t, e) for t, F, e in trace if F <= F_target), (trace[-1][0], trace[-1][2]))
     out["plain_fp64"] = {"wall_s": time.perf_counter() - t0, "prepare_s": t_prep, "F_final": s.F_best,
                          "F_init": s.F_init,
                          "evals": s.evals, "accepts": s.accepts, "converged": bool(s.converged),
+                         "wall_s_to_target": hit[0], "evals_to_target": hit[1],
                          "eval_form": tune64["eval_form"]}
-    F_target = s.F_best * (1.0 + 1e-3)
     d.close()
     h.close()
     torch.cuda.empty_cache()
@@ -393,7 +435,17 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
                                         if online_every > 0 else "none"}}
     out["F_target"] = F_target
     if t_reach:
+        # headline: plain FP64 run to its converged objective against the
+        # proposal form reaching that objective within 1e-3
         out["speedup_wall_to_objective"] = out["plain_fp64"]["wall_s"] / t_reach
+        # both forms to the same target (plain FP64 also stops at its first
+        # crossing of F_target)
+        out["speedup_both_to_target"] = out["plain_fp64"]["wall_s_to_target"] / t_reach
+        # with the network's offline data collection and training on the clock
+        t_train_all = t_collect + t_train
+        out["speedup_wall_to_objective_incl_training"] = out["plain_fp64"]["wall_s"] / (t_reach + t_train_all)
+        out["speedup_both_to_target_incl_training"] = (out["plain_fp64"]["wall_s_to_target"] /
+                                                       (t_reach + t_train_all))
     d.close()
     prop.close()
     h.close()
@@ -496,6 +548,20 @@ def group_bench(a, local, n_check=8):
 FREQS_C5 = [28.0e9, 29.33e9, 30.67e9, 32.0e9]
 
 
+def c5_compare(a, local, reduced=True):
+    """C5: 41x41 tiles (N = 30504), 4 frequencies, synthetic G and NF2FF rows
+    generated on the device; plain FP64 DBS to convergence against proposal +
+    complex64 DBS. The default run's reduced form trains the network on one
+    other seed's 2000 plain complex64 evaluations (600 Adam steps); --c5 runs
+    the full form (two seeds, 3000 evaluations each, 1000 steps)."""
+    kw = dict(train_seeds=(2,), train_evals=2000, train_steps=600) if reduced else \
+        dict(train_evals=3000, train_steps=1000)
+    out = converge_compare(41, FREQS_C5, lambda h: [h.load_G_synth(f, seed=1) for f in range(len(FREQS_C5))],
+                           a.seed, local, batch=a.batch, device_loop=bool(a.device_loop), online_every=8, **kw)
+    out["form"] = "reduced training (1 seed, 2000 evaluations)" if reduced else "full training"
+    return out
+
+
 def c5_run(a, local):
     """The learned-proposal form at 41x41 tiles (N = 30504), 4 frequencies,
     synthetic G generated on the device: wall time to the converged objective
@@ -504,9 +570,7 @@ def c5_run(a, local):
     import torch
     torch.cuda.set_device(local)
     t0 = time.perf_counter()
-    out = converge_compare(41, FREQS_C5, lambda h: [h.load_G_synth(f, seed=1) for f in range(len(FREQS_C5))],
-                           a.seed, local, train_evals=3000, train_steps=1000, batch=a.batch,
-                           device_loop=bool(a.device_loop), online_every=8)
+    out = c5_compare(a, local, reduced=False)
     print(json.dumps({"metric": "wall time to converged objective, 41x41 tiles x 4 frequencies, proposal + "
                                 "complex64 vs plain FP64", "c5": out, "total_s": time.perf_counter() - t0}),
           flush=True)
@@ -537,27 +601,28 @@ def gpu_arm(a, world, rank, local):
     peaks, peak_src = measured_peaks()
     fp64_peak = fp64_gemm_peak_tflops()
     nf = len(FREQS)
-    Gs = make_Gs(a.tiles, FREQS)
+    Gs, rows = make_Gs(a.tiles, FREQS)
     forms = a.forms.split(",")
     r64 = r32 = None
     if "fp64" in forms:
-        r64 = run_form(a, lib.PREC_FP64, Gs, rank, local, dist)
+        r64 = run_form(a, lib.PREC_FP64, Gs, rows, rank, local, dist)
         wall_m, dev_m, evals_t, accepts_t, launched_t = reduce_form(r64, dist)
     if "c64" in forms:
-        r32 = run_form(a, lib.PREC_C64, Gs, rank, local, dist)
+        r32 = run_form(a, lib.PREC_C64, Gs, rows, rank, local, dist)
         c64_red = reduce_form(r32, dist)
     r32d = None
     if "c64d" in forms:  # complex64 with the rank-k updates deferred to rank 192
-        r32d = run_form(a, lib.PREC_C64, Gs, rank, local, dist, defer_rank=192)
+        r32d = run_form(a, lib.PREC_C64, Gs, rows, rank, local, dist, defer_rank=192)
         c64d_red = reduce_form(r32d, dist)
-    iso64 = isolated_update(a, lib.PREC_FP64, Gs[0], local) if r64 is not None and rank == 0 else None
-    iso32 = isolated_update(a, lib.PREC_C64, Gs[0], local) if r32 is not None and rank == 0 else None
+    iso64 = isolated_update(a, lib.PREC_FP64, Gs[0], rows, local) if r64 is not None and rank == 0 else None
+    iso32 = isolated_update(a, lib.PREC_C64, Gs[0], rows, local) if r32 is not None and rank == 0 else None
     conv = None
     if not a.no_converge and rank == 0:
-        conv = converge_compare(a.tiles, FREQS, lambda h: [h.load_G(f, G, None) for f, G in enumerate(Gs)], a.seed,
+        conv = converge_compare(a.tiles, FREQS, lambda h: [h.load_G(f, G, rows) for f, G in enumerate(Gs)], a.seed,
                                 local, batch=a.batch, device_loop=bool(a.device_loop))
     del Gs
     grp = group_bench(a, local) if (not a.no_group and rank == 0) else None
+    c5 = c5_compare(a, local) if (not a.no_c5 and not a.no_converge and rank == 0) else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -609,8 +674,27 @@ def gpu_arm(a, world, rank, local):
                                 "launch_ms": iso64["launch_ms"], "achieved": g, "frac": g / peaks["hbm_gbs"],
                                 "launches": iso64["launches"]}
     eval_s = tm["eval_ms"] * 1e-3
+    # kernels (a)+(c): the candidate evaluation launch group (edge lists,
+    # candidate kernel, scoring). Its work is a capacitance LU per (candidate,
+    # frequency) in FP64 over gathers of k^2 + (E+1) k entries of M, so its
+    # bound is the FP64 pipe; the HBM view is reported beside it.
+    roofline_eval = {
+        "kernel": "k_eval / k_eval_warp + k_edge_lists + k_score (candidate evaluation, FP64 capacitance LU)",
+        "bound": "fp64",
+        "achieved": tm["eval_flop"] / eval_s / 1e12 if eval_s > 0 else None,
+        "peak": fp64_peak, "unit": "TFLOP/s",
+        "frac": tm["eval_flop"] / eval_s / 1e12 / fp64_peak if eval_s > 0 else None,
+        "peak_source": "cuBLAS DGEMM 4096^3 via torch on this GPU in this run, best of 5",
+        "algorithmic_flop_per_cand_freq": tm["eval_flop"] / max(1.0, tm["eval_cf"]),
+        "launch_ms": tm["eval_ms"] / max(1, tm["eval_launches"]),
+        "cand_freq_per_launch": tm["eval_cf"] / max(1, tm["eval_launches"]),
+        "hbm_view": {"achieved_gbs": tm["eval_bytes"] / eval_s / 1e9 if eval_s > 0 else None,
+                     "peak_gbs": peaks["hbm_gbs"],
+                     "frac": tm["eval_bytes"] / eval_s / 1e9 / peaks["hbm_gbs"] if eval_s > 0 else None,
+                     "algorithmic_bytes_per_cand_freq": tm["eval_bytes"] / max(1.0, tm["eval_cf"])},
+    }
     line = {
-        "metric": "DBS flip evals/s, 21x21 tiles x 5 frequencies, plain FP64 form",
+        "metric": METRIC,
         "value": evals_t / dev_m if dev_m > 0 else None,
         "unit": "flip_evals/s",
         "n_gpus": world,
@@ -622,22 +706,11 @@ def gpu_arm(a, world, rank, local):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic",
-        "config": {
-            "workload": "wideband %dx%d tiles x %d frequencies (27-33 GHz), N=%d edges, %s-tile DBS from a "
-                        "50%%-fill random design (seed %d), synthetic complex-symmetric dyadic G" % (
-                            a.tiles, a.tiles, nf, n, a.mode, a.seed),
-            "tiles": a.tiles, "freqs_ghz": [f / 1e9 for f in FREQS], "edges": n,
-            "candidates_per_pass": a.tiles * a.tiles if a.mode == "single" else None,
-            "precision": "fp64", "parallelism": "one DBS instance per GPU" if world > 1 else "single GPU",
-            "l2": "inputs larger than L2: M is %.2f GB per frequency" % ((n + 3) * r64["ldm"] * 16 / 1e9),
-            "step": "one DBS decision (speculative batches of draws in hat order until the first improving one, "
-                    "which is accepted; batch %s)" % ("adaptive from %d" % -a.batch if a.batch < 0 else
-                                                       "whole remaining hat" if a.batch == 0 else str(a.batch)),
-            "value_timing": "sum of CUDA-event spans of the hot-path launch groups on the handle's stream",
-        },
+        "config": workload_config(a, n, nf, world),
         "e2e": {"value": evals_t / wall_m, "unit": "flip_evals/s",
                 "h2d_bytes_per_step": tm["h2d_bytes"] / a.steps, "d2h_bytes_per_step": tm["d2h_bytes"] / a.steps},
         "roofline": roofline,
+        "roofline_eval": roofline_eval,
         "clocks": r64["clocks"],
         "gpu_launches": tm["kernel_launches"],
         "detail": {
@@ -648,6 +721,11 @@ def gpu_arm(a, world, rank, local):
             "eval_kernel_fp64_tflops": tm["eval_flop"] / eval_s / 1e12 if eval_s > 0 else None,
             "eval_ms": tm["eval_ms"], "accept_ms": tm["accept_ms"], "update_ms": tm["update_ms"],
             "setup_s": r64["setup_s"], "F_init": r64["F_init"], "F_best": r64["F_best"],
+            "speculation": "draws evaluated in speculative batches in hat order (batch %s); decisions, accepts and "
+                           "the counted evaluations are the reference's" % (
+                               "adaptive from %d" % -a.batch if a.batch < 0 else
+                               "whole remaining hat" if a.batch == 0 else str(a.batch)),
+            "value_timing": "sum of CUDA-event spans of the hot-path launch groups on the handle's stream",
             "fp64_gemm_tflops": fp64_peak, "autotune": r64["tune"],
         },
     }
@@ -706,6 +784,8 @@ def gpu_arm(a, world, rank, local):
         line["converge"] = conv
     if grp is not None:
         line["group"] = grp
+    if c5 is not None:
+        line["c5"] = c5
     if world == 1 and not a.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(a.tiles, a.mode, a.seed, FREQS[0], r64["evals"],
                                                    r64["accepts"], nf)
@@ -721,9 +801,9 @@ def reference_arm(a, world, rank):
     from oracle.port import threads
     nf = len(FREQS)
     t0 = time.perf_counter()
-    Gs = [np.ascontiguousarray(G) for G in make_Gs(a.tiles, FREQS)]
-    gobj = [np.zeros((2, Gs[0].shape[0]), dtype=np.complex128) for _ in Gs]
-    r = DbsRunner(Gs, gobj, FREQS, a.tiles, a.tiles, a.seed, sym=(a.mode == "sym"), algebra="port")
+    Gs, rows = make_Gs(a.tiles, FREQS)
+    n = Gs[0].shape[0]
+    r = DbsRunner(Gs, [rows] * nf, FREQS, a.tiles, a.tiles, a.seed, sym=(a.mode == "sym"), algebra="port")
     del Gs
     setup_s = time.perf_counter() - t0
     for _ in range(a.warmup):
@@ -736,13 +816,11 @@ def reference_arm(a, world, rank):
     evals = r.log.evals - e0
     v = evals / wall
     line = {
-        "metric": "DBS flip evals/s, 21x21 tiles x 5 frequencies, plain FP64 form",
+        "metric": METRIC,
         "impl": "reference", "value": v, "unit": "flip_evals/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": wall / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "wideband %dx%d tiles x %d frequencies (27-33 GHz), %s-tile DBS from a 50%%-fill "
-                               "random design (seed %d)" % (a.tiles, a.tiles, nf, a.mode, a.seed),
-                   "step": "one DBS decision (evaluations until the first improving draw, then its accept)"},
+        "config": workload_config(a, n, nf, world),
         "cpu_baseline": {"value": v, "unit": "flip_evals/s", "cores": threads(), "kind": "port",
                          "sample": "%d DBS decisions (%d evals) after %d warm-up decisions, all %d frequencies; "
                                    "setup (G, LU inverse of C) %.1f s untimed" % (a.steps, evals, a.warmup, nf,
@@ -752,11 +830,44 @@ def reference_arm(a, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def eval_probe(a, local):
+    """The candidate kernel alone at the workload's full pass (every tile at
+    every frequency: 441 x 5 (candidate, frequency) pairs at 21x21), on a
+    state-only handle whose G is generated on the device and not kept (M only:
+    about 1 GB per frequency). For ncu captures of one launch (-k regex:k_eval
+    -c 1); also prints the CUDA-event time per launch."""
+    import torch
+    from pngf_gb300 import lib
+    torch.cuda.set_device(local)
+    h = lib.Handle(a.tiles, a.tiles, FREQS, precision=lib.PREC_FP64, max_flips=1, device=local, state_only=1)
+    for f in range(len(FREQS)):
+        h.load_G_synth(f, seed=1)
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=a.seed, max_evals=1)  # prepares the design
+    h.set_eval_form(a.eval_form)
+    cands = [[t] for t in range(a.tiles * a.tiles)]
+    h.timing_enable(True)
+    for _ in range(a.eval_probe):
+        h.eval_candidates(cands)
+    tm = h.timing()
+    d.close()
+    h.close()
+    nl = max(1, tm["eval_launches"])
+    print(json.dumps({"eval_probe": {"form": a.eval_form, "launches": tm["eval_launches"],
+                                     "cand_freq_per_launch": tm["eval_cf"] / nl,
+                                     "ms_per_launch_group": tm["eval_ms"] / nl,
+                                     "fp64_tflops": tm["eval_flop"] / (tm["eval_ms"] * 1e-3) / 1e12
+                                     if tm["eval_ms"] > 0 else None}}), flush=True)
+
+
 def main():
     global FREQS
     a = parse()
     FREQS = FREQS[:max(1, min(a.nfreq, len(FREQS)))]
     world, rank, local = dist_env()
+    if a.eval_probe:
+        if rank == 0:
+            eval_probe(a, local)
+        return
     if a.c5:
         if rank == 0:
             c5_run(a, local)

@@ -119,6 +119,14 @@ long pngf_num_edges(int tiles_x, int tiles_y, int cells_x, int cells_y);
 int pngf_synth_G(int tiles_x, int tiles_y, int cells_x, int cells_y, double dx, double dy,
                  double dz, double freq_hz, double eps_r, unsigned long long seed, double *out,
                  long ld);
+/* NF2FF rows of the synthetic G (no reference counterpart; they stand in for
+ * the far-field rows acmefdfd appends to G, acmefdfd/main.cpp:466-492): the
+ * broadside far-field projection of the edge currents, row 1 (theta) over
+ * the x-directed edges and row 2 (phi) over the y-directed ones, each entry
+ * 32 eta0 dx dy dz times a seeded complex 1 + 1e-3 perturbation. Writes 2 x n
+ * complex, row-major (the gobj_rows layout below). */
+int pngf_synth_gobj(int tiles_x, int tiles_y, int cells_x, int cells_y, double dx, double dy, double dz,
+                    unsigned long long seed, double *rows);
 /* Writes / reads a G file (acmefdfd/main.cpp:533-538, pngfopt.hpp:163-180).
  * gobj_rows: (num_eobj-1) rows of n complex entries, row-major; NULL = zero. */
 int pngf_write_G_file(const char *path, long n, int num_eobj, const double *G, long ldg,
@@ -146,7 +154,8 @@ int pngf_load_G(pngf_handle *h, int f, const double *G, long ldg, const double *
 int pngf_load_G_file(pngf_handle *h, int f, const char *path);
 /* No reference counterpart: frequency f's G is the synthetic G of
  * pngf_synth_G (same recipe, generated on the device; entries agree with
- * the host generator to ~1e-15 relative), with zero objective rows. */
+ * the host generator to ~1e-15 relative), with the synthetic NF2FF rows of
+ * pngf_synth_gobj (from the same seed) as objective rows 1 and 2. */
 int pngf_load_G_synth(pngf_handle *h, int f, unsigned long long seed, double eps_r);
 
 /* Sets the design (PNGF_Optimizer::set_tile_map, pngfopt.hpp:669-674). */
@@ -206,9 +215,12 @@ int pngf_accept(pngf_handle *h, int cand);
  * (cudaStream_t, NULL = default). Scratch lives in one fixed 8 MiB device
  * array: (N+E+ldm) k 16 + k^2 16 + 20 k bytes (plus alignment) must fit, and
  * k <= 104, else PNGF_ERR_SCRATCH / PNGF_ERR_ARG. The first call on a device
- * looks up that array's address (do it before any stream capture). Calls
- * share the array: calls that overlap on the GPU race. *status (device int,
- * may be NULL) is cleared, then set to PNGF_ERR_SINGULAR if K is singular. */
+ * looks up that array's address (do it before any stream capture; the address
+ * is not valid across cudaDeviceReset). Calls share the array: calls that
+ * overlap on the GPU race. s must hold k distinct edges. *status (device int,
+ * may be NULL) is cleared, then set on the device to PNGF_ERR_ARG if an index
+ * of s is outside [0, n) or a sign of d is not +-1, or to PNGF_ERR_SINGULAR if
+ * K is singular; in both cases M is left unchanged. */
 int pngf_accept_edges_noalloc(double *M, long ldm, long n, int num_eobj, const double *Einc, const int *s,
                               const signed char *d, int k, int *status, void *stream);
 
@@ -249,6 +261,16 @@ typedef struct pngf_timing {
 int pngf_timing_enable(pngf_handle *h, int on);
 /* Synchronizes the handle's stream and returns the accumulated counters. */
 int pngf_timing_get(pngf_handle *h, pngf_timing *out);
+
+/* Bounds-checked build (no reference counterpart; libpngf_gb300_bc.so, built
+ * with python -m pngf_gb300.build --bounds-check): every data-dependent index
+ * of the gathers of M, Einc and the state rows is checked against its extent
+ * on the device; a violation is recorded and the access skipped, nothing
+ * traps. *violations receives the number recorded since the last reset,
+ * first[3] (may be NULL) the kind (1 T, 2 y, 3 R, 4 Einc, 5 state row), row
+ * and column of one of the first; reset != 0 clears the record. The default
+ * build returns PNGF_ERR_UNSUPPORTED. */
+int pngf_bounds_check_report(long long *violations, long long *first, int reset);
 
 /* ---- autotuning (no reference counterpart) ---- */
 

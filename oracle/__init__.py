@@ -8,10 +8,13 @@ Contents:
   * ``geometry``   - Yee-edge numbering, tile edge sets and P
                      (pngf-opt/pngfopt.hpp:86-94, 624-674), the source port
                      (pngfopt.hpp:559-618).
-  * ``refalg``     - numpy restatement of the reference optimizer's algebra
-                     on C^-1 (pngfopt.hpp:196-367, linalg.hpp:34-85).
-  * ``malg``       - numpy restatement of the augmented-matrix (M) algebra
-                     that the GPU path implements, used to check it.
+  * ``refalg``     - numpy restatements of the reference optimizer's algebra
+                     on C^-1 (``RefState``, pngfopt.hpp:196-367,
+                     linalg.hpp:34-85) and of the augmented-matrix (M)
+                     algebra the GPU path implements (``MState``).
+  * ``synth``      - ctypes binding of synth.c: the synthetic G and NF2FF
+                     rows (the stand-in for acmefdfd's G files) that every
+                     oracle run and golden log uses.
   * ``magichat``   - MagicHat (pngf-opt/magichat.hpp:32-111): std::mt19937
                      plus libstdc++'s uniform_int_distribution, restated.
   * ``dbs``        - the DBS loop of pngf-opt/main.cpp:338-459, both the

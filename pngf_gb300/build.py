@@ -3,6 +3,11 @@
 Each translation unit is compiled in parallel with nvcc, then linked into
 pngf_gb300/libpngf_gb300.so next to this file. Objects go to
 pngf_gb300/_build/. Run as ``python -m pngf_gb300.build``.
+
+``--bounds-check`` builds the bounds-checked variant instead
+(-DPNGF_BOUNDS_CHECK, objects in _build/bc/, pngf_gb300/libpngf_gb300_bc.so):
+the data-dependent gathers record out-of-range indices rather than reading
+them (see csrc/bounds.cuh).
 """
 from __future__ import annotations
 
@@ -17,6 +22,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpngf_gb300.so")
+LIB_BC = os.path.join(HERE, "libpngf_gb300_bc.so")
 
 SOURCES = ["kernels_fp64.cu", "kernels_c64.cu", "kernels_f64tc.cu", "capi.cu", "dbs.cpp", "dbs_device.cu", "gfile.cpp", "noalloc.cu",
            "proposal.cu", "synth.cu"]
@@ -31,35 +37,36 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build pngf_gb300")
 
 
-def _compile(src: str) -> str:
-    obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+def _compile(src: str, bounds_check: bool = False) -> str:
+    obj = os.path.join(BUILD, "bc" if bounds_check else "", os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(
             os.path.getmtime(path), *[os.path.getmtime(os.path.join(CSRC, h)) for h in os.listdir(CSRC)
                                       if h.endswith(".h") or h.endswith(".cuh")],
             os.path.getmtime(os.path.join(ROOT, "include", "pngf_gb300.h"))):
         return obj
-    cmd = [nvcc()] + ARCH + COMMON + ["-c", path, "-o", obj]
+    cmd = [nvcc()] + ARCH + COMMON + (["-DPNGF_BOUNDS_CHECK"] if bounds_check else []) + ["-c", path, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
     return obj
 
 
-def build(verbose: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, bounds_check: bool = False) -> str:
+    os.makedirs(os.path.join(BUILD, "bc") if bounds_check else BUILD, exist_ok=True)
     srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
     with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
-        objs = list(ex.map(_compile, srcs))
-    cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-Xlinker", "--no-undefined", "-o", LIB] + objs + ["-lgomp"]
+        objs = list(ex.map(lambda s: _compile(s, bounds_check), srcs))
+    out = LIB_BC if bounds_check else LIB
+    cmd = [nvcc()] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-Xlinker", "--no-undefined", "-o", out] + objs + ["-lgomp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", out)
+    return out
 
 
 if __name__ == "__main__":
-    build(verbose=True)
+    build(verbose=True, bounds_check="--bounds-check" in sys.argv[1:])
     sys.exit(0)

@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "bounds.cuh"
 #include "pngf_internal.h"
 
 namespace pngf {
@@ -54,6 +55,16 @@ static int lanes_fork(Handle *h) {
   for (size_t i = 0; i < h->lanes.size() && e == cudaSuccess; ++i)
     e = cudaStreamWaitEvent(h->lanes[i].stream, h->ev_fork, 0);
   return cuda_check(h, e, "fork onto the frequency streams");
+}
+
+cudaError_t chain_update_wait(Handle *h, int f, cudaStream_t st) {
+  if (h->lanes.size() < 2 || f <= 0 || (size_t)f >= h->lanes.size()) return cudaSuccess;
+  return cudaStreamWaitEvent(st, h->lanes[f - 1].upd, 0);
+}
+
+cudaError_t chain_update_done(Handle *h, int f, cudaStream_t st) {
+  if (h->lanes.size() < 2 || f < 0 || (size_t)f >= h->lanes.size()) return cudaSuccess;
+  return cudaEventRecord(h->lanes[f].upd, st);
 }
 
 static int lanes_join(Handle *h) {
@@ -443,6 +454,7 @@ int pngf_destroy(pngf_handle *ph) {
     dfree(L.eA);
     dfree(L.fB);
     if (L.done) cudaEventDestroy(L.done);
+    if (L.upd) cudaEventDestroy(L.upd);
     if (L.stream) cudaStreamDestroy(L.stream);
   }
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
@@ -570,7 +582,8 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
     return fail(PNGF_ERR_CUDA);
   for (Lane &L : h->lanes) {
     if (h->lanes.size() > 1 && (cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking) != cudaSuccess ||
-                                cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming) != cudaSuccess))
+                                cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming) != cudaSuccess ||
+                                cudaEventCreateWithFlags(&L.upd, cudaEventDisableTiming) != cudaSuccess))
       return fail(PNGF_ERR_CUDA);
     if ((rc = dalloc(h, &L.A, (size_t)rows * h->acc_cap)) || (rc = dalloc(h, &L.W, (size_t)h->acc_cap * h->ldm)) ||
         (rc = dalloc(h, &L.LU, (size_t)h->acc_cap * h->acc_cap)) || (rc = dalloc(h, &L.V, (size_t)h->acc_cap * h->acc_cap)) ||
@@ -665,7 +678,7 @@ int pngf_load_G_synth(pngf_handle *ph, int f, unsigned long long seed, double ep
   q.synth = true;
   q.synth_seed = seed;
   q.synth_eps = eps_r;
-  if (h->E > 1) PNGF_CUDA(h, cudaMemsetAsync(q.gobj, 0, sizeof(double2) * (size_t)(h->E - 1) * h->n, h->stream));
+  PNGF_CUDA(h, launch_synth_gobj(h, f, q.gobj));
   if (!h->cfg.state_only) PNGF_CUDA(h, launch_synth_G(h, f, q.G, h->n, h->d_colmax));
   PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
   q.loaded = true;
@@ -673,21 +686,91 @@ int pngf_load_G_synth(pngf_handle *ph, int f, unsigned long long seed, double ep
   return PNGF_OK;
 }
 
+// Streams one acmefdfd G file to the device (the reader of
+// pngfopt.hpp:160-180 without its host copy of the whole matrix): the first N
+// columns of the (N+E-1)^2 column-major file are read in panels of about
+// 32 MB into two pinned buffers; while one panel's G block is copied
+// (cudaMemcpy2DAsync, the N design rows of each column) the next is read.
+// The E-1 objective rows (rows N.. of each column) are gathered on the host
+// (E-1 values per column) and uploaded at the end. Host memory used: the two
+// panels and the objective rows, never N^2. A missing or short file is
+// PNGF_ERR_IO and leaves the frequency not loaded.
 int pngf_load_G_file(pngf_handle *ph, int f, const char *path) {
   Handle *h = H(ph);
   if (!h) return PNGF_ERR_ARG;
   if (f < 0 || f >= h->cfg.num_freq || !path) return set_error(h, PNGF_ERR_ARG, "pngf_load_G_file: bad argument");
-  const long n = h->n;
-  std::vector<double> G, gobj;
-  try {
-    G.resize((size_t)n * n * 2);
-    gobj.resize((size_t)std::max(1, h->E - 1) * n * 2);
-  } catch (...) {
-    return set_error(h, PNGF_ERR_NOMEM, "host buffer for G");
+  if (h->cfg.state_only)
+    return set_error(h, PNGF_ERR_UNSUPPORTED, "a state_only handle takes G from pngf_load_G_synth");
+  const long n = h->n, m = n + h->E - 1;
+  const size_t colb = sizeof(double2) * (size_t)m;
+  std::FILE *fp = std::fopen(path, "rb");
+  if (!fp) return set_error(h, PNGF_ERR_IO, std::string("cannot open G file ") + path);
+  if (std::fseek(fp, 0, SEEK_END) != 0 || std::ftell(fp) < (long)(colb * (size_t)n) || std::fseek(fp, 0, SEEK_SET)) {
+    std::fclose(fp);
+    return set_error(h, PNGF_ERR_IO, std::string("G file too short: ") + path);
   }
-  const int rc = pngf_read_G_file(path, n, h->E, G.data(), n, gobj.data());
-  if (rc != PNGF_OK) return set_error(h, rc, std::string("cannot read G file ") + path);
-  return pngf_load_G(ph, f, G.data(), n, h->E > 1 ? gobj.data() : nullptr);
+  const long P = std::max<long>(1, std::min<long>(n, (32l << 20) / (long)colb));  // columns per panel
+  void *buf[2] = {nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  bool used[2] = {false, false};
+  std::vector<double2> gobj((size_t)std::max(1, h->E - 1) * n);
+  int rc = PNGF_OK;
+  std::string msg;
+  Freq &q = h->f[f];
+  for (int b = 0; b < 2 && rc == PNGF_OK; ++b)
+    if (cudaHostAlloc(&buf[b], colb * P, cudaHostAllocDefault) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev[b], cudaEventDisableTiming) != cudaSuccess) {
+      rc = PNGF_ERR_NOMEM;
+      msg = "pinned panel for the G file";
+    }
+  for (long j0 = 0, it = 0; j0 < n && rc == PNGF_OK; j0 += P, ++it) {
+    const int b = (int)(it & 1);
+    const long cols = std::min(P, n - j0);
+    if (used[b] && cudaEventSynchronize(ev[b]) != cudaSuccess) {  // the panel's previous copy is done
+      rc = PNGF_ERR_CUDA;
+      msg = "G panel copy";
+      break;
+    }
+    double2 *pb = static_cast<double2 *>(buf[b]);
+    if (std::fread(pb, colb, (size_t)cols, fp) != (size_t)cols) {
+      rc = PNGF_ERR_IO;
+      msg = std::string("G file read failed: ") + path;
+      break;
+    }
+    for (long c = 0; c < cols; ++c)
+      for (int r = 0; r < h->E - 1; ++r) gobj[(size_t)r * n + j0 + c] = pb[(size_t)c * m + n + r];
+    if (cudaMemcpy2DAsync(q.G + (size_t)j0 * n, sizeof(double2) * n, pb, colb, sizeof(double2) * n, (size_t)cols,
+                          cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+        cudaEventRecord(ev[b], h->stream) != cudaSuccess) {
+      rc = PNGF_ERR_CUDA;
+      msg = "G panel copy";
+      break;
+    }
+    used[b] = true;
+  }
+  std::fclose(fp);
+  if (rc == PNGF_OK && h->E > 1 &&
+      cudaMemcpyAsync(q.gobj, gobj.data(), sizeof(double2) * (size_t)(h->E - 1) * n, cudaMemcpyHostToDevice,
+                      h->stream) != cudaSuccess) {
+    rc = PNGF_ERR_CUDA;
+    msg = "objective rows copy";
+  }
+  // every copy from the panels and the row vector completes before they are freed
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess && rc == PNGF_OK) {
+    rc = PNGF_ERR_CUDA;
+    msg = "G file load";
+  }
+  for (int b = 0; b < 2; ++b) {
+    if (ev[b]) cudaEventDestroy(ev[b]);
+    if (buf[b]) cudaFreeHost(buf[b]);
+  }
+  if (rc != PNGF_OK) {
+    q.loaded = false;
+    return set_error(h, rc, msg);
+  }
+  q.loaded = true;
+  h->prepared = false;
+  return PNGF_OK;
 }
 
 int pngf_set_tile_map(pngf_handle *ph, const int *tile_map) {
@@ -1221,3 +1304,26 @@ int pngf_autotune(pngf_handle *ph, pngf_tune *out) {
 }
 
 }  // extern "C"
+
+// Bounds-checked build only: the violations the data-dependent gathers
+// recorded (see bounds.cuh), summed over the kernel files; first[3] = kind,
+// row and column of one of the first. reset != 0 clears the records.
+extern "C" int pngf_bounds_check_report(long long *violations, long long *first, int reset) {
+#ifndef PNGF_BOUNDS_CHECK
+  (void)violations;
+  (void)first;
+  (void)reset;
+  return PNGF_ERR_UNSUPPORTED;
+#else
+  if (!violations) return PNGF_ERR_ARG;
+  long long a[4], b[4];
+  if (pngf::bounds_read_fp64(a, reset != 0) != cudaSuccess || pngf::bounds_read_f64tc(b, reset != 0) != cudaSuccess)
+    return PNGF_ERR_CUDA;
+  *violations = a[0] + b[0];
+  if (first) {
+    const long long *src = a[0] ? a : b;
+    for (int q = 0; q < 3; ++q) first[q] = src[q + 1];
+  }
+  return PNGF_OK;
+#endif
+}

@@ -128,6 +128,31 @@ extern "C" int pngf_synth_G(int tiles_x, int tiles_y, int cells_x, int cells_y, 
   return PNGF_OK;
 }
 
+// The two NF2FF rows of the synthetic G (rows N and N+1 of an acmefdfd G file,
+// acmefdfd/main.cpp:466-492): the broadside (theta = phi = 0) far-field
+// projection of the edge currents. Row 1 (theta polarisation) weights the
+// x-directed edges, row 2 (phi) the y-directed ones; a planar source's phase
+// is constant at broadside, so each entry is the amplitude kappa eta0 dx dy dz
+// (kappa = 32: a directivity term of order one on this G) for its own
+// polarisation and zero for the other, times 1 + 1e-3 q with q the complex
+// Gaussian of the pair {e, n + row} (the G perturbation's hash, on indices
+// that no entry of G uses).
+extern "C" int pngf_synth_gobj(int tiles_x, int tiles_y, int cells_x, int cells_y, double dx, double dy,
+                               double dz, unsigned long long seed, double *rows) {
+  if (tiles_x <= 0 || tiles_y <= 0 || cells_x <= 0 || cells_y <= 0 || !rows) return PNGF_ERR_ARG;
+  const long n = pngf_num_edges(tiles_x, tiles_y, cells_x, cells_y);
+  const long nx = (long)(tiles_x * cells_x) * (tiles_y * cells_y + 1);
+  const double amp = pngf::synth_gobj_amplitude(dx, dy, dz);
+  std::complex<double> *r = reinterpret_cast<std::complex<double> *>(rows);
+  for (int row = 0; row < 2; ++row)
+    for (long e = 0; e < n; ++e) {
+      const int dir = e < nx ? 0 : 1;
+      r[(size_t)row * n + e] =
+          dir == row ? amp * (1.0 + 1e-3 * pair_gaussian(seed, (uint64_t)e, (uint64_t)(n + row))) : 0.0;
+    }
+  return PNGF_OK;
+}
+
 // Writes one G file in the acmefdfd layout. gobj_rows holds num_eobj-1 rows of
 // n entries each (row-major, may be NULL for zero rows).
 extern "C" int pngf_write_G_file(const char *path, long n, int num_eobj, const double *G,

@@ -46,6 +46,7 @@
 #include <cstdint>
 #include <mutex>
 
+#include "bounds.cuh"
 #include "pngf_internal.h"
 #include "tc_common.cuh"
 
@@ -199,8 +200,9 @@ __device__ __forceinline__ double2 ld_c(const float2 *p) {
 // in TMEM columns of level p + q. Columns from ncols2 up to the end of the
 // last tile are zeros. One warp per output column, lanes over the values.
 template <typename TIN>
-__global__ void k_slice_B(const TIN *__restrict__ W, long ldw, const int *__restrict__ rowidx, long ncols2, long bcols,
-                          int k, int k2p, __nv_bfloat16 *__restrict__ Bop, int *__restrict__ fB) {
+__global__ void k_slice_B(const TIN *__restrict__ W, long ldw, const int *__restrict__ rowidx, long rowlim,
+                          long ncols2, long bcols, int k, int k2p, __nv_bfloat16 *__restrict__ Bop,
+                          int *__restrict__ fB) {
   const long jp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (jp >= bcols) return;
@@ -215,7 +217,9 @@ __global__ void k_slice_B(const TIN *__restrict__ W, long ldw, const int *__rest
   const bool im = jp & 1;
   unsigned long long mb = 0;
   for (int c = lane; c < k; c += 32) {
-    const double2 w = ld_c(W + (size_t)(rowidx ? rowidx[c] : c) * ldw + j);
+    const long rc = rowidx ? rowidx[c] : c;
+    if (!PNGF_BOUNDS_OK(rc >= 0 && rc < rowlim, kBoundsRowIdx, rc, j)) continue;
+    const double2 w = ld_c(W + (size_t)rc * ldw + j);
     mb = max(mb, max(abs_bits(w.x), abs_bits(w.y)));
   }
   for (int o = 16; o; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
@@ -223,7 +227,9 @@ __global__ void k_slice_B(const TIN *__restrict__ W, long ldw, const int *__rest
   if (lane == 0) fB[jp] = f;
   for (int v = lane; v < 2 * k; v += 32) {
     const int c = v >> 1;
-    const double2 w = ld_c(W + (size_t)(rowidx ? rowidx[c] : c) * ldw + j);
+    const long rc = rowidx ? rowidx[c] : c;
+    const double2 w = PNGF_BOUNDS_OK(rc >= 0 && rc < rowlim, kBoundsRowIdx, rc, j) ? ld_c(W + (size_t)rc * ldw + j)
+                                                                                  : make_double2(0.0, 0.0);
     // Re out: Re A Re W - Im A Im W; Im out: Re A Im W + Im A Re W
     const double x = (v & 1) ? (im ? w.x : -w.y) : (im ? w.y : w.x);
     int d[FB_S];
@@ -537,6 +543,16 @@ int g_smem_optin = 0;
 
 int f64tc_max_k() { return 32; }
 
+cudaError_t bounds_read_f64tc(long long out[4], bool reset) {
+#ifdef PNGF_BOUNDS_CHECK
+  return bounds_read_tu(out, reset);
+#else
+  (void)reset;
+  for (int q = 0; q < 4; ++q) out[q] = 0;
+  return cudaSuccess;
+#endif
+}
+
 size_t f64tc_op_cols() { return (size_t)FB_S * FB_MAX_K2P; }
 
 size_t f64tc_b_cols() { return FB_MAX_K2P; }
@@ -562,12 +578,13 @@ cudaError_t f64tc_gemm(Handle *h, int f, int k, double *D, long drows, long dcol
   cudaStream_t st = lane_stream(h, f);
   __nv_bfloat16 *A16 = static_cast<__nv_bfloat16 *>(L.A16), *B16 = static_cast<__nv_bfloat16 *>(L.B16);
   k_slice_A<<<(unsigned)((arows + 3) / 4), 128, 0, st>>>(A, lda, drows, arows, k, k2p, A16, L.eA);
+  const long rowlim = browidx ? h->n : k;  // rows a gathered B row may come from (state rows), else B's own
   if (b32)
     k_slice_B<float2><<<(unsigned)((bcols + 3) / 4), 128, 0, st>>>(static_cast<const float2 *>(B), ldb, browidx,
-                                                                    dcols2, bcols, k, k2p, B16, L.fB);
+                                                                    rowlim, dcols2, bcols, k, k2p, B16, L.fB);
   else
     k_slice_B<double2><<<(unsigned)((bcols + 3) / 4), 128, 0, st>>>(static_cast<const double2 *>(B), ldb, browidx,
-                                                                     dcols2, bcols, k, k2p, B16, L.fB);
+                                                                     rowlim, dcols2, bcols, k, k2p, B16, L.fB);
   CUtensorMap md;
   cudaError_t e;
   if ((e = make_map_f64(&md, D, drows, dcols2, ldd)) != cudaSuccess) return e;
@@ -596,9 +613,11 @@ cudaError_t f64tc_gemm(Handle *h, int f, int k, double *D, long drows, long dcol
     return e;
   const int ntiles = nrb * ncb;
   const int grid = persistent_grid(h, ntiles, g_num_sms);
+  if (timed && (e = chain_update_wait(h, f, st)) != cudaSuccess) return e;  // the M update: one lane at a time
   cudaEvent_t t0 = timed ? timing_mark(h, st) : nullptr;
   k_tc_update_f64<<<grid, FB_THREADS, smem, st>>>(A16, B16, md, (int)drows, (int)dcols2, ncb, ntiles, k2p, nb, nd,
                                                   L.eA, L.fB, h->d_tc_err);
+  if (timed && (e = chain_update_done(h, f, st)) != cudaSuccess) return e;
   if (timed) {
     const double cells = (double)drows * (double)(dcols2 / 2);
     timing_close(h, t0, T_UPDATE, 8.0 * k * cells,

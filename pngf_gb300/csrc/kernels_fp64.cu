@@ -26,6 +26,7 @@
 #include <cmath>
 #include <vector>
 
+#include "bounds.cuh"
 #include "pngf_internal.h"
 
 namespace pngf {
@@ -87,7 +88,11 @@ template <typename TM> struct SV {
   const float2 *Vt = nullptr;
   int rp = 0;
   int rcap = 0;
+  long bn = 0;  // bounds-checked build: N, the extent every edge index must fall in (0 = unchecked)
+  int be = 0;   // ... and E, the objective rows
   __device__ __forceinline__ double2 t(size_t i, size_t j) const {
+    if (bn && !PNGF_BOUNDS_OK(i < (size_t)bn && j < (size_t)bn, kBoundsT, (long long)i, (long long)j))
+      return make_double2(0.0, 0.0);
     double2 v = ldM(T, i * ldt + j);
     if (rp > 0) {
       const float2 *u = U + i * rcap, *w = Vt + j * rcap;
@@ -102,9 +107,22 @@ template <typename TM> struct SV {
     }
     return v;
   }
-  __device__ __forceinline__ double2 yv(size_t i) const { return y[i * ys]; }
-  __device__ __forceinline__ double2 r(int e, size_t j) const { return R[(size_t)e * ldr + j]; }
+  __device__ __forceinline__ double2 yv(size_t i) const {
+    if (bn && !PNGF_BOUNDS_OK(i < (size_t)bn, kBoundsY, (long long)i, 0)) return make_double2(0.0, 0.0);
+    return y[i * ys];
+  }
+  __device__ __forceinline__ double2 r(int e, size_t j) const {
+    if (bn && !PNGF_BOUNDS_OK(e >= 0 && e < be && j <= (size_t)bn, kBoundsR, e, (long long)j))
+      return make_double2(0.0, 0.0);
+    return R[(size_t)e * ldr + j];
+  }
 };
+
+// Einc[e] for an edge index from an edge list.
+__device__ __forceinline__ double2 einc_at(const double2 *__restrict__ Einc, long e, long n) {
+  if (!PNGF_BOUNDS_OK(e >= 0 && e < n, kBoundsEinc, e, 0)) return make_double2(0.0, 0.0);
+  return Einc[e];
+}
 
 struct Geo {
   int tiles_x, tiles_y, cells_x, cells_y;
@@ -397,7 +415,7 @@ __device__ int cta_capacitance(const SV<TM> &M, long n, const double2 *__restric
                                const int *s, const signed char *d, int k, double2 *K, int ld, double2 *vec,
                                double2 *einc, int *piv, double *red) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int c = tid; c < k; c += nt) einc[c] = Einc[s[c]];
+  for (int c = tid; c < k; c += nt) einc[c] = einc_at(Einc, s[c], n);
   for (int idx = tid; idx < k * k; idx += nt) {
     const int r = idx / k, c = idx % k;  // consecutive threads read along a row of M
     double2 v = M.t(s[r], s[c]);
@@ -548,7 +566,7 @@ __global__ void __launch_bounds__(32 * WPC)
   if (lane < k) {
     s_l = es[(size_t)c * kmax + lane];
     d_l = ed[(size_t)c * kmax + lane];
-    einc_l = Eincs[f][s_l];
+    einc_l = einc_at(Eincs[f], s_l, n);
   }
   // K = T[s,s] D, one row per step with the lanes along the row.
   for (int r = 0; r < k; ++r) {
@@ -707,7 +725,7 @@ __global__ void __launch_bounds__(256) k_acc_factor(const SV<TM> M, long n,
                                                     const double2 *__restrict__ Einc, const int *__restrict__ gs,
                                                     const signed char *__restrict__ gd, int k, double2 *__restrict__ LU,
                                                     int *__restrict__ gpiv, double2 *__restrict__ z,
-                                                    int *__restrict__ status) {
+                                                    int *__restrict__ status, bool check) {
   extern __shared__ double2 smem[];
   double2 *K = smem;
   double2 *vec = K + (size_t)k * k;
@@ -716,11 +734,21 @@ __global__ void __launch_bounds__(256) k_acc_factor(const SV<TM> M, long n,
   signed char *d = reinterpret_cast<signed char *>(s + k);
   __shared__ int piv[kMaxK];
   __shared__ double red[2];
+  __shared__ int bad;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
   for (int q = threadIdx.x; q < k; q += blockDim.x) {
     s[q] = gs[q];
     d[q] = gd[q];
+    // edge lists from a caller (check): every index in [0, n), every sign +-1,
+    // before any of them addresses M or Einc
+    if (check && (s[q] < 0 || (long)s[q] >= n || (d[q] != 1 && d[q] != -1))) atomicExch(&bad, 1);
   }
   __syncthreads();
+  if (bad) {
+    if (threadIdx.x == 0) *status = PNGF_ERR_ARG;
+    return;
+  }
   const int info = cta_capacitance(M, n, Einc, s, d, k, K, k, vec, einc, piv, red);
   for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) LU[idx] = K[idx];
   for (int q = threadIdx.x; q < k; q += blockDim.x) {
@@ -736,7 +764,9 @@ template <typename TM>
 __global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int *__restrict__ gs,
                                               const signed char *__restrict__ gd, int k, const double2 *__restrict__ LU,
                                               int ldlu, const int *__restrict__ gpiv,
-                                              const double2 *__restrict__ z, double2 *__restrict__ W, long ldw) {
+                                              const double2 *__restrict__ z, double2 *__restrict__ W, long ldw,
+                                              const int *__restrict__ guard) {
+  if (guard && *guard != 0) return;  // the factor step refused the edge list or found K singular
   extern __shared__ double2 smem[];
   double2 *K = smem;                         // k x k
   double2 *X = K + (size_t)k * k;            // k x bw, column j at X[j*k ..]
@@ -865,7 +895,8 @@ __global__ void k_W_init(double2 *__restrict__ W, long ldw, long n, const double
 // A[i + r*lda] = M[i][s_r], i < N+E.
 template <typename TM>
 __global__ void k_acc_gather(const SV<TM> M, long n, long rows, const int *__restrict__ gs, int k,
-                             double2 *__restrict__ A, long lda) {
+                             double2 *__restrict__ A, long lda, const int *__restrict__ guard) {
+  if (guard && *guard != 0) return;
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= rows) return;
   if (i < n)
@@ -879,7 +910,9 @@ __global__ void k_acc_gather(const SV<TM> M, long n, long rows, const int *__res
 constexpr int RU_T = 64, RU_KS = 8;
 __global__ void __launch_bounds__(256) k_rank_update(double2 *__restrict__ M, long ldm, long rows, long cols,
                                                      const double2 *__restrict__ A, long lda,
-                                                     const double2 *__restrict__ W, long ldw, int k) {
+                                                     const double2 *__restrict__ W, long ldw, int k,
+                                                     const int *__restrict__ guard) {
+  if (guard && *guard != 0) return;  // M stays as it was
   __shared__ double2 As[RU_KS][RU_T];
   __shared__ double2 Ws[RU_KS][RU_T];
   const int tid = threadIdx.x;
@@ -952,9 +985,22 @@ static ObjConst obj_const(const Handle *h) { return ObjConst{h->cfg.dx, h->cfg.d
 
 // Views of frequency f: the FP64 layout (everything in M64) and the complex64
 // layout (T in T32, y and R/Eobj in FP64).
+// Bounds-checked build: give a view the extents its indices must fall in.
+template <typename TM>
+static SV<TM> checked(SV<TM> v, long n, int E) {
+#ifdef PNGF_BOUNDS_CHECK
+  v.bn = n;
+  v.be = E;
+#else
+  (void)n;
+  (void)E;
+#endif
+  return v;
+}
+
 static SV<double2> view64(const Handle *h, int f) {
   const double2 *M = h->f[f].M64;
-  return SV<double2>{M, h->ldm, M + h->n, h->ldm, M + (size_t)h->n * h->ldm, h->ldm};
+  return checked(SV<double2>{M, h->ldm, M + h->n, h->ldm, M + (size_t)h->n * h->ldm, h->ldm}, h->n, h->E);
 }
 static SV<float2> view32(const Handle *h, int f) {
   SV<float2> v{h->f[f].T32, h->ldm, h->f[f].y64, 1, h->f[f].R64, h->ldm};
@@ -962,7 +1008,7 @@ static SV<float2> view32(const Handle *h, int f) {
   v.Vt = h->f[f].Vt;
   v.rp = h->defer_rp;
   v.rcap = h->defer_cap;
-  return v;
+  return checked(v, h->n, h->E);
 }
 
 cudaError_t setup_views(Handle *h) {
@@ -1102,7 +1148,7 @@ template <typename TM>
 static cudaError_t accept_prologue(const SV<TM> &v, long n, int E, long ldm, const double2 *Einc, const int *d_s,
                                    const signed char *d_d, int k, double2 *LU, int *piv, double2 *z, double2 *A,
                                    double2 *W, int *status, cudaStream_t stream, const LuOut *given = nullptr,
-                                   int ld_given = 0) {
+                                   int ld_given = 0, bool raw = false) {
   const long rows = n + E;
   const double2 *lu = LU, *zz = z;
   const int *pv = piv;
@@ -1117,14 +1163,18 @@ static cudaError_t accept_prologue(const SV<TM> &v, long n, int E, long ldm, con
     const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
     e = cudaFuncSetAttribute(k_acc_factor<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf);
     if (e != cudaSuccess) return e;
-    k_acc_factor<TM><<<1, 256, smf, stream>>>(v, n, Einc, d_s, d_d, k, LU, piv, z, status);
+    k_acc_factor<TM><<<1, 256, smf, stream>>>(v, n, Einc, d_s, d_d, k, LU, piv, z, status, raw);
   }
   const int wc = k <= 64 ? 64 : 32;  // columns per CTA, so that K and the block fit in shared memory
   const size_t smw = sizeof(double2) * ((size_t)k * k + (size_t)k * wc);
   e = cudaFuncSetAttribute(k_acc_W<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smw);
   if (e != cudaSuccess) return e;
-  k_acc_W<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, lu, ldlu, pv, zz, W, ldm);
-  k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(v, n, rows, d_s, k, A, rows);
+  // raw (caller-owned buffers): the later kernels skip their work once the
+  // factor step has set the status, so that M is left as it was
+  const int *guard = raw ? status : nullptr;
+  k_acc_W<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, lu, ldlu, pv, zz, W, ldm,
+                                                                    guard);
+  k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(v, n, rows, d_s, k, A, rows, guard);
   return cudaGetLastError();
 }
 
@@ -1154,7 +1204,7 @@ static cudaError_t accept_prologue_tc(Handle *h, int f, const SV<TM> &v, const v
     if ((e = cudaFuncSetAttribute(k_acc_factor<TM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf)) !=
         cudaSuccess)
       return e;
-    k_acc_factor<TM><<<1, 256, smf, st>>>(v, n, Einc, d_s, d_d, k, L.LU, L.piv, L.z, h->d_acc_status);
+    k_acc_factor<TM><<<1, 256, smf, st>>>(v, n, Einc, d_s, d_d, k, L.LU, L.piv, L.z, h->d_acc_status, false);
     h->nlaunch += 1;
   }
   const size_t smi = sizeof(double2) * ((size_t)k * k + k + (size_t)INV_COLS * k);
@@ -1164,7 +1214,7 @@ static cudaError_t accept_prologue_tc(Handle *h, int f, const SV<TM> &v, const v
   k_W_init<<<dim3((unsigned)((h->ldm + 255) / 256), (unsigned)k), 256, 0, st>>>(L.W, h->ldm, n, z, k);
   h->nlaunch += 2;
   if ((e = launch_f64tc_wgemm(h, f, k, L.V, X, x32, h->ldm, d_s, L.W)) != cudaSuccess) return e;
-  k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, st>>>(v, n, rows, d_s, k, L.A, rows);
+  k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, st>>>(v, n, rows, d_s, k, L.A, rows, nullptr);
   h->nlaunch += 1;
   return cudaGetLastError();
 }
@@ -1214,7 +1264,7 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   }
   dim3 g((unsigned)((n + 1 + RU_T - 1) / RU_T), (unsigned)((rows + RU_T - 1) / RU_T));
   cudaEvent_t t0 = timing_mark(h, st);
-  k_rank_update<<<g, 256, 0, st>>>(q.M64, h->ldm, rows, n + 1, L.A, rows, L.W, h->ldm, k);
+  k_rank_update<<<g, 256, 0, st>>>(q.M64, h->ldm, rows, n + 1, L.A, rows, L.W, h->ldm, k, nullptr);
   const double cells = (double)rows * (double)(n + 1);
   timing_close(h, t0, T_UPDATE, 8.0 * k * cells, 2.0 * 16.0 * cells + 16.0 * k * (double)(rows + n + 1), 0.0, st);
   h->nlaunch += 4;
@@ -1226,12 +1276,23 @@ cudaError_t launch_accept_raw(double2 *M, long ldm, long n, int E, const double2
                               double2 *W, int *status, cudaStream_t stream) {
   const long rows = n + E;
   if (k <= 0) return cudaSuccess;
-  const SV<double2> v{M, ldm, M + n, ldm, M + (size_t)n * ldm, ldm};
-  cudaError_t e = accept_prologue<double2>(v, n, E, ldm, Einc, d_s, d_d, k, LU, piv, z, A, W, status, stream);
+  const SV<double2> v = checked(SV<double2>{M, ldm, M + n, ldm, M + (size_t)n * ldm, ldm}, n, E);
+  cudaError_t e =
+      accept_prologue<double2>(v, n, E, ldm, Einc, d_s, d_d, k, LU, piv, z, A, W, status, stream, nullptr, 0, true);
   if (e != cudaSuccess) return e;
   dim3 g((unsigned)((n + 1 + RU_T - 1) / RU_T), (unsigned)((rows + RU_T - 1) / RU_T));
-  k_rank_update<<<g, 256, 0, stream>>>(M, ldm, rows, n + 1, A, rows, W, ldm, k);
+  k_rank_update<<<g, 256, 0, stream>>>(M, ldm, rows, n + 1, A, rows, W, ldm, k, status);
   return cudaGetLastError();
+}
+
+cudaError_t bounds_read_fp64(long long out[4], bool reset) {
+#ifdef PNGF_BOUNDS_CHECK
+  return bounds_read_tu(out, reset);
+#else
+  (void)reset;
+  for (int q = 0; q < 4; ++q) out[q] = 0;
+  return cudaSuccess;
+#endif
 }
 
 cudaError_t launch_commit(Handle *h, int c) {

@@ -91,6 +91,7 @@ struct Freq {
 struct Lane {
   cudaStream_t stream = nullptr;  // own stream (several lanes only)
   cudaEvent_t done = nullptr;
+  cudaEvent_t upd = nullptr;      // after this lane's last persistent update (several lanes only)
   double2 *A = nullptr;           // (N+E) x acc_cap, column-major (ld = N+E)
   double2 *W = nullptr;           // acc_cap x ldm row-major
   double2 *LU = nullptr;          // acc_cap^2
@@ -342,6 +343,13 @@ cudaError_t launch_drift_rows(Handle *h, int f, const int *d_rows, int nr, const
 // Writes frequency f's synthetic G (n x n column-major, leading dimension ldg);
 // colmax: n scratch words.
 cudaError_t launch_synth_G(Handle *h, int f, double2 *G, long ldg, unsigned long long *colmax);
+// Writes frequency f's synthetic NF2FF rows ((E-1) x n row-major) into rows.
+cudaError_t launch_synth_gobj(Handle *h, int f, double2 *rows);
+// Amplitude of the synthetic NF2FF rows: kappa eta0 dx dy dz with kappa = 32,
+// the broadside far-field weight of one edge's current (see pngf_synth_gobj).
+inline double synth_gobj_amplitude(double dx, double dy, double dz) {
+  return 32.0 * 3.767303134118051e02 * dx * dy * dz;
+}
 // ---- FP64-accurate update on the tensor cores (kernels_f64tc.cu) ----
 int f64tc_max_k();
 size_t f64tc_op_cols();  // row pitch of the A slices (elements)
@@ -359,6 +367,13 @@ inline int persistent_grid(const Handle *h, int ntiles, int nsm) {
   const int g = h->building && h->lanes.size() > 1 && nsm > 2 * kReservedSMs ? nsm - kReservedSMs : nsm;
   return ntiles < g ? ntiles : g;
 }
+// The frequency lanes' persistent M updates run one after another (each
+// fills every SM and is HBM-bound, so running them side by side only makes
+// them share the memory system, while their tiles' pipelines lose depth):
+// before its update, lane f's stream waits for lane f-1's last update; the
+// lanes' other kernels (factor, W, operand slicing) still overlap them.
+cudaError_t chain_update_wait(Handle *h, int f, cudaStream_t st);
+cudaError_t chain_update_done(Handle *h, int f, cudaStream_t st);
 cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W);
 // W[:, 0:N] -= Vneg X[s, 0:N] on the tensor cores (FP64-accurate): Vneg k x k
 // column-major, X rows s of the state (complex64 when x32, pitch ldx).
@@ -367,7 +382,10 @@ cudaError_t launch_f64tc_wgemm(Handle *h, int f, int k, const double2 *Vneg, con
 // Commits P and the tile map on the device for candidate c of the batch.
 cudaError_t launch_commit(Handle *h, int c);
 // The accept kernels on caller-supplied buffers (no handle): scratch LU (k^2),
-// piv (k), z (k), A ((n+E) x k), W (k x ldm), status (1, sticky).
+// piv (k), z (k), A ((n+E) x k), W (k x ldm), status (1, zero on entry). The
+// factor kernel checks the edge list (indices in [0, n), signs +-1) and sets
+// *status to PNGF_ERR_ARG, or to PNGF_ERR_SINGULAR for a singular K; the W,
+// gather and update kernels then return without touching M.
 cudaError_t launch_accept_raw(double2 *M, long ldm, long n, int E, const double2 *Einc, const int *d_s,
                               const signed char *d_d, int k, double2 *LU, int *piv, double2 *z, double2 *A,
                               double2 *W, int *status, cudaStream_t stream);

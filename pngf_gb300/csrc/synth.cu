@@ -1,4 +1,4 @@
-// Synthetic G generated on the device.
+// Synthetic G (and its NF2FF rows) generated on the device.
 //
 // The same recipe as the host generator in gfile.cpp (pngf_synth_G): the
 // free-space dyadic Helmholtz Green's function between Yee edge centres in
@@ -136,7 +136,36 @@ __global__ void k_synth_finish(double2 *__restrict__ G, long ldg, SynthGeo g,
   }
 }
 
+// The NF2FF rows of the synthetic G (the recipe of pngf_synth_gobj): row 1
+// (theta polarisation at broadside) amp on x-directed edges, row 2 (phi) amp
+// on y-directed edges, each entry times 1 + 1e-3 q, q the complex Gaussian of
+// the pair {e, n + row}; any further rows zero.
+__global__ void k_synth_gobj(double2 *__restrict__ rows, int nrows, SynthGeo g, double amp) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int row = blockIdx.y;
+  if (e >= g.n || row >= nrows) return;
+  const int dir = e < g.nx ? 0 : 1;
+  double2 v = make_double2(0.0, 0.0);
+  if (row < 2 && dir == row) {
+    const double2 q = pair_gaussian(g.seed, (uint64_t)e, (uint64_t)(g.n + row));
+    v = make_double2(amp * (1.0 + 1e-3 * q.x), amp * (1e-3 * q.y));
+  }
+  rows[(size_t)row * g.n + e] = v;
+}
+
 }  // namespace
+
+cudaError_t launch_synth_gobj(Handle *h, int f, double2 *rows) {
+  if (h->E <= 1) return cudaSuccess;
+  SynthGeo g{};
+  g.n = h->n;
+  g.nx = h->nx;
+  g.seed = h->f[f].synth_seed;
+  const dim3 grid((unsigned)((h->n + 255) / 256), (unsigned)(h->E - 1));
+  k_synth_gobj<<<grid, 256, 0, h->stream>>>(rows, h->E - 1, g, synth_gobj_amplitude(h->cfg.dx, h->cfg.dy, h->cfg.dz));
+  h->nlaunch += 1;
+  return cudaGetLastError();
+}
 
 cudaError_t launch_synth_G(Handle *h, int f, double2 *G, long ldg, unsigned long long *colmax) {
   const Freq &q = h->f[f];

@@ -13,7 +13,9 @@ import re
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libpngf_gb300.so")
+# PNGF_BOUNDS_CHECK=1 selects the bounds-checked build (libpngf_gb300_bc.so)
+LIB_PATH = os.path.join(HERE, "libpngf_gb300_bc.so" if os.environ.get("PNGF_BOUNDS_CHECK") == "1"
+                        else "libpngf_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "pngf_gb300.h")
 
 PNGF_OK = 0
@@ -100,6 +102,7 @@ def load():
         "pngf_config_default": (V, [P, I, I, I, P]),
         "pngf_num_edges": (L_, [I, I, I, I]),
         "pngf_synth_G": (I, [I, I, I, I, D, D, D, D, D, C.c_ulonglong, P, L_]),
+        "pngf_synth_gobj": (I, [I, I, I, I, D, D, D, C.c_ulonglong, P]),
         "pngf_write_G_file": (I, [C.c_char_p, L_, I, P, L_, P]),
         "pngf_read_G_file": (I, [C.c_char_p, L_, I, P, L_, P]),
         "pngf_create": (I, [P, P]),
@@ -123,6 +126,7 @@ def load():
         "pngf_drift_check": (I, [P, I, P]),
         "pngf_drift_check_freq": (I, [P, I, I, P]),
         "pngf_autotune": (I, [P, P]),
+        "pngf_bounds_check_report": (I, [P, P, I]),
         "pngf_set_eval_form": (I, [P, I]),
         "pngf_accept_edges_noalloc": (I, [P, L_, L_, I, P, P, P, I, P, P]),
         "pngf_refresh": (I, [P]),
@@ -186,6 +190,16 @@ def synth_G(tiles_x, tiles_y, freq_hz, seed=1, eps_r=2.25, cells=3, dx=0.01 / 60
     if rc:
         raise PngfError(rc, "pngf_synth_G")
     return G
+
+
+def synth_gobj(tiles_x, tiles_y, seed=1, cells=3, dx=0.01 / 60, dy=0.01 / 60, dz=0.01 / 180):
+    """The synthetic G's two NF2FF rows (2 x N complex128, row-major)."""
+    n = num_edges(tiles_x, tiles_y, cells, cells)
+    rows = np.empty((2, n), dtype=np.complex128)
+    rc = load().pngf_synth_gobj(tiles_x, tiles_y, cells, cells, dx, dy, dz, seed, _ptr(rows))
+    if rc:
+        raise PngfError(rc, "pngf_synth_gobj")
+    return rows
 
 
 def write_G_file(path, G, gobj_rows=None, num_eobj=3):

@@ -32,15 +32,20 @@ def cases():
 _G_CACHE = {}
 
 
-def case_G(case, built_lib):
-    """(Gs, gobj_rows) for a golden case, from the library's generator."""
-    from pngf_gb300 import lib
+def case_G(case, built_lib=None):
+    """(Gs, gobj_rows) for a golden case: the inputs the reference ran on, from
+    the oracle's generator (oracle/synth.c) -- G per frequency and the two
+    synthetic NF2FF rows (zero rows for a case recorded without them)."""
+    from oracle import synth
     key = case["name"]
     if key not in _G_CACHE:
-        Gs = [np.ascontiguousarray(lib.synth_G(case["tiles"], case["tiles"], f, seed=case["g_seed"]))
-              for f in case["freqs"]]
+        Gs = [synth.synth_G(case["tiles"], case["tiles"], f, seed=case["g_seed"]) for f in case["freqs"]]
         n = Gs[0].shape[0]
-        _G_CACHE[key] = (Gs, [np.zeros((2, n), dtype=np.complex128) for _ in Gs])
+        if case.get("gobj") == "synth":
+            rows = synth.synth_gobj(case["tiles"], case["tiles"], seed=case["g_seed"])
+        else:
+            rows = np.zeros((2, n), dtype=np.complex128)
+        _G_CACHE[key] = (Gs, [rows for _ in Gs])
     return _G_CACHE[key]
 
 

@@ -3,12 +3,15 @@
 Builds the reference optimizer from its own sources (oracle/Makefile target
 ``ref``, which compiles pngf-opt/{pngfopt,linalg,magichat,acmetime}.hpp in
 place from the reference tree), writes synthetic G files in the acmefdfd
-layout with the library's generator, runs the reference DBS on each case and
-copies its log here. ``cases.json`` records each case and checksums of the G
-matrices it used, so that a test can confirm the generator reproduces them.
+layout with the oracle's generator (oracle/synth.c: G plus the two NF2FF
+rows, so that the directivity half of the objective and the far-field rows of
+R are exercised), runs the reference DBS on each case and copies its log here.
+``cases.json`` records each case and checksums of the G matrices and NF2FF
+rows it used, so that a test can confirm the generators reproduce them.
 
-Usage: python tests/golden/make_golden.py [--ref /path/to/reference]
-Needs the built libpngf_gb300.so (only its CPU-side G generator is used).
+Usage: python tests/golden/make_golden.py --ref <reference tree> [--only NAME ...]
+(or set PNGF_REFERENCE). The 21x21 x 5-frequency case needs about 15 GB of
+host memory and a few minutes of the reference's OpenBLAS time.
 """
 from __future__ import annotations
 
@@ -25,9 +28,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from pngf_gb300 import lib  # noqa: E402
+from oracle import synth  # noqa: E402
 
 FREQS_REF = [25.0e9, 27.5e9, 30.0e9, 32.5e9, 35.0e9]
+FREQS_WIDE = [27.0e9, 28.5e9, 30.0e9, 31.5e9, 33.0e9]
 
 CASES = [
     # The CPU-runnable plain case: 7x7 tiles, one frequency at 30 GHz, 50%-fill
@@ -44,6 +48,11 @@ CASES = [
     # A longer single-tile prefix at 11x11 with three frequencies.
     dict(name="single_11x11_f3_seed2", tiles=11, freqs=[28e9, 30e9, 32e9], seed=2, init="random",
          mode="single", max_evals=300),
+    # The benchmarked wideband workload itself: 21x21 tiles (N = 8064), five
+    # frequencies 27-33 GHz, single-tile hat, 50%-fill start from seed 1; the
+    # first 120 evaluations.
+    dict(name="single_21x21_f5_seed1", tiles=21, freqs=FREQS_WIDE, seed=1, init="random", mode="single",
+         max_evals=120),
 ]
 
 
@@ -55,20 +64,34 @@ def g_checksum(G):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("PNGF_REFERENCE"),
+                    help="the reference tree (default: $PNGF_REFERENCE)")
+    ap.add_argument("--only", nargs="*", help="regenerate only these cases (cases.json keeps the others)")
     a = ap.parse_args()
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "REF=" + a.ref], check=True)
+    if not a.ref:
+        ap.error("give --ref <reference tree> or set PNGF_REFERENCE")
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", "synth", "REF=" + a.ref], check=True)
     exe = os.path.join(ROOT, "oracle", "_ref", "pngf_ref")
+    meta_path = os.path.join(HERE, "cases.json")
+    old = {}
+    if a.only and os.path.exists(meta_path):
+        old = {c["name"]: c for c in json.load(open(meta_path))}
     meta = []
-    with tempfile.TemporaryDirectory() as tmp:
-        for c in CASES:
+    for c in CASES:
+        if a.only and c["name"] not in a.only:
+            if c["name"] in old:
+                meta.append(old[c["name"]])
+            continue
+        with tempfile.TemporaryDirectory() as tmp:
             gfiles, sums = [], []
+            rows = synth.synth_gobj(c["tiles"], c["tiles"], seed=1)
             for i, f in enumerate(c["freqs"]):
-                G = lib.synth_G(c["tiles"], c["tiles"], f, seed=1)
+                G = synth.synth_G(c["tiles"], c["tiles"], f, seed=1)
                 p = os.path.join(tmp, "%s_%d.bin" % (c["name"], i))
-                lib.write_G_file(p, G)
+                synth.write_G_file(p, G, rows)
                 gfiles.append(p)
                 sums.append(g_checksum(G))
+                del G
             cmd = [exe, "--tiles", str(c["tiles"]), str(c["tiles"]), "--freq",
                    ",".join(repr(float(f)) for f in c["freqs"]), "--seed", str(c["seed"]), "--init", c["init"],
                    "--mode", c["mode"], "--max-evals", str(c["max_evals"]),
@@ -77,9 +100,10 @@ def main():
                 cmd += ["--gfile", p]
             env = dict(os.environ, OMP_NUM_THREADS=os.environ.get("OMP_NUM_THREADS", "4"))
             out = subprocess.run(cmd, check=True, capture_output=True, text=True, env=env).stdout
-            print(c["name"], out.strip().splitlines()[-1])
-            meta.append(dict(c, g_seed=1, eps_r=2.25, g_checksums=sums))
-    with open(os.path.join(HERE, "cases.json"), "w") as fh:
+            print(c["name"], out.strip().splitlines()[-1], flush=True)
+        meta.append(dict(c, g_seed=1, eps_r=2.25, gobj="synth", g_checksums=sums,
+                         gobj_checksum=g_checksum(rows)))
+    with open(meta_path, "w") as fh:
         json.dump(meta, fh, indent=1)
 
 
