@@ -242,6 +242,216 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Long-K form of the complex64 update (deferred flushes, build chunks):
+// T -= A_real B_real^T with the 3xTF32 products taken from separate hi and lo
+// operands -- per K stage the MMAs A_hi.B_hi, A_hi.B_lo and A_lo.B_hi -- so
+// that each operand element crosses L2 once per tile instead of being stored
+// and read twice as in the [A_hi | A_hi | A_lo] layout (a third less operand
+// traffic), and with 128 x 256 output tiles (two TMEM accumulators of 256
+// columns) so that each operand byte feeds twice the MMA work of a 128 x 128
+// tile. At a flush's rank (K = 2r = 384 real columns at r = 192) the
+// operands are re-read from L2 for every tile, which sets the pace; the T tile
+// itself never enters shared memory: the epilogue writes -acc in 128 x 32
+// boxes and the TMA unit adds them into T in L2 (cp.reduce.async.bulk.tensor
+// .add), so T is read and written once in HBM and no staging slot waits on a
+// load of T.
+//
+// Warp 0 issues the TMA loads of the K stages (hi parts and lo parts on their
+// own full barriers, so that A_hi.B_hi starts while the lo parts land), warp
+// 1 allocates TMEM and issues the MMAs, warps 2-9 are the epilogue in two
+// groups of four (one warp per TMEM lane quarter), each group with one 16 KB
+// staging box: a group reads 32 accumulator columns, writes them negated into
+// its box, and its issuing thread adds the box into T; the groups alternate
+// over the eight 32-column chunks of a tile. Every wait is bounded; on a
+// timeout the kernel records an error code, drains its copies and reduces,
+// frees its TMEM and returns.
+constexpr int LK_BN = 256;                             // fp32 output columns per tile (MMA N)
+constexpr uint32_t LK_A = TC_BM * TC_BK * 4;           // one K stage of A_hi or A_lo (16 KB)
+constexpr uint32_t LK_B = LK_BN * TC_BK * 4;           // one K stage of B_hi or B_lo (32 KB)
+constexpr uint32_t LK_HALF = LK_A + LK_B;              // hi (or lo) part of a stage
+constexpr uint32_t LK_STAGE = 2 * LK_HALF;             // 96 KB
+constexpr int LK_ST = 2;                               // stages in the ring
+constexpr uint32_t LK_STG = TC_BM * 128;               // a 128 x 32-float box of the epilogue output
+constexpr int LK_EPI_WARPS = 8;                        // two groups of four
+constexpr int LK_CHUNKS = LK_BN / 32;                  // 32-column chunks per tile
+constexpr int LK_THREADS = 64 + 32 * LK_EPI_WARPS;     // producer, MMA, epilogue
+constexpr int LK_NBARS = 3 * LK_ST + 8;                // full_hi, full_lo, empty; acc_full/empty; stg_full/free
+constexpr size_t LK_SMEM = 1024 + (size_t)LK_ST * LK_STAGE + 2 * LK_STG + 256;
+static_assert(LK_SMEM <= kTcSmemOptin && LK_NBARS * 8 + 4 <= 256, "long-K shared memory and barrier block");
+constexpr uint32_t LK_IDESC =
+    (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(LK_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+
+__global__ void __launch_bounds__(LK_THREADS, 1)
+    k_tc_update_longk(const __grid_constant__ CUtensorMap tmAhi, const __grid_constant__ CUtensorMap tmAlo,
+                      const __grid_constant__ CUtensorMap tmBhi, const __grid_constant__ CUtensorMap tmBlo,
+                      const __grid_constant__ CUtensorMap tmD, int cols, int ncb, int ntiles, int nkb, int *err) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                          ~static_cast<uintptr_t>(1023));
+  const uint32_t sbase = smem_u32(base);
+  constexpr uint32_t stg_off = LK_ST * LK_STAGE;  // staging boxes after the ring (1024-aligned)
+  uint64_t *bars = reinterpret_cast<uint64_t *>(base + stg_off + 2 * LK_STG);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + LK_NBARS);
+  const uint32_t bar0 = smem_u32(bars);
+  auto full_hi = [&](int s) { return bar0 + 8u * (uint32_t)s; };
+  auto full_lo = [&](int s) { return bar0 + 8u * (uint32_t)(LK_ST + s); };
+  auto empty = [&](int s) { return bar0 + 8u * (uint32_t)(2 * LK_ST + s); };
+  auto acc_full = [&](int b) { return bar0 + 8u * (uint32_t)(3 * LK_ST + b); };
+  auto acc_empty = [&](int b) { return bar0 + 8u * (uint32_t)(3 * LK_ST + 2 + b); };
+  auto stg_full = [&](int g) { return bar0 + 8u * (uint32_t)(3 * LK_ST + 4 + g); };
+  auto stg_free = [&](int g) { return bar0 + 8u * (uint32_t)(3 * LK_ST + 6 + g); };
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t_begin = (int)(((long long)ntiles * blockIdx.x) / gridDim.x);
+  const int t_end = (int)(((long long)ntiles * (blockIdx.x + 1)) / gridDim.x);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < LK_ST; ++s) {
+      mbar_init(full_hi(s), 1);
+      mbar_init(full_lo(s), 1);
+      mbar_init(empty(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(acc_full(b), 1);
+      mbar_init(acc_empty(b), LK_EPI_WARPS);
+      mbar_init(stg_full(b), 4);
+      mbar_init(stg_free(b), 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) tmem_alloc(smem_u32(tslot), 2 * LK_BN);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      bool ok = true;
+      int g = 0;
+      for (int t = t_begin; t < t_end && ok; ++t) {
+        const int rb = t / ncb, cb = t - rb * ncb, m0 = rb * TC_BM, n0 = cb * LK_BN;
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          const int st = g % LK_ST;
+          if (g >= LK_ST && !mbar_wait(empty(st), ((g / LK_ST) - 1) & 1)) { ok = false; break; }
+          const uint32_t sa = sbase + (uint32_t)st * LK_STAGE;
+          mbar_expect_tx(full_hi(st), LK_HALF);
+          tma_load_2d(sa, &tmAhi, kb * TC_BK, m0, full_hi(st));
+          tma_load_2d(sa + LK_A, &tmBhi, kb * TC_BK, n0, full_hi(st));
+          mbar_expect_tx(full_lo(st), LK_HALF);
+          tma_load_2d(sa + LK_HALF, &tmAlo, kb * TC_BK, m0, full_lo(st));
+          tma_load_2d(sa + LK_HALF + LK_A, &tmBlo, kb * TC_BK, n0, full_lo(st));
+        }
+      }
+      if (!ok) atomicExch(err, 41);
+      // Drain: every stage issued has landed before the CTA can exit.
+      for (int q = g > LK_ST ? g - LK_ST : 0; q < g; ++q) {
+        if (!mbar_wait(full_hi(q % LK_ST), (q / LK_ST) & 1)) atomicExch(err, 44);
+        if (!mbar_wait(full_lo(q % LK_ST), (q / LK_ST) & 1)) atomicExch(err, 44);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      bool ok = true;
+      int g = 0;
+      for (int t = t_begin; t < t_end && ok; ++t) {
+        const int li = t - t_begin, b = li & 1;
+        if (li >= 2 && !mbar_wait(acc_empty(b), ((li >> 1) - 1) & 1)) { ok = false; break; }
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * LK_BN);
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          const int st = g % LK_ST;
+          const uint32_t sa = sbase + (uint32_t)st * LK_STAGE;
+          const uint64_t ahi = sw128_desc(sa), bhi = sw128_desc(sa + LK_A);
+          const uint64_t alo = sw128_desc(sa + LK_HALF), blo = sw128_desc(sa + LK_HALF + LK_A);
+          if (!mbar_wait(full_hi(st), (g / LK_ST) & 1)) { ok = false; break; }
+          tc_fence_after();
+#pragma unroll
+          for (int kk = 0; kk < TC_BK / 8; ++kk)  // K = 8 tf32 = 32 bytes per MMA: +2 in 16-byte units
+            mma_tf32(acc, ahi + 2 * kk, bhi + 2 * kk, LK_IDESC, (kb | kk) != 0);
+          if (!mbar_wait(full_lo(st), (g / LK_ST) & 1)) { ok = false; break; }
+          tc_fence_after();
+#pragma unroll
+          for (int kk = 0; kk < TC_BK / 8; ++kk) {
+            mma_tf32(acc, ahi + 2 * kk, blo + 2 * kk, LK_IDESC, 1u);
+            mma_tf32(acc, alo + 2 * kk, bhi + 2 * kk, LK_IDESC, 1u);
+          }
+          mma_commit(empty(st));
+        }
+        if (ok) mma_commit(acc_full(b));
+      }
+      if (!ok) atomicExch(err, 42);
+    }
+    __syncwarp();
+  } else {
+    const int ew = warp - 2;          // 0..7
+    const int grp = ew >> 2;          // group 0: warps 2-5, group 1: warps 6-9
+    const int q = warp & 3;           // TMEM lanes 32q .. 32q+31 (each group covers all four)
+    const int r = q * 32 + lane;      // row of the tile
+    const bool issuer = (q == 0) && lane == 0;  // one thread per group issues its reductions
+    const uint32_t stg = sbase + stg_off + (uint32_t)grp * LK_STG;
+    unsigned char *stg_row = base + stg_off + (size_t)grp * LK_STG + (size_t)r * 128;
+    bool ok = true;
+    int n = 0;  // chunks this group has written (its staging box's uses)
+    for (int t = t_begin; t < t_end && ok; ++t) {
+      const int li = t - t_begin, b = li & 1, rb = t / ncb, cb = t - rb * ncb;
+      ok = __all_sync(0xffffffffu, mbar_wait(acc_full(b), (li >> 1) & 1));
+      if (!ok) break;
+      tc_fence_after();
+      for (int c = grp; c < LK_CHUNKS; c += 2, ++n) {
+        uint32_t v[32];
+        const uint32_t ta = tmem + (uint32_t)(b * LK_BN + c * 32) + ((uint32_t)(q * 32) << 16);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) tmem_ld8_nowait(ta + (uint32_t)(8 * u), v + 8 * u);
+        tmem_wait_ld();
+        if (c + 2 >= LK_CHUNKS) {  // this warp's last read of the accumulator
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(acc_empty(b));
+        }
+        // the box is free once the group's previous reduction has read it
+        if (n > 0) {
+          ok = __all_sync(0xffffffffu, mbar_wait(stg_free(grp), (n - 1) & 1));
+          if (!ok) break;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {  // 16-byte unit u of the row, 128-byte swizzle
+          float4 x;
+          x.x = -__uint_as_float(v[4 * u]);
+          x.y = -__uint_as_float(v[4 * u + 1]);
+          x.z = -__uint_as_float(v[4 * u + 2]);
+          x.w = -__uint_as_float(v[4 * u + 3]);
+          *reinterpret_cast<float4 *>(stg_row + 16 * (u ^ (r & 7))) = x;
+        }
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(stg_full(grp));
+        if (issuer) {
+          if (!mbar_wait(stg_full(grp), n & 1)) {
+            ok = false;
+          } else {
+            const int x0 = cb * LK_BN + 32 * c;
+            if (x0 < cols) tma_reduce_add_2d(&tmD, stg, x0, rb * TC_BM);  // rows past T are clipped
+            bulk_commit();
+            bulk_wait_read_all();
+            mbar_arrive(stg_free(grp));
+          }
+        }
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) break;
+      }
+    }
+    if (issuer) bulk_wait_all();  // every reduction of this group has completed
+    if (!ok && lane == 0) atomicExch(err, 43);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 2 * LK_BN);
+  }
+}
+
 // A_op rows i < n: 3xTF32 segments of the interleaved real form of A[i, :].
 // One block per 32 rows: A's 32 x k block is read column-coalesced into shared
 // memory, then the rows of A_op are written along K.
@@ -353,6 +563,101 @@ __global__ void k_build_Bop_f(const float2 *__restrict__ Vt, int rcap, long n, i
     v = seg == 1 ? to_tf32(b - hi) : hi;
   }
   Bop[(size_t)jp * ldk + c] = v;
+}
+
+// Operands of the long-K kernel: the interleaved real forms of A and B split
+// into TF32 hi and lo parts, stored as separate matrices (rows x K2, K2 = 2k
+// padded to 32, zeros past 2k): A_hi at Ahi, A_lo at Alo, B likewise. From
+// the pending factors (A = U, W[r][j] = Vt[j][r]) ...
+__global__ void k_build_hl_Af(const float2 *__restrict__ U, int rcap, long n, int k, int K2, float *__restrict__ Ahi,
+                              float *__restrict__ Alo) {
+  const long i = (long)blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || c >= K2) return;
+  float hi = 0.f, lo = 0.f;
+  if (c < 2 * k) {
+    const float2 a = U[(size_t)i * rcap + (c >> 1)];
+    const float x = (c & 1) ? a.y : a.x;
+    hi = to_tf32(x);
+    lo = to_tf32(x - hi);
+  }
+  Ahi[(size_t)i * K2 + c] = hi;
+  Alo[(size_t)i * K2 + c] = lo;
+}
+
+__global__ void k_build_hl_Bf(const float2 *__restrict__ Vt, int rcap, long n, int k, int K2, float *__restrict__ Bhi,
+                              float *__restrict__ Blo) {
+  const long jp = (long)blockIdx.y;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (jp >= 2 * n || c >= K2) return;
+  float hi = 0.f, lo = 0.f;
+  if (c < 2 * k) {
+    const float2 wv = Vt[(size_t)(jp >> 1) * rcap + (c >> 1)];
+    float b;
+    if ((jp & 1) == 0) b = (c & 1) ? -wv.y : wv.x;  // Re out: Re A Re W - Im A Im W
+    else b = (c & 1) ? wv.x : wv.y;                 // Im out: Re A Im W + Im A Re W
+    hi = to_tf32(b);
+    lo = to_tf32(b - hi);
+  }
+  Bhi[(size_t)jp * K2 + c] = hi;
+  Blo[(size_t)jp * K2 + c] = lo;
+}
+
+// ... and from an accept's FP64 factors A ((n+E) x k, column-major, lda) and W
+// (k x ldw row-major), rounded to FP32 first as k_build_Aop / k_build_Bop do,
+// staged through shared memory like them (coalesced reads of A's columns and
+// W's rows, rows of the operands written along K).
+__global__ void __launch_bounds__(256) k_build_hl_A(const double2 *__restrict__ A, long lda, long n, int k, int K2,
+                                                    float *__restrict__ Ahi, float *__restrict__ Alo) {
+  extern __shared__ double2 bsm[];  // k x (BO_ROWS + 1)
+  const long i0 = (long)blockIdx.x * BO_ROWS;
+  for (int idx = threadIdx.x; idx < k * BO_ROWS; idx += blockDim.x) {
+    const int r = idx / BO_ROWS, ii = idx - r * BO_ROWS;
+    bsm[r * (BO_ROWS + 1) + ii] = i0 + ii < n ? A[(size_t)r * lda + i0 + ii] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < BO_ROWS * K2; idx += blockDim.x) {
+    const int ii = idx / K2, c = idx - ii * K2;
+    const long i = i0 + ii;
+    if (i >= n) break;
+    float hi = 0.f, lo = 0.f;
+    if (c < 2 * k) {
+      const double2 a = bsm[(c >> 1) * (BO_ROWS + 1) + ii];
+      const float x = (float)((c & 1) ? a.y : a.x);
+      hi = to_tf32(x);
+      lo = to_tf32(x - hi);
+    }
+    Ahi[(size_t)i * K2 + c] = hi;
+    Alo[(size_t)i * K2 + c] = lo;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_build_hl_B(const double2 *__restrict__ W, long ldw, long n, int k, int K2,
+                                                    float *__restrict__ Bhi, float *__restrict__ Blo) {
+  extern __shared__ double2 bsm[];  // k x (BO_COLS + 1)
+  const long j0 = (long)blockIdx.x * BO_COLS;
+  for (int idx = threadIdx.x; idx < k * BO_COLS; idx += blockDim.x) {
+    const int r = idx / BO_COLS, jj = idx - r * BO_COLS;
+    bsm[r * (BO_COLS + 1) + jj] = j0 + jj < n ? W[(size_t)r * ldw + j0 + jj] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 2 * BO_COLS * K2; idx += blockDim.x) {
+    const int jl = idx / K2, c = idx - jl * K2;
+    const long jp = 2 * j0 + jl;
+    if (jp >= 2 * n) break;
+    float hi = 0.f, lo = 0.f;
+    if (c < 2 * k) {
+      const double2 wv = bsm[(c >> 1) * (BO_COLS + 1) + (jl >> 1)];
+      double b;
+      if ((jp & 1) == 0) b = (c & 1) ? -wv.y : wv.x;
+      else b = (c & 1) ? wv.x : wv.y;
+      const float x = (float)b;
+      hi = to_tf32(x);
+      lo = to_tf32(x - hi);
+    }
+    Bhi[(size_t)jp * K2 + c] = hi;
+    Blo[(size_t)jp * K2 + c] = lo;
+  }
 }
 
 // FP64 part of the complex64 accept: y_i -= sum_r A[i,r] W[r,N] (i < N) and
@@ -663,6 +968,7 @@ cudaError_t launch_c64_tc(Handle *h, int f, int Kt, int rank) {
   }
   const int ncb = (dcols + bn - 1) / bn, ntiles = ncb * (int)((n + TC_BM - 1) / TC_BM);
   const int grid = persistent_grid(h, ntiles, g_c64_sms);
+  if ((e = chain_update_wait(h, f, st)) != cudaSuccess) return e;  // one lane's update at a time
   cudaEvent_t t0 = timing_mark(h, st);
   // long K (build chunks, flushes of deferred updates): one staged tile of T
   // and a deeper operand ring
@@ -679,6 +985,7 @@ cudaError_t launch_c64_tc(Handle *h, int f, int Kt, int rank) {
   else
     e = longk ? go(k_tc_update<128, 1>, C64Tile<128, 1>::SMEM) : go(k_tc_update<128, 2>, C64Tile<128, 2>::SMEM);
   if (e != cudaSuccess) return e;
+  if ((e = chain_update_done(h, f, st)) != cudaSuccess) return e;
   const double cells = (double)n * (double)n;  // complex entries of T updated
   timing_close(h, t0, T_UPDATE, 8.0 * rank * cells,
                2.0 * 8.0 * cells + 4.0 * Kt * ((double)h->aop_rows + (double)h->bop_rows), 0.0, st);
@@ -699,6 +1006,56 @@ cudaError_t launch_side_update(Handle *h, int f, int k) {
 
 int kt_of(int rank) { return (6 * rank + TC_BK - 1) / TC_BK * TC_BK; }
 
+// Ranks from which updates take the long-K kernel (build chunks, flushes).
+constexpr int kLongKRank = 64;
+int k2_of(int rank) { return (2 * rank + TC_BK - 1) / TC_BK * TC_BK; }
+bool use_longk(const Handle *h, int rank) { return rank >= kLongKRank && 2 * k2_of(rank) <= h->kt_cap; }
+
+// T32 -= A_real B_real^T with the long-K kernel, from the hi / lo operands the
+// caller built in the lane's operand buffers (A_hi at Aop, A_lo after it; B
+// likewise; leading dimension K2).
+cudaError_t launch_c64_tc_longk(Handle *h, int f, int rank) {
+  Freq &q = h->f[f];
+  const long n = h->n;
+  cudaError_t e = get_encoder();
+  if (e != cudaSuccess) return e;
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
+  const int K2 = k2_of(rank);
+  const int dcols = (int)(2 * n);
+  float *Ahi = L.Aop, *Alo = L.Aop + (size_t)h->aop_rows * K2;
+  float *Bhi = L.Bop, *Blo = L.Bop + (size_t)h->bop_rows * K2;
+  CUtensorMap mahi, malo, mbhi, mblo, md;
+  if ((e = make_map(&mahi, Ahi, h->aop_rows, K2, K2, TC_BM)) != cudaSuccess ||
+      (e = make_map(&malo, Alo, h->aop_rows, K2, K2, TC_BM)) != cudaSuccess ||
+      (e = make_map(&mbhi, Bhi, h->bop_rows, K2, K2, LK_BN)) != cudaSuccess ||
+      (e = make_map(&mblo, Blo, h->bop_rows, K2, K2, LK_BN)) != cudaSuccess ||
+      (e = make_map(&md, reinterpret_cast<const float *>(q.T32), n, dcols, 2 * h->ldm, TC_BM)) != cudaSuccess)
+    return e;
+  if (g_c64_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_c64_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_c64_sms <= 0) g_c64_sms = 1;
+  }
+  const int ncb = (dcols + LK_BN - 1) / LK_BN, ntiles = ncb * (int)((n + TC_BM - 1) / TC_BM);
+  const int grid = persistent_grid(h, ntiles, g_c64_sms);
+  if ((e = cudaFuncSetAttribute(k_tc_update_longk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LK_SMEM)) !=
+      cudaSuccess)
+    return e;
+  if ((e = chain_update_wait(h, f, st)) != cudaSuccess) return e;
+  cudaEvent_t t0 = timing_mark(h, st);
+  k_tc_update_longk<<<grid, LK_THREADS, LK_SMEM, st>>>(mahi, malo, mbhi, mblo, md, dcols, ncb, ntiles, K2 / TC_BK,
+                                                        h->d_tc_err);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = chain_update_done(h, f, st)) != cudaSuccess) return e;
+  const double cells = (double)n * (double)n;  // complex entries of T updated
+  timing_close(h, t0, T_UPDATE, 8.0 * rank * cells,
+               2.0 * 8.0 * cells + 2.0 * 4.0 * K2 * ((double)h->aop_rows + (double)h->bop_rows), 0.0, st);
+  h->nlaunch += 1;
+  return cudaSuccess;
+}
+
 }  // namespace
 
 cudaError_t launch_c64_update(Handle *h, int f, int k) {
@@ -712,6 +1069,18 @@ cudaError_t launch_c64_update(Handle *h, int f, int k) {
   const size_t sma = sizeof(double2) * (size_t)k * (BO_ROWS + 1), smb = sizeof(double2) * (size_t)k * (BO_COLS + 1);
   if ((e = cudaFuncSetAttribute(k_build_Aop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma)) != cudaSuccess)
     return e;
+  if (use_longk(h, k)) {  // build chunks: hi / lo operands for the long-K kernel
+    const int K2 = k2_of(k);
+    if ((e = cudaFuncSetAttribute(k_build_hl_A, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma)) !=
+        cudaSuccess)
+      return e;
+    k_build_hl_A<<<(unsigned)((n + BO_ROWS - 1) / BO_ROWS), 256, sma, st>>>(L.A, rows, n, k, K2, L.Aop,
+                                                                             L.Aop + (size_t)h->aop_rows * K2);
+    k_build_hl_B<<<(unsigned)((n + BO_COLS - 1) / BO_COLS), 256, smb, st>>>(L.W, h->ldm, n, k, K2, L.Bop,
+                                                                             L.Bop + (size_t)h->bop_rows * K2);
+    h->nlaunch += 2;
+    return launch_c64_tc_longk(h, f, k);
+  }
   k_build_Aop<<<(unsigned)((n + BO_ROWS - 1) / BO_ROWS), 256, sma, st>>>(L.A, rows, n, k, Kt, h->kt_cap, L.Aop);
   k_build_Bop<<<(unsigned)((n + BO_COLS - 1) / BO_COLS), 256, smb, st>>>(L.W, h->ldm, n, k, Kt, h->kt_cap, L.Bop);
   h->nlaunch += 2;
@@ -727,6 +1096,14 @@ cudaError_t launch_c64_flush(Handle *h, int f) {
   Freq &q = h->f[f];
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
+  if (use_longk(h, rank)) {
+    const int K2 = k2_of(rank);
+    const dim3 ga((unsigned)((K2 + 127) / 128), (unsigned)n), gb((unsigned)((K2 + 127) / 128), (unsigned)(2 * n));
+    k_build_hl_Af<<<ga, 128, 0, st>>>(q.U, h->defer_cap, n, rank, K2, L.Aop, L.Aop + (size_t)h->aop_rows * K2);
+    k_build_hl_Bf<<<gb, 128, 0, st>>>(q.Vt, h->defer_cap, n, rank, K2, L.Bop, L.Bop + (size_t)h->bop_rows * K2);
+    h->nlaunch += 2;
+    return launch_c64_tc_longk(h, f, rank);
+  }
   const dim3 ga((unsigned)((Kt + 127) / 128), (unsigned)n), gb((unsigned)((Kt + 127) / 128), (unsigned)(2 * n));
   k_build_Aop_f<<<ga, 128, 0, st>>>(q.U, h->defer_cap, n, rank, Kt, h->kt_cap, L.Aop);
   k_build_Bop_f<<<gb, 128, 0, st>>>(q.Vt, h->defer_cap, n, rank, Kt, h->kt_cap, L.Bop);

@@ -79,6 +79,16 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap *map, uint32_t sr
                "r"(src), "r"(c0), "r"(c1)
                : "memory");
 }
+// Tiled 2-D reduction of a shared-memory box into global memory: every
+// element of the box is added to the tensor's element in place (the tensor
+// map's type, f32 here; the add is done by the TMA unit in L2). Bulk
+// async-group, like tma_store_2d; out-of-range rows and columns are clipped.
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap *map, uint32_t src, int c0, int c1) {
+  asm volatile("cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(src), "r"(c0), "r"(c1)
+               : "memory");
+}
 // Plain bulk copy of `bytes` (a multiple of 16; both addresses 16-byte
 // aligned) from global to shared memory, completing on the mbarrier.
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
