@@ -443,6 +443,12 @@ const char *pngf_prop_last_error(const pngf_prop *p);
  * steps (batch train_batch, learning rate lr) on the recorded samples. */
 int pngf_dbs_set_proposal(pngf_dbs *d, pngf_prop *p, int topk, int train_every, int train_steps, int train_batch,
                           float lr);
+/* Which improving flip of an exactly evaluated proposal batch is accepted:
+ * PNGF_PROP_BEST (default) the largest improvement, PNGF_PROP_FIRST the first
+ * improving flip in the network's predicted order (a less greedy descent). */
+#define PNGF_PROP_BEST 0
+#define PNGF_PROP_FIRST 1
+int pngf_dbs_set_proposal_rule(pngf_dbs *d, int rule);
 
 #ifdef __cplusplus
 }

@@ -105,6 +105,7 @@ struct pngf_dbs {
   // learned proposals (optional)
   pngf_prop *prop = nullptr;
   int topk = 0, train_every = 0, train_steps = 0, train_batch = 32;
+  int prop_rule = PNGF_PROP_BEST;  // which improving flip of an exact batch is accepted
   float train_lr = 1e-3f;
   long prop_steps = 0, prop_hits = 0, full_passes = 0;
   // the batch being evaluated: hat state at its start, its draws, staging
@@ -172,9 +173,11 @@ void log_row(pngf_dbs *d, const Cand &c, int acc, double F, const double *perf, 
 }
 
 // Proposal-driven decision (no reference counterpart): the network's top-k
-// single-tile flips are evaluated exactly and the best improving one is
-// accepted; if none improves, a full exact pass over every candidate tile
-// follows, and if that finds nothing either the design is a local minimum.
+// single-tile flips are evaluated exactly and an improving one is accepted --
+// the best (PNGF_PROP_BEST) or the first in predicted order (PNGF_PROP_FIRST);
+// if none improves, a full exact pass over every candidate tile follows (in
+// predicted order), and if that finds nothing either the design is a local
+// minimum.
 int proposal_step(pngf_dbs *d, int *accepted) {
   pngf::Handle *h = d->h;
   const int map_sz = h->map_sz, nf = h->cfg.num_freq, mf = h->cfg.max_flips;
@@ -200,7 +203,7 @@ int proposal_step(pngf_dbs *d, int *accepted) {
     if ((rc = pngf_prop_record(d->prop, list.data(), gains.data(), n))) return rc;
     *best = -1;
     for (int i = 0; i < n; ++i)
-      if (o.F[i] < d->F_best && (*best < 0 || o.F[i] < o.F[*best])) *best = i;
+      if (o.F[i] < d->F_best && (*best < 0 || (d->prop_rule == PNGF_PROP_BEST && o.F[i] < o.F[*best]))) *best = i;
     for (int i = 0; i < n; ++i) {
       Cand c{list[i], 1, {list[i], 0, 0, 0}};
       log_row(d, c, i == *best, o.F[i], o.perf.data() + (size_t)i * nf * 3, nf);
@@ -224,14 +227,12 @@ int proposal_step(pngf_dbs *d, int *accepted) {
   }
   pngf::EvalOut o;
   int best = -1;
+  std::vector<int> full(elig);  // the fallback pass, in predicted order when there are predictions
   if (pngf_prop_num_samples(d->prop) > 0) {
     std::vector<float> pred(map_sz);
     if ((rc = pngf_prop_predict(d->prop, pred.data()))) return rc;
-    std::vector<int> order(elig);
-    const int k = std::min<int>(d->topk, (int)order.size());
-    std::partial_sort(order.begin(), order.begin() + k, order.end(),
-                      [&](int a, int b) { return pred[a] < pred[b]; });
-    order.resize(k);
+    std::stable_sort(full.begin(), full.end(), [&](int a, int b) { return pred[a] < pred[b]; });
+    std::vector<int> order(full.begin(), full.begin() + std::min<int>(d->topk, (int)full.size()));
     if ((rc = run_batch(order, o, &best))) return rc;
     if (best >= 0) {
       ++d->prop_hits;
@@ -239,8 +240,8 @@ int proposal_step(pngf_dbs *d, int *accepted) {
     }
   }
   ++d->full_passes;
-  if ((rc = run_batch(elig, o, &best))) return rc;
-  if (best >= 0) return take(elig, o, best);
+  if ((rc = run_batch(full, o, &best))) return rc;
+  if (best >= 0) return take(full, o, best);
   d->converged = d->done = true;
   return PNGF_OK;
 }
@@ -429,6 +430,12 @@ int pngf_dbs_set_proposal(pngf_dbs *d, pngf_prop *p, int topk, int train_every, 
   d->train_steps = train_steps;
   d->train_batch = train_batch > 0 ? train_batch : 32;
   d->train_lr = lr > 0 ? lr : 1e-3f;
+  return PNGF_OK;
+}
+
+int pngf_dbs_set_proposal_rule(pngf_dbs *d, int rule) {
+  if (!d || (rule != PNGF_PROP_BEST && rule != PNGF_PROP_FIRST)) return PNGF_ERR_ARG;
+  d->prop_rule = rule;
   return PNGF_OK;
 }
 

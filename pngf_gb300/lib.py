@@ -25,6 +25,7 @@ ERRORS = {1: "PNGF_ERR_ARG", 2: "PNGF_ERR_CUDA", 3: "PNGF_ERR_NOMEM", 4: "PNGF_E
 PREC_FP64, PREC_C64 = 0, 1
 F64_TENSOR, F64_SIMT = 0, 1
 DBS_SYMMETRIC, DBS_SINGLE = 0, 1
+PROP_BEST, PROP_FIRST = 0, 1
 INIT_EMPTY, INIT_RANDOM = 0, 1
 MAX_FREQ = 16
 TUNE_MAX = 8
@@ -157,6 +158,7 @@ def load():
         "pngf_prop_forward_backward": (I, [P, P, I, P, P, P, P, P]),
         "pngf_prop_last_error": (C.c_char_p, [P]),
         "pngf_dbs_set_proposal": (I, [P, P, I, I, I, I, C.c_float]),
+        "pngf_dbs_set_proposal_rule": (I, [P, I]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -551,6 +553,7 @@ class Proposal:
             pass
 
 
-def dbs_set_proposal(dbs: Dbs, prop, topk=64, train_every=0, train_steps=0, train_batch=32, lr=1e-3):
+def dbs_set_proposal(dbs: Dbs, prop, topk=64, train_every=0, train_steps=0, train_batch=32, lr=1e-3, rule=PROP_BEST):
     dbs.hd._chk(dbs.hd.L.pngf_dbs_set_proposal(dbs.d, prop.p if prop else None, topk, train_every, train_steps,
                                               train_batch, lr), "pngf_dbs_set_proposal")
+    dbs.hd._chk(dbs.hd.L.pngf_dbs_set_proposal_rule(dbs.d, rule), "pngf_dbs_set_proposal_rule")

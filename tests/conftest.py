@@ -52,3 +52,26 @@ def case_G(case, built_lib=None):
 def golden_log(name):
     from oracle.dbs import parse_ref_log
     return parse_ref_log(os.path.join(GOLDEN, name + ".log"))
+
+
+def force_port_tiles(tm, tiles_x, tiles_y):
+    """The tiles pngf-opt/main.cpp:209-218 forces around the lumped port at the
+    map centre (source tile and the tiles above and below it empty, the tiles
+    left and right of it metal); DBS never flips them. Random test designs
+    get the same, so that the port is not shorted (|S11| = 1, an objective
+    with a 0/0 directivity)."""
+    mx, my = (tiles_x - 1) // 2, (tiles_y - 1) // 2
+    tm = [int(v) for v in tm]
+    tm[my * tiles_x + mx - 1] = 1
+    tm[my * tiles_x + mx + 1] = 1
+    tm[my * tiles_x + mx] = 0
+    tm[(my - 1) * tiles_x + mx] = 0
+    tm[(my + 1) * tiles_x + mx] = 0
+    return tm
+
+
+def free_tiles(tiles_x, tiles_y):
+    """Tiles a DBS candidate may flip: all but the source tile and its two
+    forced metal neighbours (main.cpp:358-359)."""
+    mx, my = (tiles_x - 1) // 2, (tiles_y - 1) // 2
+    return [t for t in range(tiles_x * tiles_y) if not (t // tiles_x == my and t % tiles_x in (mx - 1, mx, mx + 1))]

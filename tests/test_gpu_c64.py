@@ -4,13 +4,13 @@ accept test in FP64) against the plain FP64 form on the same G and design.
 
 Tolerances: the prepared state differs only by the complex64 rounding of T
 (relative 2^-24); tensor-core accepts keep T within 5e-6 of max|T|;
-newEobj within 1e-5 relative, F within 1e-7 relative (1e-6 after accepted
-4-tile flips); a DBS run's objective
-within 1e-3 relative of the FP64 run's."""
+newEobj within 1e-5 relative, F within 1e-7 relative (1e-4 after accepts:
+the flip undoing an accept cancels in its NF2FF outputs); a DBS run's
+objective within 1e-3 relative of the FP64 run's."""
 import numpy as np
 import pytest
 
-from conftest import case_G
+from conftest import case_G, force_port_tiles, free_tiles
 
 pytestmark = pytest.mark.gpu
 
@@ -37,7 +37,7 @@ def test_c64_eval_and_tensor_core_accept_match_fp64(max_flips, cases, built_lib)
     Gs, gobj = case_G(c, built_lib)
     a = c["tiles"]
     rng = np.random.default_rng(7)
-    tm = [int(v) for v in rng.integers(0, 2, a * a)]
+    tm = force_port_tiles(rng.integers(0, 2, a * a), a, a)
     h64, h32 = handles(c, Gs, gobj, tm, max_flips)
     n = h64.n
     for f in range(len(Gs)):
@@ -47,10 +47,8 @@ def test_c64_eval_and_tensor_core_accept_match_fp64(max_flips, cases, built_lib)
         assert np.abs(M32[:n, :n] - M64[:n, :n]).max() <= 2e-7 * scale
         # R and Eobj stay FP64; the two handles build them with different chunkings
         np.testing.assert_allclose(M32[n:], M64[n:], rtol=0, atol=1e-11 * np.abs(M64[n:]).max())
-    # DBS never flips the source tile (main.cpp:358-359): metal on the port
-    # edges shorts the port (|S11| = 1), an ill-conditioned case.
-    mid = (a - 1) // 2
-    pool = [t for t in range(a * a) if t != mid * a + mid]
+    # DBS never flips the source tile or its forced neighbours (main.cpp:358-359)
+    pool = free_tiles(a, a)
     cands = [[int(t) for t in rng.choice(pool, size=max_flips, replace=False)] for _ in range(40)]
     eo64, F64 = h64.eval_candidates(cands)
     eo32, F32 = h32.eval_candidates(cands)
@@ -72,7 +70,10 @@ def test_c64_eval_and_tensor_core_accept_match_fp64(max_flips, cases, built_lib)
             np.testing.assert_allclose(e32, e64, rtol=1e-5, atol=1e-5 * np.abs(e64).max())
         eo64, F64 = h64.eval_candidates(cands)
         eo32, F32 = h32.eval_candidates(cands)
-        np.testing.assert_allclose(F32, F64, rtol=1e-6)  # accepted 4-tile flips carry ~1e-7 of c64 rounding
+        # after accepts T carries ~1e-6 of max|T| (complex64 rounding through K^-1
+        # and the 3xTF32 products); the flip that undoes an accept cancels in its
+        # NF2FF outputs (measured: 2e-5 relative in F on this case)
+        np.testing.assert_allclose(F32, F64, rtol=1e-4)
 
 
 def test_drift_check_measures_complex64_error(cases, built_lib):
@@ -82,11 +83,10 @@ def test_drift_check_measures_complex64_error(cases, built_lib):
     Gs, gobj = case_G(c, built_lib)
     a = c["tiles"]
     rng = np.random.default_rng(4)
-    tm = [int(v) for v in rng.integers(0, 2, a * a)]
+    tm = force_port_tiles(rng.integers(0, 2, a * a), a, a)
     h64, h32 = handles(c, Gs, gobj, tm, 1)
     n = h64.n
-    mid = (a - 1) // 2
-    pool = [t for t in range(a * a) if t != mid * a + mid]
+    pool = free_tiles(a, a)
     for step in range(3):
         cands = [[int(t)] for t in rng.choice(pool, size=8, replace=False)]
         h64.eval_candidates(cands)
@@ -119,4 +119,6 @@ def test_c64_dbs_reaches_fp64_objective(cases, built_lib):
     F64, F32 = res[lib.PREC_FP64].F_best, res[lib.PREC_C64].F_best
     assert abs(F32 - F64) <= 1e-3 * abs(F64)
     s32 = res[lib.PREC_C64]
-    assert s32.drift_checks >= 1 and 0 < s32.drift_max < 1e-4
+    assert s32.drift_checks >= 1 and 0 < s32.drift_max < 1e-2
+    # a drift above the tolerance rebuilt the state from G
+    assert s32.drift_max <= 1e-4 or s32.refreshes >= 1

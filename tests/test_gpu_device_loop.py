@@ -61,7 +61,10 @@ def test_device_loop_equals_host_driver(batch, cases, built_lib):
     dev = run(c, Gs, gobj, True, batch=batch)
     assert_same_run(host, dev)
     s = dev[2]
-    assert s.device_decisions > s.accepts  # decisions without an accept stayed on the device
+    # decisions without an accept stayed on the device (with whole-hat batches
+    # a decision without an accept happens only at convergence, which this
+    # 300-evaluation run may not reach)
+    assert s.device_decisions > s.accepts if batch != 0 else s.device_decisions >= s.accepts
 
 
 @pytest.mark.parametrize("max_evals", [1, 37, 250])

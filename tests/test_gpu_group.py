@@ -33,7 +33,7 @@ def prepared(a, freqs, prec, synth, tm, **kw):
         if synth:
             h.load_G_synth(f, seed=1)
         else:
-            h.load_G(f, np.ascontiguousarray(lib.synth_G(a, a, fr, seed=1)), None)
+            h.load_G(f, np.ascontiguousarray(lib.synth_G(a, a, fr, seed=1)), lib.synth_gobj(a, a, seed=1))
     mid = (a - 1) // 2
     h.set_tile_map(tm)
     h.set_source_port(mid, mid, 1, 2)

@@ -8,7 +8,7 @@ objective value within 1e-10 relative (S11 / D within 1e-10 relative or
 import numpy as np
 import pytest
 
-from conftest import case_G, golden_log
+from conftest import case_G, force_port_tiles, free_tiles, golden_log
 
 pytestmark = pytest.mark.gpu
 
@@ -94,7 +94,7 @@ def test_eval_and_accept_match_oracle(cases, built_lib):
     a = c["tiles"]
     geo = Geometry(a, a)
     rng = np.random.default_rng(5)
-    tm = list(rng.integers(0, 2, a * a))
+    tm = force_port_tiles(rng.integers(0, 2, a * a), a, a)
     mid = (a - 1) // 2
     P = geo.compute_P(tm)
     port = geo.port_indices(mid, mid, 1, 2)
@@ -112,7 +112,8 @@ def test_eval_and_accept_match_oracle(cases, built_lib):
         e, v = h.eobj(f)
         np.testing.assert_allclose(e, refs[f].Eobj, rtol=1e-11, atol=1e-14)
         np.testing.assert_allclose(v, consts[f][:3], rtol=1e-13, atol=1e-16)
-    cands = [list(rng.choice(a * a, size=rng.integers(1, 5), replace=False)) for _ in range(40)]
+    pool = free_tiles(a, a)
+    cands = [[int(t) for t in rng.choice(pool, size=rng.integers(1, 5), replace=False)] for _ in range(40)]
     eo, F = h.eval_candidates(cands)
     for i, cand in enumerate(cands):
         s, d = geo.flip_set(tm, P, cand)
