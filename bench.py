@@ -340,7 +340,7 @@ def autotune_on(h, mode_single=True):
 
 
 def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), train_evals=1500, train_steps=600,
-                     topk=64, state_only=0, batch=0, device_loop=False, online_every=0):
+                     topk=64, state_only=0, batch=0, device_loop=False, online_every=0, rule=0):
     """Wall time to the converged objective: plain FP64 DBS (reference order,
     run until the hat is empty) against the proposal + complex64 form, whose
     network is trained only on plain complex64 runs from other seeds. The
@@ -403,7 +403,8 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
     d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, batch=0, drift_every=32, drift_tol=1e-4)
     # online_every > 0: 20 more training steps on the run's own exact pairs every
     # that many proposal steps (0: the network trained beforehand is kept)
-    lib.dbs_set_proposal(d, prop, topk=topk, train_every=online_every, train_steps=20, train_batch=32, lr=1e-3)
+    lib.dbs_set_proposal(d, prop, topk=topk, train_every=online_every, train_steps=20, train_batch=32, lr=1e-3,
+                         rule=rule)
     torch.cuda.synchronize()
     t_prep = time.perf_counter() - t0
     h.timing_enable(True)
@@ -427,6 +428,7 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
                            "converged": bool(s.converged), "drift_max": s.drift_max,
                            "drift_checks": s.drift_checks, "refreshes": s.refreshes,
                            "eval_form": tune32["eval_form"], "update_cols": tune32["update"][tune32["update_form"]]["cols"],
+                           "accept_rule": "first improving in predicted order" if rule else "best improving",
                            "reached_target": t_reach is not None,
                            "training": {"seeds": list(train_seeds), "collect_s": t_collect, "train_s": t_train,
                                         "samples": samples, "pairs": pairs, "final_loss": loss,
@@ -456,16 +458,18 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
 FREQS_GROUP = [28.0e9, 30.0e9, 32.0e9]
 
 
-def group_member(tiles, seed, max_evals, batch, local):
+def group_member(tiles, seed, max_evals, batch, local, device_loop=False):
     """One instance of the group workload: complex64 state built on the tensor
     cores, G generated on the device and not kept (state_only), single-tile
-    DBS from the 50%-fill design of `seed`, its kernel forms autotuned."""
+    DBS from the 50%-fill design of `seed`, its kernel forms autotuned;
+    device_loop: its decisions drawn and taken on the device."""
     from pngf_gb300 import lib
     h = lib.Handle(tiles, tiles, FREQS_GROUP, precision=lib.PREC_C64, max_flips=1, device=local,
                    c64_build=lib.BUILD_C64, state_only=1)
     for f in range(len(FREQS_GROUP)):
         h.load_G_synth(f, seed=seed)
-    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, max_evals=max_evals, batch=batch)
+    d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, max_evals=max_evals, batch=batch,
+                device_loop=device_loop)
     h.autotune()
     return h, d
 
@@ -506,26 +510,33 @@ def group_bench(a, local, n_check=8):
     t_seq = time.perf_counter() - t0
     seq_logs = logs_of(runs)
     close(runs)
-    runs = [group_member(sizes[i], i + 1, a.group_evals, a.group_batch, local) for i in range(nc)]
-    g = lib.Group([d for _, d in runs], use_graphs=True)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    g.run()
-    torch.cuda.synchronize()
-    t_grp = time.perf_counter() - t0
-    same = all(np.array_equal(l1["tile"], l0["tile"]) and np.array_equal(l1["accept"], l0["accept"]) and
-               np.array_equal(l1["F"].view(np.uint64), l0["F"].view(np.uint64)) and F1 == F0
-               for (l0, F0), (l1, F1) in zip(seq_logs, logs_of(runs)))
-    g.close()
-    close(runs)
-    out["check"] = {"instances": nc, "sequential_s": t_seq, "group_s": t_grp, "speedup": t_seq / t_grp,
-                    "logs_identical": bool(same)}
+    check = {"instances": nc, "sequential_s": t_seq}
+    for mode, dev in (("host_drawn", False), ("device_resident", True)):
+        runs = [group_member(sizes[i], i + 1, a.group_evals, a.group_batch, local, device_loop=dev)
+                for i in range(nc)]
+        g = lib.Group([d for _, d in runs], use_graphs=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.run()
+        torch.cuda.synchronize()
+        t_grp = time.perf_counter() - t0
+        same = all(np.array_equal(l1["tile"], l0["tile"]) and np.array_equal(l1["accept"], l0["accept"]) and
+                   np.array_equal(l1["F"].view(np.uint64), l0["F"].view(np.uint64)) and F1 == F0
+                   for (l0, F0), (l1, F1) in zip(seq_logs, logs_of(runs)))
+        st = g.stats()
+        check[mode] = {"group_s": t_grp, "speedup": t_seq / t_grp, "logs_identical": bool(same),
+                       "rounds": st["rounds"], "graph_captures": st["captures"]}
+        g.close()
+        close(runs)
+    out["check"] = check
     # the whole group
     free0 = torch.cuda.mem_get_info(local)[0]
     t0 = time.perf_counter()
-    runs = [group_member(sizes[i], i + 1, a.group_evals, a.group_batch, local) for i in range(a.instances)]
+    runs = [group_member(sizes[i], i + 1, a.group_evals, a.group_batch, local, device_loop=True)
+            for i in range(a.instances)]
     torch.cuda.synchronize()
     out["setup_s"] = time.perf_counter() - t0
+    out["decisions"] = "device-resident: one graph of the instances' decision loops (draw, evaluate, decide)"
     out["device_gb_held"] = (free0 - torch.cuda.mem_get_info(local)[0]) / 1e9
     out["edges_total"] = int(sum(h.n for h, _ in runs))
     g = lib.Group([d for _, d in runs], use_graphs=True)

@@ -389,7 +389,14 @@ int pngf_dbs_end(pngf_dbs *d);
  * so), then takes each member's decision exactly as pngf_dbs_step would and
  * launches its accept without waiting. Each member's accepted flips,
  * objectives and log equal those of stepping it alone with pngf_dbs_step.
- * Members with an attached proposal network are refused. */
+ * Members with an attached proposal network are refused.
+ * If the members run device-resident decisions (pngf_dbs_set_device_loop,
+ * all of them or none), the group holds one CUDA graph whose root nodes are
+ * the members' decision loops (each a WHILE node: draw, evaluate, decide on
+ * the device), captured once and rebuilt only when a member's buffers or
+ * kernel forms change; one pngf_group_step launches it, every unfinished
+ * member decides on the device until its next accept, and the group then
+ * performs those accepts on the members' streams without waiting. */
 typedef struct pngf_group pngf_group;
 typedef struct pngf_group_stats {
   long rounds;          /* group steps that launched work */

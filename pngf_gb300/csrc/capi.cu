@@ -58,12 +58,14 @@ static int lanes_fork(Handle *h) {
 }
 
 cudaError_t chain_update_wait(Handle *h, int f, cudaStream_t st) {
-  if (h->lanes.size() < 2 || f <= 0 || (size_t)f >= h->lanes.size()) return cudaSuccess;
+  // builds keep their lanes concurrent: a chunk's update overlaps the other
+  // lanes' capacitance LUs, and its narrower tile shapes (k = 32) gain from it
+  if (h->building || h->lanes.size() < 2 || f <= 0 || (size_t)f >= h->lanes.size()) return cudaSuccess;
   return cudaStreamWaitEvent(st, h->lanes[f - 1].upd, 0);
 }
 
 cudaError_t chain_update_done(Handle *h, int f, cudaStream_t st) {
-  if (h->lanes.size() < 2 || f < 0 || (size_t)f >= h->lanes.size()) return cudaSuccess;
+  if (h->building || h->lanes.size() < 2 || f < 0 || (size_t)f >= h->lanes.size()) return cudaSuccess;
   return cudaEventRecord(h->lanes[f].upd, st);
 }
 

@@ -348,43 +348,55 @@ int batch_finish(pngf_dbs *d, int *accepted, bool sync_accept) {
 
 // One DBS decision on the device-resident loop: decisions without an accept
 // run on the GPU; an accept is performed here as on the host path.
+// Takes a device-loop launch's outcome: the counters and, on an accept, the
+// accept itself on the host path (not waited for: the next launch's decide
+// kernel reads the tensor-core error flag before it decides). *more = the
+// run continues without an accept (another launch is due).
+int device_after(pngf_dbs *d, const pngf::DevLoopResult &r, int *accepted, bool *more) {
+  pngf::Handle *h = d->h;
+  *more = false;
+  d->evals = r.evals;
+  d->accepts = r.accepts;
+  d->launched = r.launched;
+  d->F_best = r.F_best;
+  d->converged = r.converged != 0;
+  d->done = r.done != 0;
+  ++d->dev_launches;
+  d->dev_decisions += r.decisions;
+  if (r.err == 2) {
+    d->done = true;
+    cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->stream);
+    return pngf::set_error(h, PNGF_ERR_TIMEOUT,
+                           "tensor-core update gave up waiting (code " + std::to_string(r.tc_code) + ")");
+  }
+  if (r.err) {
+    d->done = true;
+    return pngf::set_error(h, PNGF_ERR_ARG, "invalid candidate produced by the driver");
+  }
+  if (r.accepted) {
+    int rc;
+    if ((rc = pngf::adopt_device_batch(h, r.nc, r.j, r.tiles, r.nflip)) ||
+        (rc = pngf::accept_cand_async(h, r.j, r.k, false)))
+      return rc;
+    if (accepted) *accepted = 1;
+    const double fb = d->F_best;
+    if ((rc = drift_after_accept(d))) return rc;
+    if (!(d->F_best == fb) && (rc = pngf::devloop_set_fbest(h, d->dev, d->F_best))) return rc;
+    return PNGF_OK;
+  }
+  *more = !d->done;
+  return PNGF_OK;
+}
+
 int device_step(pngf_dbs *d, int *accepted) {
   pngf::Handle *h = d->h;
   pngf::DevLoopLog lg{d->lg_tile, d->lg_acc, d->lg_F, d->lg_Fb, d->lg_perf};
-  while (!d->done) {
+  bool more = !d->done;
+  while (more) {
     pngf::DevLoopResult r{};
     int rc = pngf::devloop_run(h, d->dev, &r, &lg);
     if (rc) return rc;
-    d->evals = r.evals;
-    d->accepts = r.accepts;
-    d->launched = r.launched;
-    d->F_best = r.F_best;
-    d->converged = r.converged != 0;
-    d->done = r.done != 0;
-    ++d->dev_launches;
-    d->dev_decisions += r.decisions;
-    if (r.err == 2) {
-      d->done = true;
-      cudaMemsetAsync(h->d_tc_err, 0, sizeof(int), h->stream);
-      return pngf::set_error(h, PNGF_ERR_TIMEOUT,
-                             "tensor-core update gave up waiting (code " + std::to_string(r.tc_code) + ")");
-    }
-    if (r.err) {
-      d->done = true;
-      return pngf::set_error(h, PNGF_ERR_ARG, "invalid candidate produced by the driver");
-    }
-    if (r.accepted) {
-      // not waited for: the next launch's decide kernel reads the tensor-core
-      // error flag before it decides
-      if ((rc = pngf::adopt_device_batch(h, r.nc, r.j, r.tiles, r.nflip)) ||
-          (rc = pngf::accept_cand_async(h, r.j, r.k, false)))
-        return rc;
-      if (accepted) *accepted = 1;
-      const double fb = d->F_best;
-      if ((rc = drift_after_accept(d))) return rc;
-      if (!(d->F_best == fb) && (rc = pngf::devloop_set_fbest(h, d->dev, d->F_best))) return rc;
-      return PNGF_OK;
-    }
+    if ((rc = device_after(d, r, accepted, &more))) return rc;
   }
   return PNGF_OK;
 }
@@ -608,6 +620,10 @@ struct pngf_group {
   cudaGraphExec_t exec = nullptr;
   std::vector<long> key;  // per member: batch size and staging addresses the graph was captured with
   long graph_nodes_launches = 0;
+  // device-resident members: one graph holding every member's decision loop
+  bool device = false;
+  cudaGraph_t dgraph = nullptr;
+  cudaGraphExec_t dexec = nullptr;
   pngf_group_stats st{};
 };
 
@@ -615,6 +631,8 @@ namespace {
 
 void group_release(pngf_group *g) {
   if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->dexec) cudaGraphExecDestroy(g->dexec);
+  if (g->dgraph) cudaGraphDestroy(g->dgraph);
   for (cudaEvent_t e : g->ready)
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : g->join)
@@ -666,6 +684,69 @@ int group_capture(pngf_group *g, const std::vector<char> &on) {
   return PNGF_OK;
 }
 
+// Device-resident members: one graph whose root nodes are the members' WHILE
+// loops (independent branches; each member draws, evaluates and decides on
+// the device until its next accept), captured once and rebuilt only if a
+// member's buffers or kernel forms change. A finished member's loop exits on
+// its first iteration.
+int group_device_build(pngf_group *g) {
+  if (g->dexec) cudaGraphExecDestroy(g->dexec);
+  if (g->dgraph) cudaGraphDestroy(g->dgraph);
+  g->dexec = nullptr;
+  g->dgraph = nullptr;
+  cudaError_t e = cudaGraphCreate(&g->dgraph, 0);
+  if (e != cudaSuccess) return group_err(g, e, "cudaGraphCreate");
+  for (pngf_dbs *d : g->m) {
+    const int rc = pngf::devloop_add_to_graph(d->h, d->dev, g->dgraph);
+    if (rc) return rc;
+  }
+  if ((e = cudaGraphInstantiate(&g->dexec, g->dgraph, 0)) != cudaSuccess)
+    return group_err(g, e, "instantiation of the members' decision loops");
+  ++g->st.captures;
+  return PNGF_OK;
+}
+
+int group_device_step(pngf_group *g, int *active) {
+  const size_t nm = g->m.size();
+  int rc, n_on = 0;
+  bool stale = !g->dexec;
+  for (pngf_dbs *d : g->m) {
+    n_on += !d->done;
+    stale = stale || !pngf::devloop_key_current(d->h, d->dev);
+  }
+  if (n_on > 0) {
+    if (stale && (rc = group_device_build(g))) return rc;
+    cudaError_t e = cudaSuccess;
+    for (size_t i = 0; i < nm && e == cudaSuccess; ++i) {  // after each member's earlier accepts
+      pngf::Handle *h = g->m[i]->h;
+      if ((rc = pngf::devloop_prepare(h, g->m[i]->dev))) return rc;
+      if ((e = cudaEventRecord(g->ready[i], h->stream)) == cudaSuccess) e = cudaStreamWaitEvent(g->s0, g->ready[i], 0);
+    }
+    if (e == cudaSuccess) e = cudaGraphLaunch(g->dexec, g->s0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->s0);
+    if (e != cudaSuccess) return group_err(g, e, "graph launch of the members' decision loops");
+    ++g->st.rounds;
+    ++g->st.graph_launches;
+    for (size_t i = 0; i < nm; ++i) {  // outcomes and accepts, in member order
+      pngf_dbs *d = g->m[i];
+      if (d->done) continue;
+      pngf::Handle *h = d->h;
+      const long l0 = h->nlaunch;
+      pngf::DevLoopLog lg{d->lg_tile, d->lg_acc, d->lg_F, d->lg_Fb, d->lg_perf};
+      pngf::DevLoopResult r{};
+      int acc = 0;
+      bool more = false;
+      if ((rc = pngf::devloop_collect(h, d->dev, &r, &lg)) || (rc = device_after(d, r, &acc, &more))) return rc;
+      g->st.kernel_launches += h->nlaunch - l0;
+      g->st.accepts += acc;
+    }
+  }
+  int left = 0;
+  for (size_t i = 0; i < nm; ++i) left += !g->m[i]->done;
+  if (active) *active = left;
+  return PNGF_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -677,8 +758,9 @@ int pngf_group_create(pngf_dbs *const *members, int count, int use_graphs, pngf_
     if (!members[i]) return PNGF_ERR_ARG;
     if (members[i]->prop && members[i]->topk > 0)
       return pngf::set_error(members[i]->h, PNGF_ERR_UNSUPPORTED, "proposal-driven runs are stepped on their own");
-    if (members[i]->dev)
-      return pngf::set_error(members[i]->h, PNGF_ERR_UNSUPPORTED, "device-loop runs are stepped on their own");
+    if ((members[i]->dev != nullptr) != (members[0]->dev != nullptr))
+      return pngf::set_error(members[i]->h, PNGF_ERR_UNSUPPORTED,
+                             "a group's members all run device-resident decisions or none does");
     for (int j = 0; j < i; ++j)
       if (members[j]->h == members[i]->h)
         return pngf::set_error(members[i]->h, PNGF_ERR_ARG, "two group members share a handle");
@@ -687,6 +769,7 @@ int pngf_group_create(pngf_dbs *const *members, int count, int use_graphs, pngf_
   if (!g) return PNGF_ERR_NOMEM;
   g->m.assign(members, members + count);
   g->graphs = use_graphs != 0;
+  g->device = members[0]->dev != nullptr;
   g->ready.assign(count, nullptr);
   g->join.assign(count, nullptr);
   cudaError_t e = cudaStreamCreateWithFlags(&g->s0, cudaStreamNonBlocking);
@@ -707,6 +790,7 @@ int pngf_group_create(pngf_dbs *const *members, int count, int use_graphs, pngf_
 int pngf_group_step(pngf_group *g, int *active) {
   pngf::TraceRange trace_("pngf_group_step");
   if (!g) return PNGF_ERR_ARG;
+  if (g->device) return group_device_step(g, active);
   const size_t nm = g->m.size();
   std::vector<char> on(nm, 0);
   std::vector<long> key(3 * nm, 0);

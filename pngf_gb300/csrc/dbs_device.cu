@@ -284,17 +284,18 @@ void capture_key(const Handle *h, uintptr_t *key) {
 
 size_t draw_smem(const DevLoop *L) { return sizeof(MtState) + sizeof(int) * (size_t)L->c.hat_entries; }
 
-int graph_build(Handle *h, DevLoop *L) {
-  graph_release(L);
-  PNGF_CUDA(h, cudaGraphCreate(&L->graph, 0));
-  PNGF_CUDA(h, cudaGraphConditionalHandleCreate(&L->c.cond, L->graph, 1, cudaGraphCondAssignDefault));
+// Adds to `graph` a WHILE node (on its own conditional handle, reset to 1 at
+// every launch) whose body is one decision of this loop: draw, edge lists,
+// candidate kernel(s), decide. L->c.cond is left at the new handle.
+int loop_body_build(Handle *h, DevLoop *L, cudaGraph_t graph) {
+  PNGF_CUDA(h, cudaGraphConditionalHandleCreate(&L->c.cond, graph, 1, cudaGraphCondAssignDefault));
   cudaGraphNodeParams np{};
   np.type = cudaGraphNodeTypeConditional;
   np.conditional.handle = L->c.cond;
   np.conditional.type = cudaGraphCondTypeWhile;
   np.conditional.size = 1;
   cudaGraphNode_t node;
-  PNGF_CUDA(h, cudaGraphAddNode(&node, L->graph, nullptr, nullptr, 0, &np));
+  PNGF_CUDA(h, cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np));
   cudaGraph_t body = np.conditional.phGraph_out[0];
   const int cap = L->c.hat_entries;
   const int small = std::min(cap, kSmallBatch);
@@ -329,6 +330,14 @@ int graph_build(Handle *h, DevLoop *L) {
   h->capturing = false;
   h->stream = user;
   PNGF_CUDA(h, e);
+  return PNGF_OK;
+}
+
+int graph_build(Handle *h, DevLoop *L) {
+  graph_release(L);
+  PNGF_CUDA(h, cudaGraphCreate(&L->graph, 0));
+  int rc = loop_body_build(h, L, L->graph);
+  if (rc) return rc;
   PNGF_CUDA(h, cudaGraphInstantiate(&L->exec, L->graph, 0));
   capture_key(h, L->key);
   return PNGF_OK;
@@ -423,19 +432,45 @@ int devloop_set_fbest(Handle *h, DevLoop *L, double F_best) {
   return PNGF_OK;
 }
 
-int devloop_run(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log) {
-  pngf::TraceRange trace_("pngf device decisions");
+bool devloop_key_current(const Handle *h, const DevLoop *L) {
   uintptr_t key[kKeyLen];
   capture_key(h, key);
-  int rc;
-  if (!std::equal(key, key + kKeyLen, L->key) && (rc = graph_build(h, L))) return rc;
+  return std::equal(key, key + kKeyLen, L->key);
+}
+
+int devloop_add_to_graph(Handle *h, DevLoop *L, cudaGraph_t graph) {
+  const cudaGraphConditionalHandle own = L->c.cond;
+  const int rc = loop_body_build(h, L, graph);
+  L->c.cond = own;  // the loop's own graph keeps its handle
+  if (rc == PNGF_OK) capture_key(h, L->key);
+  return rc;
+}
+
+int devloop_prepare(Handle *h, DevLoop *L) {
   DevScalars *dv = reinterpret_cast<DevScalars *>(L->d_rep);
   PNGF_CUDA(h, cudaMemsetAsync(&dv->iters, 0, 3 * sizeof(int), h->stream));
+  return PNGF_OK;
+}
+
+int devloop_collect(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log) { return devloop_read(h, L, r, log, 0); }
+
+int devloop_run(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log) {
+  pngf::TraceRange trace_("pngf device decisions");
+  int rc;
+  if (!devloop_key_current(h, L) && (rc = graph_build(h, L))) return rc;
+  if ((rc = devloop_prepare(h, L))) return rc;
   // one timing span per launch: the decisions' draws, evaluations and scores
   cudaEvent_t t0 = timing_mark(h);
   PNGF_CUDA(h, cudaGraphLaunch(L->exec, h->stream));
   const size_t span = h->pending.size();
   timing_close(h, t0, T_EVAL, 0.0, 0.0, 0.0);
+  return devloop_read(h, L, r, log, span + 1);
+}
+
+// Reads a launch's report (the scalars and the first rows in one copy, the
+// rest in a second) and appends its log rows; span1 = index + 1 of the
+// launch's timing span (0: none).
+int devloop_read(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log, size_t span1) {
   // the scalars and the first rows in one copy; the rest, if any, in a second
   const int rb = log_rec_bytes(L->c.nf);
   const int first_rows = std::min(L->c.log_cap, kReportRows);
@@ -449,7 +484,8 @@ int devloop_run(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log) {
                                  cudaMemcpyDeviceToHost, h->stream));
     PNGF_CUDA(h, cudaStreamSynchronize(h->stream));
   }
-  if (h->pending.size() > span) h->pending[span].x1 = (double)(v.launched - L->launched_seen) * L->c.nf;
+  if (span1 > 0 && h->pending.size() >= span1)
+    h->pending[span1 - 1].x1 = (double)(v.launched - L->launched_seen) * L->c.nf;
   L->launched_seen = v.launched;
   h->nlaunch += (long)v.iters * L->per_iter;
   const int n = v.log_n, pw = 3 * L->c.nf;

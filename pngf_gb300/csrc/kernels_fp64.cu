@@ -46,6 +46,15 @@ __device__ __forceinline__ double2 cfnma(double2 a, double2 b, double2 c) {
 }
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 __device__ __forceinline__ double cabs1(double2 a) { return fabs(a.x) + fabs(a.y); }
+// Pivot key of a complex entry: the bit pattern of |re| + |im| (LAPACK's
+// izamax measure) as an integer -- non-negative doubles order like their bit
+// patterns, so the argmax over a column runs on the integer pipes and only
+// the one add uses GB300's narrow FP64 pipe. A NaN measure gets -1, so that,
+// as with a floating-point compare, it is never chosen.
+__device__ __forceinline__ long long pivot_key(double2 a) {
+  const long long b = __double_as_longlong(cabs1(a));
+  return (b & 0x7FFFFFFFFFFFFFFFll) > 0x7FF0000000000000ll ? -1ll : b;
+}
 __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
   const double den = __fma_rn(b.x, b.x, __dmul_rn(b.y, b.y));
   return make_double2(__ddiv_rn(__fma_rn(a.x, b.x, __dmul_rn(a.y, b.y)), den),
@@ -335,21 +344,21 @@ __device__ int cta_lu(double2 *K, int ld, int k, int *piv, double *red_v, int *r
   if (tid == 0) s_info = 0;
   for (int j = 0; j < k; ++j) {
     if (tid < 32) {  // pivot: largest |re|+|im| (first on ties), as izamax
-      double bv = -1.0;
+      long long bv = -1;
       int bi = j;
       for (int i = j + tid; i < k; i += 32) {
-        const double v = cabs1(K[i + j * ld]);
+        const long long v = pivot_key(K[i + j * ld]);
         if (v > bv) { bv = v; bi = i; }
       }
       for (int o = 16; o; o >>= 1) {
-        const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+        const long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
         const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
         if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
       }
       if (tid == 0) {
         piv[j] = bi;
-        red_v[0] = bv;
-        if (bv == 0.0 && s_info == 0) s_info = j + 1;
+        red_v[0] = bv >= 0 ? __longlong_as_double(bv) : -1.0;
+        if (bv == 0 && s_info == 0) s_info = j + 1;
       }
       if (bi != j)
         for (int c = tid; c < k; c += 32) {
@@ -358,7 +367,7 @@ __device__ int cta_lu(double2 *K, int ld, int k, int *piv, double *red_v, int *r
           K[bi + c * ld] = t;
         }
       __syncwarp();
-      if (bv != 0.0) {
+      if (bv != 0) {
         const double2 r = crecip(K[j + j * ld]);
         for (int i = j + 1 + tid; i < k; i += 32) K[i + j * ld] = cmul(K[i + j * ld], r);
       }
@@ -590,10 +599,10 @@ __global__ void __launch_bounds__(32 * WPC)
   // LU with partial pivoting (izamax: largest |re|+|im|, first on ties).
   int info = 0, piv_l = lane;
   for (int j = 0; j < k; ++j) {
-    double bv = -1.0;
+    long long bv = -1;
     int bi = j;
     if (lane >= j && lane < k) {
-      const double v = cabs1(K[lane + j * ld]);
+      const long long v = pivot_key(K[lane + j * ld]);
       if (v > bv) {
         bv = v;
         bi = lane;
@@ -601,7 +610,7 @@ __global__ void __launch_bounds__(32 * WPC)
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
-      const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
       if (ov > bv || (ov == bv && oi < bi)) {
         bv = ov;
@@ -610,7 +619,7 @@ __global__ void __launch_bounds__(32 * WPC)
     }
     const int p = bi;
     if (lane == j) piv_l = p;
-    if (bv == 0.0 && info == 0) info = j + 1;
+    if (bv == 0 && info == 0) info = j + 1;
     if (p != j) {
       if (lane < k) {
         const double2 t = K[j + lane * ld];
@@ -619,7 +628,7 @@ __global__ void __launch_bounds__(32 * WPC)
       }
       __syncwarp();
     }
-    if (bv != 0.0) {
+    if (bv != 0) {
       const double2 r = crecip(K[j + j * ld]);
       if (lane > j && lane < k) K[lane + j * ld] = cmul(K[lane + j * ld], r);
     }

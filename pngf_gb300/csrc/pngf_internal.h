@@ -288,6 +288,16 @@ int devloop_create(Handle *h, const DevLoopConfig &cfg, DevLoop **out);
 // Runs decisions on the device until an accept, the end of the run or a
 // launch limit; appends the log rows and reports the state.
 int devloop_run(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log);
+// Many loops in one graph (groups): adds this loop's WHILE node to `graph`
+// (its own launch graph is kept); devloop_prepare queues the per-launch reset
+// on the handle's stream, and after `graph` has run devloop_collect reads
+// the report as devloop_run does. devloop_key_current is false when the
+// handle's buffers or kernel forms changed since the loop was captured.
+int devloop_add_to_graph(Handle *h, DevLoop *L, cudaGraph_t graph);
+int devloop_prepare(Handle *h, DevLoop *L);
+int devloop_collect(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log);
+int devloop_read(Handle *h, DevLoop *L, DevLoopResult *r, DevLoopLog *log, size_t span1);
+bool devloop_key_current(const Handle *h, const DevLoop *L);
 // New F_best after the host changed it (drift refresh).
 int devloop_set_fbest(Handle *h, DevLoop *L, double F_best);
 void devloop_destroy(DevLoop *L);
@@ -372,6 +382,7 @@ inline int persistent_grid(const Handle *h, int ntiles, int nsm) {
 // them share the memory system, while their tiles' pipelines lose depth):
 // before its update, lane f's stream waits for lane f-1's last update; the
 // lanes' other kernels (factor, W, operand slicing) still overlap them.
+// Design builds (h->building) keep the lanes' updates concurrent.
 cudaError_t chain_update_wait(Handle *h, int f, cudaStream_t st);
 cudaError_t chain_update_done(Handle *h, int f, cudaStream_t st);
 cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const double2 *A, const double2 *W);

@@ -107,8 +107,13 @@ def test_device_loop_api_rules(cases, built_lib):
     with pytest.raises(lib.PngfError) as e:
         lib.dbs_set_proposal(d, prop, topk=0)
     assert e.value.code == 8  # PNGF_ERR_UNSUPPORTED
+    # a group's members all run device-resident decisions or none does
+    h2 = lib.Handle(7, 7, c["freqs"], max_flips=1)
+    for f, G in enumerate(Gs):
+        h2.load_G(f, G, gobj[f])
+    d2 = lib.Dbs(h2, mode=lib.DBS_SINGLE, seed=2, batch=-4)
     with pytest.raises(lib.PngfError) as e:
-        lib.Group([d])
+        lib.Group([d, d2])
     assert e.value.code == 8
 
 

@@ -90,7 +90,7 @@ def test_state_only_handle_matches_full_handle(build, built_lib):
 MEMBERS = [(7, 0, 0, 1, 16, 0), (9, 1, 1, 2, 32, 1), (11, 0, 1, 3, 32, 0), (9, 0, 0, 4, 8, 0), (11, 1, 1, 5, 48, 0)]
 
 
-def member_runs(built_lib):
+def member_runs(built_lib, device_loop=False):
     from pngf_gb300 import lib
     runs = []
     for a, prec, mode, seed, batch, so in MEMBERS:
@@ -98,13 +98,17 @@ def member_runs(built_lib):
         for f in range(3):
             h.load_G_synth(f, seed=seed)
         d = lib.Dbs(h, mode=lib.DBS_SYMMETRIC if mode == 0 else lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed,
-                    max_evals=700, batch=batch, drift_every=16 if prec == 1 else 0, drift_tol=1e-4)
+                    max_evals=700, batch=batch, drift_every=16 if prec == 1 else 0, drift_tol=1e-4,
+                    device_loop=device_loop)
         runs.append((h, d))
     return runs
 
 
-@pytest.mark.parametrize("graphs", [True, False])
-def test_group_equals_sequential_runs(graphs, built_lib):
+@pytest.mark.parametrize("graphs,device_loop", [(True, False), (False, False), (True, True)])
+def test_group_equals_sequential_runs(graphs, device_loop, built_lib):
+    """Host-drawn groups (one graph of the members' batches per round) and
+    device-resident groups (one graph of the members' decision loops,
+    captured once) reproduce every member's sequential host-driver run."""
     from pngf_gb300 import lib
     seq = []
     for h, d in member_runs(built_lib):
@@ -112,12 +116,14 @@ def test_group_equals_sequential_runs(graphs, built_lib):
         seq.append((d.log(), s.F_best, s.accepts))
         d.close()
         h.close()
-    runs = member_runs(built_lib)
+    runs = member_runs(built_lib, device_loop=device_loop)
     g = lib.Group([d for _, d in runs], use_graphs=graphs)
     st = g.run()
     assert st["rounds"] > 0 and st["accepts"] > 0
     if graphs:
         assert st["graph_launches"] == st["rounds"] and st["captures"] < st["rounds"]
+    if device_loop:
+        assert st["captures"] == 1
     for (h, d), (log0, F0, acc0) in zip(runs, seq):
         s = d.stats()
         log1 = d.log()
