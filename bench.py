@@ -340,7 +340,7 @@ def autotune_on(h, mode_single=True):
 
 
 def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), train_evals=1500, train_steps=600,
-                     topk=64, state_only=0, batch=0, device_loop=False, online_every=0, rule=0):
+                     topk=64, state_only=0, batch=0, device_loop=False, online_every=0, rule=0, defer_rank=0):
     """Wall time to the converged objective: plain FP64 DBS (reference order,
     run until the hat is empty) against the proposal + complex64 form, whose
     network is trained only on plain complex64 runs from other seeds. The
@@ -379,9 +379,10 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
     d.close()
     h.close()
     torch.cuda.empty_cache()
-    # complex64 state built directly in complex64 on the tensor cores
+    # complex64 state built directly in complex64 on the tensor cores; accepts
+    # deferred to pending factors, flushed at rank defer_rank (0: immediate)
     h = lib.Handle(tiles, tiles, freqs, precision=lib.PREC_C64, max_flips=nfl, device=local,
-                   c64_build=lib.BUILD_C64, state_only=state_only)
+                   c64_build=lib.BUILD_C64, state_only=state_only, defer_rank=defer_rank)
     load_G(h)
     prop = lib.Proposal(h, channels=32, seed=1)
     t0 = time.perf_counter()
@@ -429,6 +430,7 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
                            "drift_checks": s.drift_checks, "refreshes": s.refreshes,
                            "eval_form": tune32["eval_form"], "update_cols": tune32["update"][tune32["update_form"]]["cols"],
                            "accept_rule": "first improving in predicted order" if rule else "best improving",
+                           "defer_rank": defer_rank,
                            "reached_target": t_reach is not None,
                            "training": {"seeds": list(train_seeds), "collect_s": t_collect, "train_s": t_train,
                                         "samples": samples, "pairs": pairs, "final_loss": loss,
@@ -567,8 +569,10 @@ def c5_compare(a, local, reduced=True):
     the full form (two seeds, 3000 evaluations each, 1000 steps)."""
     kw = dict(train_seeds=(2,), train_evals=2000, train_steps=600) if reduced else \
         dict(train_evals=3000, train_steps=1000)
+    # deferred complex64 updates: at N = 30504 an update pass over T dominates an accept
     out = converge_compare(41, FREQS_C5, lambda h: [h.load_G_synth(f, seed=1) for f in range(len(FREQS_C5))],
-                           a.seed, local, batch=a.batch, device_loop=bool(a.device_loop), online_every=8, **kw)
+                           a.seed, local, batch=a.batch, device_loop=bool(a.device_loop), online_every=8,
+                           defer_rank=192, **kw)
     out["form"] = "reduced training (1 seed, 2000 evaluations)" if reduced else "full training"
     return out
 
@@ -629,8 +633,26 @@ def gpu_arm(a, world, rank, local):
     iso32 = isolated_update(a, lib.PREC_C64, Gs[0], rows, local) if r32 is not None and rank == 0 else None
     conv = None
     if not a.no_converge and rank == 0:
-        conv = converge_compare(a.tiles, FREQS, lambda h: [h.load_G(f, G, rows) for f, G in enumerate(Gs)], a.seed,
-                                local, batch=a.batch, device_loop=bool(a.device_loop))
+        # the complex64 form of the proposal run: deferred updates when this run
+        # measured them faster than immediate ones at this size
+        defer = 0
+        if r32 is not None and r32d is not None:
+            defer = 192 if reduce_form(r32d, None)[2] / reduce_form(r32d, None)[1] > \
+                reduce_form(r32, None)[2] / reduce_form(r32, None)[1] else 0
+        load = lambda h: [h.load_G(f, G, rows) for f, G in enumerate(Gs)]  # noqa: E731
+        runs = []
+        for sd in (a.seed, a.seed + 1, a.seed + 2):  # the network of each run trains on two other seeds
+            runs.append(converge_compare(a.tiles, FREQS, load, sd, local, train_seeds=(sd + 10, sd + 20),
+                                         batch=a.batch, device_loop=bool(a.device_loop), defer_rank=defer))
+        conv = runs[0]
+        conv["complex64_form"] = ("deferred (rank 192): measured faster than immediate updates in this run"
+                                  if defer else "immediate updates: measured faster than deferred in this run")
+        keys = ("speedup_wall_to_objective", "speedup_both_to_target", "speedup_wall_to_objective_incl_training",
+                "speedup_both_to_target_incl_training")
+        conv["seeds"] = [dict({"seed": a.seed + i, "reached_target": r["proposal_c64"]["reached_target"],
+                               "F_plain": r["plain_fp64"]["F_final"], "F_proposal": r["proposal_c64"]["F_final"]},
+                              **{k: r.get(k) for k in keys}) for i, r in enumerate(runs)]
+        conv["reached_fraction"] = sum(x["reached_target"] for x in conv["seeds"]) / len(runs)
     del Gs
     grp = group_bench(a, local) if (not a.no_group and rank == 0) else None
     c5 = c5_compare(a, local) if (not a.no_c5 and not a.no_converge and rank == 0) else None
