@@ -68,7 +68,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--device-loop", type=int, default=0,
                     help="1: DBS decisions without an accept run on the device (one CUDA graph with a WHILE node)")
-    ap.add_argument("--forms", default="fp64,c64,c64d", help="precision forms to run; the first is the headline")
+    ap.add_argument("--forms", default="fp64,c64,c64d,sym",
+                    help="forms to run (fp64 is the headline; c64, c64d: complex64 immediate / deferred; sym: the "
+                         "4-fold mirror hat in FP64)")
     ap.add_argument("--nfreq", type=int, default=5, help="use the first NFREQ of the five frequencies")
     ap.add_argument("--no-converge", action="store_true",
                     help="skip the wall time to convergence, plain FP64 DBS against proposal + complex64 DBS")
@@ -460,14 +462,15 @@ def converge_compare(tiles, freqs, load_G, seed, local, train_seeds=(2, 3), trai
 FREQS_GROUP = [28.0e9, 30.0e9, 32.0e9]
 
 
-def group_member(tiles, seed, max_evals, batch, local, device_loop=False):
+def group_member(tiles, seed, max_evals, batch, local, device_loop=False, defer_rank=192):
     """One instance of the group workload: complex64 state built on the tensor
-    cores, G generated on the device and not kept (state_only), single-tile
-    DBS from the 50%-fill design of `seed`, its kernel forms autotuned;
-    device_loop: its decisions drawn and taken on the device."""
+    cores, G generated on the device and not kept (state_only), accepts
+    deferred to rank defer_rank (0: immediate), single-tile DBS from the
+    50%-fill design of `seed`, its kernel forms autotuned; device_loop: its
+    decisions drawn and taken on the device."""
     from pngf_gb300 import lib
     h = lib.Handle(tiles, tiles, FREQS_GROUP, precision=lib.PREC_C64, max_flips=1, device=local,
-                   c64_build=lib.BUILD_C64, state_only=1)
+                   c64_build=lib.BUILD_C64, state_only=1, defer_rank=defer_rank)
     for f in range(len(FREQS_GROUP)):
         h.load_G_synth(f, seed=seed)
     d = lib.Dbs(h, mode=lib.DBS_SINGLE, init=lib.INIT_RANDOM, seed=seed, max_evals=max_evals, batch=batch,
@@ -539,6 +542,7 @@ def group_bench(a, local, n_check=8):
     torch.cuda.synchronize()
     out["setup_s"] = time.perf_counter() - t0
     out["decisions"] = "device-resident: one graph of the instances' decision loops (draw, evaluate, decide)"
+    out["accepts_form"] = "complex64, deferred to pending rank 192 (flushed by the long-K tensor-core kernel)"
     out["device_gb_held"] = (free0 - torch.cuda.mem_get_info(local)[0]) / 1e9
     out["edges_total"] = int(sum(h.n for h, _ in runs))
     g = lib.Group([d for _, d in runs], use_graphs=True)
@@ -629,6 +633,12 @@ def gpu_arm(a, world, rank, local):
     if "c64d" in forms:  # complex64 with the rank-k updates deferred to rank 192
         r32d = run_form(a, lib.PREC_C64, Gs, rows, rank, local, dist, defer_rank=192)
         c64d_red = reduce_form(r32d, dist)
+    rsym = None
+    if "sym" in forms and a.mode == "single":  # the reference's own 4-fold mirror hat, plain FP64, 10 decisions
+        import copy
+        asym = copy.copy(a)
+        asym.mode, asym.steps = "sym", 10
+        rsym = run_form(asym, lib.PREC_FP64, Gs, rows, rank, local, dist)
     iso64 = isolated_update(a, lib.PREC_FP64, Gs[0], rows, local) if r64 is not None and rank == 0 else None
     iso32 = isolated_update(a, lib.PREC_C64, Gs[0], rows, local) if r32 is not None and rank == 0 else None
     conv = None
@@ -813,6 +823,17 @@ def gpu_arm(a, world, rank, local):
             r32d, c64d_red, "the complex64 form with the T part of each accept appended to pending rank-k factors "
                             "(candidates and accepts read T minus the pending product) and flushed to T on the tensor "
                             "cores when the pending rank reaches 192 - 24: roofline per flush launch")
+    if rsym is not None:
+        ts = rsym["tm"]
+        line["symmetric_form"] = {
+            "what": "the reference's default candidate set: the 4-fold mirror quarter hat (flips of 1, 2 or 4 tiles, "
+                    "up to 96 edges), plain FP64, same workload, 10 decisions",
+            "value": rsym["evals"] / rsym["dev_s"] if rsym["dev_s"] > 0 else None,
+            "e2e": rsym["evals"] / rsym["wall"], "unit": "flip_evals/s", "evals": rsym["evals"],
+            "accepts": rsym["accepts"], "eval_ms": ts["eval_ms"], "accept_ms": ts["accept_ms"],
+            "update_ms": ts["update_ms"], "update_launches": ts["update_launches"],
+            "ms_per_accept": ts["accept_ms"] / max(1, rsym["accepts"]),
+        }
     if conv is not None:
         line["converge"] = conv
     if grp is not None:

@@ -567,7 +567,8 @@ namespace {
 // complex64 when b32), its row c taken from row browidx[c] when given. On
 // the lane's operand scratch and stream.
 cudaError_t f64tc_gemm(Handle *h, int f, int k, double *D, long drows, long dcols2, long ldd, const double2 *A,
-                       long lda, const void *B, bool b32, long ldb, const int *browidx, bool timed) {
+                       long lda, const void *B, bool b32, long ldb, const int *browidx, bool timed,
+                       bool chain = true) {
   if (k < 1 || k > f64tc_max_k()) return cudaErrorInvalidValue;
   const int k2p = (2 * k + 15) / 16 * 16;
   const int nrb = (int)((drows + FB_BM - 1) / FB_BM), ncb = (int)((dcols2 + FB_BN - 1) / FB_BN);
@@ -613,11 +614,11 @@ cudaError_t f64tc_gemm(Handle *h, int f, int k, double *D, long drows, long dcol
     return e;
   const int ntiles = nrb * ncb;
   const int grid = persistent_grid(h, ntiles, g_num_sms);
-  if (timed && (e = chain_update_wait(h, f, st)) != cudaSuccess) return e;  // the M update: one lane at a time
+  if (timed && chain && (e = chain_update_wait(h, f, st)) != cudaSuccess) return e;  // the M update: one lane at a time
   cudaEvent_t t0 = timed ? timing_mark(h, st) : nullptr;
   k_tc_update_f64<<<grid, FB_THREADS, smem, st>>>(A16, B16, md, (int)drows, (int)dcols2, ncb, ntiles, k2p, nb, nd,
                                                   L.eA, L.fB, h->d_tc_err);
-  if (timed && (e = chain_update_done(h, f, st)) != cudaSuccess) return e;
+  if (timed && chain && (e = chain_update_done(h, f, st)) != cudaSuccess) return e;
   if (timed) {
     const double cells = (double)drows * (double)(dcols2 / 2);
     timing_close(h, t0, T_UPDATE, 8.0 * k * cells,
@@ -633,12 +634,14 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
   const long n = h->n, rows = n + h->E;
   // the inner dimension in pieces of at most f64tc_max_k(): each piece's
   // product is exact and rounded once into M (as a K-blocked DGEMM rounds
-  // once per block); A and W are copies, so later pieces see the same operands
+  // once per block); A and W are copies, so later pieces see the same operands.
+  // Updates in pieces (k = 32 tile shapes) keep the frequency lanes concurrent.
+  const bool chain = k <= f64tc_max_k();
   for (int c0 = 0; c0 < k; c0 += f64tc_max_k()) {
     const int kc = std::min(k - c0, f64tc_max_k());
     const cudaError_t e = f64tc_gemm(h, f, kc, reinterpret_cast<double *>(M), rows, 2 * (n + 1), 2 * h->ldm,
                                      A + (size_t)c0 * rows, rows, W + (size_t)c0 * h->ldm, false, h->ldm, nullptr,
-                                     true);
+                                     true, chain);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

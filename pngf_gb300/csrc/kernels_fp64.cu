@@ -1235,10 +1235,14 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
   cudaError_t e;
-  if (h->f64tc && layout == PNGF_PREC_C64 && h->defer_cap == 0 && k <= kMaxTcW) {
+  // complex64 with nothing pending (no deferral, a build, or the first accept
+  // after a flush): W on the tensor cores from the rows of T32 as stored;
+  // with pending deferred updates the rows are read through the correction
+  // by the FP64 triangular solves below
+  if (h->f64tc && layout == PNGF_PREC_C64 && (h->defer_cap == 0 || h->defer_rp == 0) && k <= kMaxTcW) {
     if ((e = accept_prologue_tc<float2>(h, f, view32(h, f), q.T32, true, q.Einc, d_s, d_d, k)) != cudaSuccess)
       return e;
-    return launch_c64_update(h, f, k);
+    return h->defer_now ? launch_c64_defer(h, f, k) : launch_c64_update(h, f, k);
   }
   // FP64: W from K's explicit inverse only up to f64tc_max_k() edges; above,
   // its error grows with cond(K) beyond that of the triangular solves
