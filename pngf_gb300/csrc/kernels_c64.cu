@@ -266,6 +266,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // over the eight 32-column chunks of a tile. Every wait is bounded; on a
 // timeout the kernel records an error code, drains its copies and reduces,
 // frees its TMEM and returns.
+//
+// The CTAs take tiles in turn (tile blockIdx.x + i * gridDim.x in step i) in
+// a column-major raster over bands of LK_GROUP row blocks, so that the tiles
+// in flight at one time share one or two B panels and at most LK_GROUP A
+// panels: the operands stay in L2 while T streams through it.
+constexpr int LK_GROUP = 64;                           // row blocks per band of the raster
 constexpr int LK_BN = 256;                             // fp32 output columns per tile (MMA N)
 constexpr uint32_t LK_A = TC_BM * TC_BK * 4;           // one K stage of A_hi or A_lo (16 KB)
 constexpr uint32_t LK_B = LK_BN * TC_BK * 4;           // one K stage of B_hi or B_lo (32 KB)
@@ -281,6 +287,14 @@ constexpr size_t LK_SMEM = 1024 + (size_t)LK_ST * LK_STAGE + 2 * LK_STG + 256;
 static_assert(LK_SMEM <= kTcSmemOptin && LK_NBARS * 8 + 4 <= 256, "long-K shared memory and barrier block");
 constexpr uint32_t LK_IDESC =
     (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(LK_BN >> 3) << 17) | ((uint32_t)(TC_BM >> 4) << 24);
+
+// Row and column block of tile t in the banded column-major raster.
+__device__ __forceinline__ void lk_tile(int t, int nrb, int ncb, int &rb, int &cb) {
+  const int per = LK_GROUP * ncb, band = t / per, first = band * LK_GROUP, w = t - band * per;
+  const int rows = min(nrb - first, LK_GROUP);
+  rb = first + w % rows;
+  cb = w / rows;
+}
 
 __global__ void __launch_bounds__(LK_THREADS, 1)
     k_tc_update_longk(const __grid_constant__ CUtensorMap tmAhi, const __grid_constant__ CUtensorMap tmAlo,
@@ -302,8 +316,9 @@ __global__ void __launch_bounds__(LK_THREADS, 1)
   auto stg_full = [&](int g) { return bar0 + 8u * (uint32_t)(3 * LK_ST + 4 + g); };
   auto stg_free = [&](int g) { return bar0 + 8u * (uint32_t)(3 * LK_ST + 6 + g); };
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t_begin = (int)(((long long)ntiles * blockIdx.x) / gridDim.x);
-  const int t_end = (int)(((long long)ntiles * (blockIdx.x + 1)) / gridDim.x);
+  const int nrb = ntiles / ncb;
+  // this CTA's tiles: t = blockIdx.x + li * gridDim.x for li < nloc
+  const int nloc = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < LK_ST; ++s) {
@@ -329,8 +344,10 @@ __global__ void __launch_bounds__(LK_THREADS, 1)
     if (lane == 0) {
       bool ok = true;
       int g = 0;
-      for (int t = t_begin; t < t_end && ok; ++t) {
-        const int rb = t / ncb, cb = t - rb * ncb, m0 = rb * TC_BM, n0 = cb * LK_BN;
+      for (int li = 0; li < nloc && ok; ++li) {
+        int rb, cb;
+        lk_tile((int)blockIdx.x + li * (int)gridDim.x, nrb, ncb, rb, cb);
+        const int m0 = rb * TC_BM, n0 = cb * LK_BN;
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           const int st = g % LK_ST;
           if (g >= LK_ST && !mbar_wait(empty(st), ((g / LK_ST) - 1) & 1)) { ok = false; break; }
@@ -354,8 +371,8 @@ __global__ void __launch_bounds__(LK_THREADS, 1)
     if (lane == 0) {
       bool ok = true;
       int g = 0;
-      for (int t = t_begin; t < t_end && ok; ++t) {
-        const int li = t - t_begin, b = li & 1;
+      for (int li = 0; li < nloc && ok; ++li) {
+        const int b = li & 1;
         if (li >= 2 && !mbar_wait(acc_empty(b), ((li >> 1) - 1) & 1)) { ok = false; break; }
         tc_fence_after();
         const uint32_t acc = tmem + (uint32_t)(b * LK_BN);
@@ -393,8 +410,10 @@ __global__ void __launch_bounds__(LK_THREADS, 1)
     unsigned char *stg_row = base + stg_off + (size_t)grp * LK_STG + (size_t)r * 128;
     bool ok = true;
     int n = 0;  // chunks this group has written (its staging box's uses)
-    for (int t = t_begin; t < t_end && ok; ++t) {
-      const int li = t - t_begin, b = li & 1, rb = t / ncb, cb = t - rb * ncb;
+    for (int li = 0; li < nloc && ok; ++li) {
+      const int b = li & 1;
+      int rb, cb;
+      lk_tile((int)blockIdx.x + li * (int)gridDim.x, nrb, ncb, rb, cb);
       ok = __all_sync(0xffffffffu, mbar_wait(acc_full(b), (li >> 1) & 1));
       if (!ok) break;
       tc_fence_after();

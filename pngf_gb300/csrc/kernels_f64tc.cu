@@ -460,6 +460,13 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
 #pragma unroll
         for (int l = 0; l < FB_NLEV; ++l) tmem_ld8_nowait(tbase + (uint32_t)(l * FB_BN), v[l]);
         tmem_wait_ld();
+        if (c == 1) {
+          // every level of the tile is in registers: the accumulator set is
+          // free once every warp of the group has read it
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(acc_empty(g));
+        }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
           auto F = [&](int l) { return (unsigned)fbits(__uint_as_float(v[l][u])); };
@@ -469,10 +476,6 @@ __global__ void __launch_bounds__(FB_THREADS, 1)
           Y[c * 8 + u] = ((long long)p23 << 28) + ((long long)p45 << 14) + (long long)(p67 + r8);
         }
       }
-      // the accumulator set is free once every warp of the group has read it
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(acc_empty(g));
       int fb[16];
       const int4 *f4 = reinterpret_cast<const int4 *>(fB + col0);
 #pragma unroll
