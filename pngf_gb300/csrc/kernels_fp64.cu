@@ -373,10 +373,13 @@ __device__ int cta_lu(double2 *K, int ld, int k, int *piv, double *red_v, int *r
       }
     }
     __syncthreads();
-    const int m = k - j - 1;
-    for (int idx = tid; idx < m * m; idx += nt) {
-      const int i = j + 1 + idx % m, c = j + 1 + idx / m;
-      K[i + c * ld] = cfnma(K[i + c * ld], K[i + j * ld], K[j + c * ld]);
+    // trailing update: lanes over rows, warps over columns, so that a lane
+    // reads its rows' multipliers once per step and the pivot row's entry is
+    // a broadcast (the same element operations as any other mapping)
+    const int wid = tid >> 5, ln = tid & 31, nw = nt >> 5;
+    for (int i = j + 1 + ln; i < k; i += 32) {
+      const double2 l = K[i + j * ld];
+      for (int c = j + 1 + wid; c < k; c += nw) K[i + c * ld] = cfnma(K[i + c * ld], l, K[j + c * ld]);
     }
     __syncthreads();
   }
@@ -843,7 +846,7 @@ __global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int 
 // one warp per column c solves K x = e_c (the substitutions of k_acc_W, with
 // U's diagonal inverted once). INV_COLS columns per CTA share the LU, staged in
 // shared memory so that the sequential steps never wait on global memory.
-constexpr int INV_COLS = 4;
+constexpr int INV_COLS = 2;  // columns of K^-1 per CTA (a warp each): the FP64 solves spread over k / 2 SMs
 constexpr int kMaxTcW = 96;  // edges per accept on the tensor-core W path (the LU fits shared memory)
 __global__ void __launch_bounds__(32 * INV_COLS) k_acc_inverse(const double2 *__restrict__ LU, int ldlu,
                                                                const int *__restrict__ gpiv,
@@ -854,13 +857,14 @@ __global__ void __launch_bounds__(32 * INV_COLS) k_acc_inverse(const double2 *__
   double2 *rdiag = K + (size_t)k * k;          // 1 / U[q][q]
   double2 *xs = rdiag + k;                     // INV_COLS x k
   __shared__ int piv[kMaxK];
-  for (int idx = threadIdx.x; idx < k * k; idx += blockDim.x) K[idx] = LU[(idx % k) + (size_t)(idx / k) * ldlu];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int col = w; col < k; col += INV_COLS)  // a warp per column, lanes along it
+    for (int r = lane; r < k; r += 32) K[r + (size_t)col * k] = LU[r + (size_t)col * ldlu];
   for (int q = threadIdx.x; q < k; q += blockDim.x) {
     piv[q] = gpiv[q];
     rdiag[q] = crecip(LU[q + (size_t)q * ldlu]);
   }
   __syncthreads();
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int c = blockIdx.x * INV_COLS + w;
   if (c >= k) return;
   double2 *x = xs + (size_t)w * k;
