@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 #include "bounds.cuh"
@@ -771,13 +772,16 @@ __global__ void __launch_bounds__(256) k_acc_factor(const SV<TM> M, long n,
 }
 
 // W[r][j] = d_r (K^-1 M[s, j])_r for j < N, W[r][N] = z_r. One thread per
-// column, blockDim.x (32 or 64) columns per CTA; K's LU in shared memory.
+// column, blockDim.x (32 or 64) columns per CTA; K's LU in shared memory. The
+// rows M[s, :] come from Xrows (row r at Xrows + r * ldw, which may be W
+// itself: a CTA reads its column block before it writes it) when given, else
+// through the view.
 template <typename TM>
 __global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int *__restrict__ gs,
                                               const signed char *__restrict__ gd, int k, const double2 *__restrict__ LU,
                                               int ldlu, const int *__restrict__ gpiv,
-                                              const double2 *__restrict__ z, double2 *__restrict__ W, long ldw,
-                                              const int *__restrict__ guard) {
+                                              const double2 *__restrict__ z, double2 *W, long ldw,
+                                              const int *__restrict__ guard, const double2 *Xrows = nullptr) {
   if (guard && *guard != 0) return;  // the factor step refused the edge list or found K singular
   extern __shared__ double2 smem[];
   double2 *K = smem;                         // k x k
@@ -798,7 +802,7 @@ __global__ void __launch_bounds__(64) k_acc_W(const SV<TM> M, long n, const int 
   for (int idx = threadIdx.x; idx < k * bw; idx += blockDim.x) {
     const int r = idx / bw, jj = idx % bw;
     const long j = j0 + jj;
-    X[(size_t)jj * k + r] = j < n ? M.t(s[r], j) : make_double2(0.0, 0.0);
+    X[(size_t)jj * k + r] = j >= n ? make_double2(0.0, 0.0) : Xrows ? Xrows[(size_t)r * ldw + j] : M.t(s[r], j);
   }
   __syncthreads();
   const long j = j0 + threadIdx.x;
@@ -908,14 +912,87 @@ __global__ void k_W_init(double2 *__restrict__ W, long ldw, long n, const double
 // A[i + r*lda] = M[i][s_r], i < N+E.
 template <typename TM>
 __global__ void k_acc_gather(const SV<TM> M, long n, long rows, const int *__restrict__ gs, int k,
-                             double2 *__restrict__ A, long lda, const int *__restrict__ guard) {
+                             double2 *__restrict__ A, long lda, const int *__restrict__ guard, long row0 = 0) {
   if (guard && *guard != 0) return;
-  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long i = row0 + (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= rows) return;
   if (i < n)
     for (int r = 0; r < k; ++r) A[(size_t)r * lda + i] = M.t(i, gs[r]);
   else
     for (int r = 0; r < k; ++r) A[(size_t)r * lda + i] = M.r((int)(i - n), gs[r]);
+}
+
+// The rows s (ROWS) or the columns s (!ROWS) of T_true = T - U Vt^T for a
+// complex64 state with a pending rank-rp correction, as dense FP64 blocks:
+//   ROWS:  out[r * ldo + j] = T_true(s_r, j), r < k, j < n;
+//   !ROWS: out[c * ldo + i] = T_true(i, s_c), c < k, i < n.
+// Reading them through SV::t() costs every element rp loads of a row of Vt
+// (or U) 8 * rcap bytes away from its neighbour's; here a CTA stages 64 of
+// those rows and the k rows of the other factor in shared memory, 32 ranks at
+// a time, and each element's correction is summed in the order and form of
+// SV::t(), so the values are bit for bit those read through the view. CTA:
+// 64 indices along N (the "many" side), 256 threads, 4 elements each per
+// block of 16 edges.
+constexpr int PB_M = 64, PB_Q = 32, PB_F = 16;
+template <bool ROWS>
+__global__ void __launch_bounds__(256) k_pend_block(const float2 *__restrict__ T, long ldt,
+                                                    const float2 *__restrict__ U, const float2 *__restrict__ Vt,
+                                                    int rcap, int rp, long n, const int *__restrict__ gs, int k,
+                                                    double2 *__restrict__ out, long ldo) {
+  __shared__ float2 Mc[PB_M][PB_Q + 1];  // padded: lanes read 64-bit words 66 words apart
+  __shared__ float2 Fc[PB_F][PB_Q];
+  __shared__ int sf[PB_F];
+  const long m0 = (long)blockIdx.x * PB_M;
+  const int t = threadIdx.x, m = t & (PB_M - 1), fg = t >> 6;  // 4 groups of 4 edges
+  const float2 *many = ROWS ? Vt : U, *few = ROWS ? U : Vt;
+  for (int fb = 0; fb < k; fb += PB_F) {
+    const int nf = min(PB_F, k - fb);
+    __syncthreads();
+    if (t < PB_F) {
+      int e = t < nf ? gs[fb + t] : 0;
+      if (!PNGF_BOUNDS_OK(e >= 0 && e < n, kBoundsT, e, 0)) e = 0;
+      sf[t] = e;
+    }
+    float cx[4] = {0.f, 0.f, 0.f, 0.f}, cy[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int q0 = 0; q0 < rp; q0 += PB_Q) {
+      const int nq = min(PB_Q, rp - q0);
+      __syncthreads();  // sf written; the previous chunk consumed
+      for (int idx = t; idx < PB_M * PB_Q; idx += 256) {
+        const int r = idx / PB_Q, q = idx % PB_Q;
+        const long i = m0 + r;
+        Mc[r][q] = (i < n && q < nq) ? many[(size_t)i * rcap + q0 + q] : make_float2(0.f, 0.f);
+      }
+      for (int idx = t; idx < PB_F * PB_Q; idx += 256) {
+        const int r = idx / PB_Q, q = idx % PB_Q;
+        Fc[r][q] = (r < nf && q < nq) ? few[(size_t)sf[r] * rcap + q0 + q] : make_float2(0.f, 0.f);
+      }
+      __syncthreads();
+      for (int q = 0; q < nq; ++q) {
+        const float2 mv = Mc[m][q];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float2 fv = Fc[fg * 4 + u][q];
+          // SV::t(): a = U[i][q], b = Vt[j][q]
+          const float2 a = ROWS ? fv : mv, b = ROWS ? mv : fv;
+          cx[u] = fmaf(a.x, b.x, fmaf(-a.y, b.y, cx[u]));
+          cy[u] = fmaf(a.x, b.y, fmaf(a.y, b.x, cy[u]));
+        }
+      }
+    }
+    const long i = m0 + m;
+    if (i < n) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int f = fg * 4 + u;
+        if (f >= nf) continue;
+        const float2 tv = ROWS ? T[(size_t)sf[f] * ldt + i] : T[(size_t)i * ldt + sf[f]];
+        double2 v = make_double2((double)tv.x, (double)tv.y);
+        v.x -= (double)cx[u];
+        v.y -= (double)cy[u];
+        out[(size_t)(fb + f) * ldo + i] = v;
+      }
+    }
+  }
 }
 
 // M[i][j] -= sum_r A[i][r] W[r][j] for i < rows, j < cols. 64x64 tile per
@@ -1185,6 +1262,22 @@ static cudaError_t accept_prologue(const SV<TM> &v, long n, int E, long ldm, con
   // raw (caller-owned buffers): the later kernels skip their work once the
   // factor step has set the status, so that M is left as it was
   const int *guard = raw ? status : nullptr;
+  if constexpr (std::is_same<TM, float2>::value) {
+    if (v.rp > 0 && !raw) {
+      // a pending correction: the rows s of T_true into W (read back by
+      // k_acc_W) and its columns s into A, each element's correction summed
+      // once; then the objective rows of A from the view
+      const unsigned gb = (unsigned)((n + PB_M - 1) / PB_M);
+      k_pend_block<true><<<gb, 256, 0, stream>>>(v.T, v.ldt, v.U, v.Vt, v.rcap, v.rp, n, d_s, k, W, ldm);
+      k_acc_W<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, lu, ldlu, pv, zz, W,
+                                                                        ldm, guard, W);
+      k_pend_block<false><<<gb, 256, 0, stream>>>(v.T, v.ldt, v.U, v.Vt, v.rcap, v.rp, n, d_s, k, A, rows);
+      if (rows > n)
+        k_acc_gather<TM><<<(unsigned)((rows - n + 255) / 256), 256, 0, stream>>>(v, n, rows, d_s, k, A, rows, guard,
+                                                                                 n);
+      return cudaGetLastError();
+    }
+  }
   k_acc_W<TM><<<(unsigned)((ldm + wc - 1) / wc), wc, smw, stream>>>(v, n, d_s, d_d, k, lu, ldlu, pv, zz, W, ldm,
                                                                     guard);
   k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(v, n, rows, d_s, k, A, rows, guard);
