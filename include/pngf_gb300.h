@@ -326,7 +326,8 @@ typedef struct pngf_dbs_params {
   int batch;      /* speculative candidates per launch: > 0 fixed; 0 = the whole remaining hat; < 0 adaptive,
                      -batch draws after an accept, doubling after each batch without an accept */
   int drift_every;   /* PNGF_PREC_C64: drift check every this many accepts (0 = never) */
-  double drift_tol;  /* ... and rebuild M from G in FP64 when the drift exceeds this */
+  double drift_tol;  /* ... and rebuild M from G when the drift exceeds this (in complex64 for a
+                        PNGF_BUILD_C64 handle, else in FP64) */
 } pngf_dbs_params;
 
 typedef struct pngf_dbs pngf_dbs;

@@ -146,7 +146,9 @@ bool next_candidate(pngf_dbs *d, Cand *c) {
 
 // Complex64 state: every drift_every accepts, an FP64 drift check of 4 sampled
 // rows of T at one frequency (frequencies in turn); the state is rebuilt from
-// G in FP64 when the drift exceeds drift_tol.
+// G when the drift exceeds drift_tol -- in the handle's own build form (a
+// complex64 build for PNGF_BUILD_C64, whose fresh state is within the drift
+// tolerance and costs a fifth of an FP64 build), else in FP64.
 int drift_after_accept(pngf_dbs *d) {
   pngf::Handle *h = d->h;
   if (h->cfg.precision != PNGF_PREC_C64 || d->p.drift_every <= 0 || d->accepts % d->p.drift_every != 0)
@@ -158,7 +160,8 @@ int drift_after_accept(pngf_dbs *d) {
   ++d->drift_checks;
   d->drift_max = std::max(d->drift_max, rel);
   if (d->p.drift_tol > 0 && rel > d->p.drift_tol) {
-    if ((rc = pngf_refresh(ph)) || (rc = pngf_objective(ph, &d->F_best))) return rc;
+    rc = h->cfg.c64_build == PNGF_BUILD_C64 ? pngf_prepare(ph) : pngf_refresh(ph);
+    if (rc || (rc = pngf_objective(ph, &d->F_best))) return rc;
     ++d->refreshes;
   }
   return PNGF_OK;
@@ -175,7 +178,7 @@ void log_row(pngf_dbs *d, const Cand &c, int acc, double F, const double *perf, 
 // Proposal-driven decision (no reference counterpart): the network's top-k
 // single-tile flips are evaluated exactly and an improving one is accepted --
 // the best (PNGF_PROP_BEST) or the first in predicted order (PNGF_PROP_FIRST);
-// if none improves, a full exact pass over every candidate tile follows (in
+// if none improves, an exact pass over every other candidate tile follows (in
 // predicted order), and if that finds nothing either the design is a local
 // minimum.
 int proposal_step(pngf_dbs *d, int *accepted) {
@@ -232,12 +235,20 @@ int proposal_step(pngf_dbs *d, int *accepted) {
     std::vector<float> pred(map_sz);
     if ((rc = pngf_prop_predict(d->prop, pred.data()))) return rc;
     std::stable_sort(full.begin(), full.end(), [&](int a, int b) { return pred[a] < pred[b]; });
-    std::vector<int> order(full.begin(), full.begin() + std::min<int>(d->topk, (int)full.size()));
+    const int nt = std::min<int>(d->topk, (int)full.size());
+    std::vector<int> order(full.begin(), full.begin() + nt);
     if ((rc = run_batch(order, o, &best))) return rc;
     if (best >= 0) {
       ++d->prop_hits;
       return take(order, o, best);
     }
+    // none of them improves: the fallback pass takes the rest, in predicted
+    // order (its best improving flip is the best of all eligible flips)
+    full.erase(full.begin(), full.begin() + nt);
+  }
+  if (full.empty()) {  // the top k were every eligible flip
+    d->converged = d->done = true;
+    return PNGF_OK;
   }
   ++d->full_passes;
   if ((rc = run_batch(full, o, &best))) return rc;
