@@ -352,6 +352,7 @@ int accept_cand_async(Handle *h, int c, int k, bool check_now) {
   if (c < 0 || c >= h->batch_n) return set_error(h, PNGF_ERR_ARG, "candidate index outside the last batch");
   if (k < 0 || k > h->kmax) return set_error(h, PNGF_ERR_ARG, "invalid flipped-edge count");
   PNGF_CUDA(h, cudaMemsetAsync(h->d_acc_status, 0, sizeof(int), h->stream));
+  ++h->state_version;
   // the frequencies' accepts are independent: one lane (stream + scratch) each
   cudaEvent_t t0 = timing_mark(h);
   int rc;
@@ -818,6 +819,7 @@ int pngf_set_source_port(pngf_handle *ph, int tile_x, int tile_y, int y_offset, 
 // frequency (before anything reads T32 directly).
 static int flush_pending(Handle *h) {
   if (h->defer_rp == 0) return PNGF_OK;
+  ++h->state_version;
   int rc = lanes_fork(h);
   for (int f = 0; f < h->cfg.num_freq && rc == PNGF_OK; ++f) rc = cuda_check(h, launch_c64_flush(h, f), "flush");
   const int rj = lanes_join(h);
@@ -860,6 +862,7 @@ static int prepare_impl(Handle *h, bool fp64) {
     if (!h->f[f].loaded) return set_error(h, PNGF_ERR_STATE, "G not loaded for frequency " + std::to_string(f));
   if (!h->have_map) return set_error(h, PNGF_ERR_STATE, "tile map not set");
   if (!h->have_port) return set_error(h, PNGF_ERR_STATE, "source port not set");
+  ++h->state_version;
   h->defer_rp = 0;  // a build starts from G: nothing is pending (build chunks are not deferred)
   PNGF_CUDA(h, launch_set_pending_rank(h));
   // Set edges of the design, ascending; M is built from P = 0 by accepting

@@ -197,6 +197,7 @@ struct Handle {
   std::vector<Pending> pending;
   std::vector<cudaEvent_t> ev_pool;
   long nlaunch = 0;
+  long state_version = 0;  // bumped whenever the stored state or the design changes (accept, build, flush)
 
   std::string err;
 };

@@ -461,6 +461,10 @@ struct pngf_prop {
   std::vector<float> last_gain;  // per tile, raw objective change
   double gain_scale = 0.0, gain_sq = 0.0;
   long gain_n = 0;
+  // the normalized sensitivity map last computed, valid while the handle's
+  // state (Handle::state_version) does not change
+  std::vector<float> sens_cache;
+  long sens_state = -1;
   std::mt19937 rng{1};
   std::string err;
 };
@@ -817,27 +821,34 @@ static int prop_features(pngf_prop *p, int slot, float *feat) {
   Handle *h = p->h;
   if (!h->prepared) return prop_err(p, PNGF_ERR_STATE, "handle not prepared");
   const int HW = p->map_sz;
-  if (h->cfg.precision == PNGF_PREC_FP64)
-    k_tile_sensitivity<double2><<<(HW + 3) / 4, 128, 0, h->stream>>>(
-        h->f[0].M64, h->ldm, h->cfg.tiles_x, h->cfg.tiles_y, h->cfg.cells_x, h->cfg.cells_y, h->ex_xsz, h->ey_xsz,
-        h->nx, p->d_sens);
-  else
-    k_tile_sensitivity<float2><<<(HW + 3) / 4, 128, 0, h->stream>>>(
-        h->f[0].T32, h->ldm, h->cfg.tiles_x, h->cfg.tiles_y, h->cfg.cells_x, h->cfg.cells_y, h->ex_xsz, h->ey_xsz,
-        h->nx, p->d_sens);
-  std::vector<float> sens(HW), f(3 * HW);
-  if (cudaMemcpyAsync(sens.data(), p->d_sens, sizeof(float) * HW, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
-      cudaStreamSynchronize(h->stream) != cudaSuccess)
-    return prop_err(p, PNGF_ERR_CUDA, "feature extraction");
-  double mu = 0.0, sd = 0.0;
-  for (float v : sens) mu += v;
-  mu /= HW;
-  for (float v : sens) sd += (v - mu) * (v - mu);
-  sd = std::sqrt(sd / HW) + 1e-12;
+  if (p->sens_state != h->state_version || (int)p->sens_cache.size() != HW) {  // the sensitivity map
+    if (h->cfg.precision == PNGF_PREC_FP64)
+      k_tile_sensitivity<double2><<<(HW + 3) / 4, 128, 0, h->stream>>>(
+          h->f[0].M64, h->ldm, h->cfg.tiles_x, h->cfg.tiles_y, h->cfg.cells_x, h->cfg.cells_y, h->ex_xsz, h->ey_xsz,
+          h->nx, p->d_sens);
+    else
+      k_tile_sensitivity<float2><<<(HW + 3) / 4, 128, 0, h->stream>>>(
+          h->f[0].T32, h->ldm, h->cfg.tiles_x, h->cfg.tiles_y, h->cfg.cells_x, h->cfg.cells_y, h->ex_xsz, h->ey_xsz,
+          h->nx, p->d_sens);
+    std::vector<float> sens(HW);
+    if (cudaMemcpyAsync(sens.data(), p->d_sens, sizeof(float) * HW, cudaMemcpyDeviceToHost, h->stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+      return prop_err(p, PNGF_ERR_CUDA, "feature extraction");
+    double mu = 0.0, sd = 0.0;
+    for (float v : sens) mu += v;
+    mu /= HW;
+    for (float v : sens) sd += (v - mu) * (v - mu);
+    sd = std::sqrt(sd / HW) + 1e-12;
+    p->sens_cache.resize(HW);
+    for (int t = 0; t < HW; ++t) p->sens_cache[t] = (float)((sens[t] - mu) / sd);
+    p->sens_state = h->state_version;
+  }
+  std::vector<float> f(3 * HW);
   const double gs = p->gain_scale > 0 ? p->gain_scale : 1.0;
   for (int t = 0; t < HW; ++t) {
     f[t] = h->tile_map[t] ? 1.f : -1.f;
-    f[HW + t] = (float)((sens[t] - mu) / sd);
+    f[HW + t] = p->sens_cache[t];
     f[2 * HW + t] = (float)std::max(-4.0, std::min(4.0, p->last_gain[t] / gs));
   }
   if (feat) std::memcpy(feat, f.data(), sizeof(float) * 3 * HW);
