@@ -440,6 +440,7 @@ int pngf_destroy(pngf_handle *ph) {
   }
   dfree(h->d_fconst);
   dfree(h->d_views);
+  dfree(h->d_iota);
   dfree(h->d_Eincs);
   dfree(h->d_tc_err);
   for (Lane &L : h->lanes) {
@@ -454,6 +455,7 @@ int pngf_destroy(pngf_handle *ph) {
     dfree(L.V);
     dfree(L.A16);
     dfree(L.B16);
+    dfree(L.Xs);
     dfree(L.eA);
     dfree(L.fB);
     if (L.done) cudaEventDestroy(L.done);
@@ -610,7 +612,15 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
         return fail(rc);
       if (cudaMemset(L.A16, 0, 2 * ca) != cudaSuccess || cudaMemset(L.B16, 0, 2 * cb) != cudaSuccess)
         return fail(PNGF_ERR_CUDA);
+      if (c64 && h->defer_cap > 0 && (rc = dalloc(h, &L.Xs, (size_t)h->acc_cap * h->ldm))) return fail(rc);
     }
+  }
+  if (c64 && h->defer_cap > 0 && h->f64tc) {
+    std::vector<int> iota(h->acc_cap);
+    for (int q = 0; q < h->acc_cap; ++q) iota[q] = q;
+    if ((rc = dalloc(h, &h->d_iota, (size_t)h->acc_cap))) return fail(rc);
+    if (cudaMemcpy(h->d_iota, iota.data(), sizeof(int) * h->acc_cap, cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(PNGF_ERR_CUDA);
   }
   {
     void *v = nullptr;

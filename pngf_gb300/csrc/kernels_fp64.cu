@@ -1325,6 +1325,50 @@ static cudaError_t accept_prologue_tc(Handle *h, int f, const SV<TM> &v, const v
   return cudaGetLastError();
 }
 
+// The same with a pending correction (deferred complex64): the rows s of
+// T_true are formed densely first (k_pend_block, in the lane's Xs) and the
+// tensor-core product reads them in place of the stored rows; A's T part is
+// the dense block of columns s, its objective rows come through the view.
+static cudaError_t accept_prologue_tc_pend(Handle *h, int f, const SV<float2> &v, const double2 *Einc,
+                                           const int *d_s, const signed char *d_d, int k) {
+  const long n = h->n, rows = n + h->E;
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
+  cudaError_t e;
+  const double2 *LU = L.LU, *z = L.z;
+  const int *piv = L.piv;
+  int ldlu = k;
+  if (h->acc_cand >= 0) {  // a candidate of the evaluated batch: its kernel left K's LU and z
+    const size_t cf = (size_t)h->acc_cand * h->cfg.num_freq + f, km = (size_t)h->kmax;
+    LU = h->d_eval_LU + cf * km * km;
+    piv = h->d_eval_piv + cf * km;
+    z = h->d_eval_z + cf * km;
+    ldlu = h->kmax;
+  } else {
+    const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
+    if ((e = cudaFuncSetAttribute(k_acc_factor<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf)) !=
+        cudaSuccess)
+      return e;
+    k_acc_factor<float2><<<1, 256, smf, st>>>(v, n, Einc, d_s, d_d, k, L.LU, L.piv, L.z, h->d_acc_status, false);
+    h->nlaunch += 1;
+  }
+  const size_t smi = sizeof(double2) * ((size_t)k * k + k + (size_t)INV_COLS * k);
+  if ((e = cudaFuncSetAttribute(k_acc_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smi)) != cudaSuccess)
+    return e;
+  k_acc_inverse<<<(unsigned)((k + INV_COLS - 1) / INV_COLS), 32 * INV_COLS, smi, st>>>(LU, ldlu, piv, d_d, k, L.V);
+  k_W_init<<<dim3((unsigned)((h->ldm + 255) / 256), (unsigned)k), 256, 0, st>>>(L.W, h->ldm, n, z, k);
+  const unsigned gb = (unsigned)((n + PB_M - 1) / PB_M);
+  k_pend_block<true><<<gb, 256, 0, st>>>(v.T, v.ldt, v.U, v.Vt, v.rcap, v.rp, n, d_s, k, L.Xs, h->ldm);
+  h->nlaunch += 3;
+  if ((e = launch_f64tc_wgemm(h, f, k, L.V, L.Xs, false, h->ldm, h->d_iota, L.W)) != cudaSuccess) return e;
+  k_pend_block<false><<<gb, 256, 0, st>>>(v.T, v.ldt, v.U, v.Vt, v.rcap, v.rp, n, d_s, k, L.A, rows);
+  if (rows > n)
+    k_acc_gather<float2><<<(unsigned)((rows - n + 255) / 256), 256, 0, st>>>(v, n, rows, d_s, k, L.A, rows, nullptr,
+                                                                            n);
+  h->nlaunch += 2;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed char *d_d, int k, int layout) {
   Freq &q = h->f[f];
   const long n = h->n, rows = n + h->E;
@@ -1334,11 +1378,16 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   cudaError_t e;
   // complex64 with nothing pending (no deferral, a build, or the first accept
   // after a flush): W on the tensor cores from the rows of T32 as stored;
-  // with pending deferred updates the rows are read through the correction
-  // by the FP64 triangular solves below
+  // with pending deferred updates from the dense rows of T_true (the FP64
+  // triangular solves below remain for larger edge lists)
   if (h->f64tc && layout == PNGF_PREC_C64 && (h->defer_cap == 0 || h->defer_rp == 0) && k <= kMaxTcW) {
     if ((e = accept_prologue_tc<float2>(h, f, view32(h, f), q.T32, true, q.Einc, d_s, d_d, k)) != cudaSuccess)
       return e;
+    return h->defer_now ? launch_c64_defer(h, f, k) : launch_c64_update(h, f, k);
+  }
+  // with pending deferred updates: the same, from dense rows of T_true
+  if (h->f64tc && layout == PNGF_PREC_C64 && L.Xs && h->d_iota && k <= kMaxTcW && k <= h->acc_cap) {
+    if ((e = accept_prologue_tc_pend(h, f, view32(h, f), q.Einc, d_s, d_d, k)) != cudaSuccess) return e;
     return h->defer_now ? launch_c64_defer(h, f, k) : launch_c64_update(h, f, k);
   }
   // FP64: W from K's explicit inverse only up to f64tc_max_k() edges; above,

@@ -103,6 +103,7 @@ struct Lane {
   void *A16 = nullptr, *B16 = nullptr;  // FP64 tensor-core update: bf16 slices, a16_rows x f64tc_op_cols(),
                                         // b16_rows x f64tc_b_cols()
   int *eA = nullptr, *fB = nullptr;     // per-row / per-column power-of-two scales
+  double2 *Xs = nullptr;  // deferred complex64: the rows s of T_true (acc_cap x ldm), input of the tensor-core W
 };
 
 struct Handle {
@@ -119,6 +120,7 @@ struct Handle {
   std::vector<Freq> f;
   FreqConst *d_fconst = nullptr;
   void *d_views = nullptr;     // device array of per-frequency state views (kernels_fp64.cu)
+  int *d_iota = nullptr;       // 0, 1, ..., acc_cap - 1 (row indices of a dense block; deferred complex64)
   void **d_Eincs = nullptr;    // device array of per-frequency Einc pointers
   // per-frequency accept scratch and streams
   std::vector<Lane> lanes;
