@@ -535,14 +535,36 @@ __global__ void __launch_bounds__(256) k_build_Bop(const double2 *__restrict__ W
 
 // Deferred updates: appends the T part of an accept to the pending factors,
 // U[i][rp + c] = A[i][c] and Vt[j][rp + c] = W[c][j] (i, j < N), in complex64.
-__global__ void k_defer_append(const double2 *__restrict__ A, long lda, const double2 *__restrict__ W, long ldw,
-                               long n, int k, int rp, int rcap, float2 *__restrict__ U, float2 *__restrict__ Vt) {
-  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  for (int c = 0; c < k; ++c) {
-    const double2 a = A[(size_t)c * lda + i], w = W[(size_t)c * ldw + i];
-    U[(size_t)i * rcap + rp + c] = make_float2((float)a.x, (float)a.y);
-    Vt[(size_t)i * rcap + rp + c] = make_float2((float)w.x, (float)w.y);
+// A CTA takes DA_ROWS rows: it reads A's and W's columns along the rows
+// (coalesced) into shared memory and writes each row's k new entries as one
+// contiguous run, threads along the run.
+constexpr int DA_ROWS = 32;
+__global__ void __launch_bounds__(256) k_defer_append(const double2 *__restrict__ A, long lda,
+                                                      const double2 *__restrict__ W, long ldw, long n, int k,
+                                                      int rp, int rcap, float2 *__restrict__ U,
+                                                      float2 *__restrict__ Vt) {
+  extern __shared__ float2 da[];  // [2][k][DA_ROWS + 1] (padded: a run's reads fall in different banks)
+  constexpr int P = DA_ROWS + 1;
+  float2 *sa = da, *sw = da + (size_t)k * P;
+  const long i0 = (long)blockIdx.x * DA_ROWS;
+  const int t = threadIdx.x;
+  for (int idx = t; idx < k * DA_ROWS; idx += blockDim.x) {
+    const int c = idx / DA_ROWS, r = idx % DA_ROWS;
+    const long i = i0 + r;
+    if (i < n) {
+      const double2 a = A[(size_t)c * lda + i], w = W[(size_t)c * ldw + i];
+      sa[c * P + r] = make_float2((float)a.x, (float)a.y);
+      sw[c * P + r] = make_float2((float)w.x, (float)w.y);
+    }
+  }
+  __syncthreads();
+  for (int idx = t; idx < k * DA_ROWS; idx += blockDim.x) {
+    const int r = idx / k, c = idx % k;
+    const long i = i0 + r;
+    if (i < n) {
+      U[(size_t)i * rcap + rp + c] = sa[c * P + r];
+      Vt[(size_t)i * rcap + rp + c] = sw[c * P + r];
+    }
   }
 }
 
@@ -1136,8 +1158,12 @@ cudaError_t launch_c64_defer(Handle *h, int f, int k) {
   Lane &L = lane_of(h, f);
   cudaError_t e = launch_side_update(h, f, k);
   if (e != cudaSuccess) return e;
-  k_defer_append<<<(unsigned)((n + 127) / 128), 128, 0, lane_stream(h, f)>>>(L.A, rows, L.W, h->ldm, n, k,
-                                                                               h->defer_rp, h->defer_cap, q.U, q.Vt);
+  const size_t sma = sizeof(float2) * 2 * (size_t)k * (DA_ROWS + 1);  // k <= kMaxK: at most 99 KB
+  if ((e = cudaFuncSetAttribute(k_defer_append, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma)) !=
+      cudaSuccess)
+    return e;
+  k_defer_append<<<(unsigned)((n + DA_ROWS - 1) / DA_ROWS), 256, sma, lane_stream(h, f)>>>(
+      L.A, rows, L.W, h->ldm, n, k, h->defer_rp, h->defer_cap, q.U, q.Vt);
   h->nlaunch += 1;
   if ((e = cudaGetLastError()) != cudaSuccess || !h->defer_flush) return e;
   const int rp = h->defer_rp;
