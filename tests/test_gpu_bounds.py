@@ -3,7 +3,8 @@ golden cases: every data-dependent gather checks its index on the device and
 records a violation instead of reading out of range. The DBS runs here --
 the host driver (candidate kernels of both shapes, FP64 accepts on the
 tensor cores including 96-edge accepts in pieces, the FP64 triangular-solve
-W), the device-resident loop and the complex64 form -- must record no
+W), the device-resident loop and the complex64 forms, immediate and deferred
+(dense pending blocks, pending-factor appends, flushes) -- must record no
 violation and still reproduce the reference's golden logs. This is the check
 that stands in for compute-sanitizer. It runs in a child process, which loads
 the checked library instead of the default one."""
@@ -28,13 +29,16 @@ assert lib.LIB_PATH.endswith("_bc.so")
 L = lib.load()
 cases = {c["name"]: c for c in json.load(open(sys.argv[1] + "/tests/golden/cases.json"))}
 out = []
-for name, prec, dev_loop, simt in (("sym_9x9_f2_seed3", lib.PREC_FP64, False, False),
-                                   ("sym_9x9_f2_seed3", lib.PREC_FP64, False, True),
-                                   ("single_7x7_f2_seed1", lib.PREC_FP64, True, False),
-                                   ("single_11x11_f3_seed2", lib.PREC_C64, False, False)):
+for name, prec, dev_loop, simt, defer in (("sym_9x9_f2_seed3", lib.PREC_FP64, False, False, 0),
+                                          ("sym_9x9_f2_seed3", lib.PREC_FP64, False, True, 0),
+                                          ("single_7x7_f2_seed1", lib.PREC_FP64, True, False, 0),
+                                          ("single_11x11_f3_seed2", lib.PREC_C64, False, False, 0),
+                                          ("single_11x11_f3_seed2", lib.PREC_C64, False, False, 48)):
     c = cases[name]
     Gs, gobj = case_G(c)
     kw = {"fp64_update": lib.F64_SIMT} if simt else {}
+    if defer:
+        kw["defer_rank"] = defer
     h = lib.Handle(c["tiles"], c["tiles"], c["freqs"], precision=prec,
                    max_flips=4 if c["mode"] == "sym" else 1, **kw)
     for f, G in enumerate(Gs):
@@ -50,7 +54,7 @@ for name, prec, dev_loop, simt in (("sym_9x9_f2_seed3", lib.PREC_FP64, False, Fa
     v = C.c_longlong(-1)
     first = (C.c_longlong * 3)()
     rc = L.pngf_bounds_check_report(C.byref(v), first, 1)
-    out.append(dict(name=name, prec=prec, device_loop=dev_loop, simt=simt, rc=rc, violations=v.value,
+    out.append(dict(name=name, prec=prec, device_loop=dev_loop, simt=simt, defer=defer, rc=rc, violations=v.value,
                     first=list(first), sequence_matches=bool(same) if prec == lib.PREC_FP64 else None,
                     evals=s.evals))
     d.close()
@@ -68,7 +72,7 @@ def test_bounds_checked_build_records_no_violation():
     assert r.returncode == 0, r.stderr[-3000:]
     line = [x for x in r.stdout.splitlines() if x.startswith("RESULT ")][-1]
     res = json.loads(line[len("RESULT "):])
-    assert len(res) == 4
+    assert len(res) == 5
     for x in res:
         assert x["rc"] == 0, x
         assert x["violations"] == 0, x
