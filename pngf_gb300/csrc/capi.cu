@@ -456,6 +456,7 @@ int pngf_destroy(pngf_handle *ph) {
     dfree(L.A16);
     dfree(L.B16);
     dfree(L.Xs);
+    dfree(L.KD);
     dfree(L.eA);
     dfree(L.fB);
     if (L.done) cudaEventDestroy(L.done);
@@ -612,7 +613,11 @@ int pngf_create(const pngf_config *cfg, pngf_handle **out) {
         return fail(rc);
       if (cudaMemset(L.A16, 0, 2 * ca) != cudaSuccess || cudaMemset(L.B16, 0, 2 * cb) != cudaSuccess)
         return fail(PNGF_ERR_CUDA);
-      if (c64 && h->defer_cap > 0 && (rc = dalloc(h, &L.Xs, (size_t)h->acc_cap * h->ldm))) return fail(rc);
+      // dense rows s: the deferred complex64 accept, and FP64 accepts of more than 32 edges (with K D)
+      const bool big64 = !c64 && h->acc_cap > f64tc_max_k();
+      if (((c64 && h->defer_cap > 0) || big64) && (rc = dalloc(h, &L.Xs, (size_t)h->acc_cap * h->ldm)))
+        return fail(rc);
+      if (big64 && (rc = dalloc(h, &L.KD, (size_t)h->acc_cap * h->acc_cap))) return fail(rc);
     }
   }
   if (c64 && h->defer_cap > 0 && h->f64tc) {

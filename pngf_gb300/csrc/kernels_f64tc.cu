@@ -650,6 +650,17 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
   return cudaSuccess;
 }
 
+cudaError_t launch_f64tc_small(Handle *h, int f, int k, double2 *D, long drows, long ncols, long ldd,
+                               const double2 *A, long lda, const double2 *B, long ldb) {
+  for (int c0 = 0; c0 < k; c0 += f64tc_max_k()) {
+    const int kc = std::min(k - c0, f64tc_max_k());
+    const cudaError_t e = f64tc_gemm(h, f, kc, reinterpret_cast<double *>(D), drows, 2 * ncols, 2 * ldd,
+                                     A + (size_t)c0 * lda, lda, B + (size_t)c0 * ldb, false, ldb, nullptr, false);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t launch_f64tc_wgemm(Handle *h, int f, int k, const double2 *Vneg, const void *X, bool x32, long ldx,
                                const int *d_s, double2 *W) {
   // W[:, 0:N] -= Vneg X[s, 0:N], the inner dimension in pieces of at most f64tc_max_k()

@@ -1325,6 +1325,72 @@ static cudaError_t accept_prologue_tc(Handle *h, int f, const SV<TM> &v, const v
   return cudaGetLastError();
 }
 
+// FP64 accepts of more than f64tc_max_k() edges: the rows s of the state as
+// a dense block, Xs[r][j] = T[s_r][j] (j < N), and K D = T[s,s] + D
+// (column-major k x k), for the refinement of W below.
+__global__ void k_rows_kd(const SV<double2> M, long n, const int *__restrict__ gs,
+                          const signed char *__restrict__ gd, int k, double2 *__restrict__ Xs, long ldx,
+                          double2 *__restrict__ KD) {
+  const int r = blockIdx.y;
+  const long j = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= k || j >= n) return;
+  const int sr = gs[r];
+  Xs[(size_t)r * ldx + j] = M.t(sr, j);
+  if (j < k) {  // column c = j of K D
+    double2 v = M.t(sr, gs[j]);
+    if (j == r) v.x += (double)gd[j];
+    KD[r + (size_t)j * k] = v;
+  }
+}
+
+// Accept prologue of an FP64 accept of more than f64tc_max_k() (and at most
+// kMaxTcW) edges with W on the tensor cores: W0 = -Vneg X with the explicit
+// inverse, then one step of refinement, W = W0 - Vneg (X - K D W0), all three
+// products FP64-accurate on the tensor cores. An explicit inverse alone is
+// not backward stable (at 96 edges it cost a factor of about 10 in the
+// state's error); the refinement step brings W back to the accuracy of
+// triangular solves, which on GB300's narrow FP64 pipe (one thread per
+// column of W) took longer than the three products together.
+static cudaError_t accept_prologue_tc_refined(Handle *h, int f, const SV<double2> &v, const double2 *Einc,
+                                              const int *d_s, const signed char *d_d, int k) {
+  const long n = h->n, rows = n + h->E;
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
+  cudaError_t e;
+  const double2 *LU = L.LU, *z = L.z;
+  const int *piv = L.piv;
+  int ldlu = k;
+  if (h->acc_cand >= 0) {  // a candidate of the evaluated batch: its kernel left K's LU and z
+    const size_t cf = (size_t)h->acc_cand * h->cfg.num_freq + f, km = (size_t)h->kmax;
+    LU = h->d_eval_LU + cf * km * km;
+    piv = h->d_eval_piv + cf * km;
+    z = h->d_eval_z + cf * km;
+    ldlu = h->kmax;
+  } else {
+    const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
+    if ((e = cudaFuncSetAttribute(k_acc_factor<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf)) !=
+        cudaSuccess)
+      return e;
+    k_acc_factor<double2><<<1, 256, smf, st>>>(v, n, Einc, d_s, d_d, k, L.LU, L.piv, L.z, h->d_acc_status, false);
+    h->nlaunch += 1;
+  }
+  const size_t smi = sizeof(double2) * ((size_t)k * k + k + (size_t)INV_COLS * k);
+  if ((e = cudaFuncSetAttribute(k_acc_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smi)) != cudaSuccess)
+    return e;
+  k_acc_inverse<<<(unsigned)((k + INV_COLS - 1) / INV_COLS), 32 * INV_COLS, smi, st>>>(LU, ldlu, piv, d_d, k, L.V);
+  k_W_init<<<dim3((unsigned)((h->ldm + 255) / 256), (unsigned)k), 256, 0, st>>>(L.W, h->ldm, n, z, k);
+  k_rows_kd<<<dim3((unsigned)((n + 255) / 256), (unsigned)k), 256, 0, st>>>(v, n, d_s, d_d, k, L.Xs, h->ldm, L.KD);
+  h->nlaunch += 3;
+  if ((e = launch_f64tc_wgemm(h, f, k, L.V, v.T, false, h->ldm, d_s, L.W)) != cudaSuccess) return e;  // W0
+  if ((e = launch_f64tc_small(h, f, k, L.Xs, k, n, h->ldm, L.KD, k, L.W, h->ldm)) != cudaSuccess)
+    return e;  // Xs = X - K D W0
+  if ((e = launch_f64tc_small(h, f, k, L.W, k, n, h->ldm, L.V, k, L.Xs, h->ldm)) != cudaSuccess)
+    return e;  // W = W0 - Vneg (X - K D W0)
+  k_acc_gather<double2><<<(unsigned)((rows + 255) / 256), 256, 0, st>>>(v, n, rows, d_s, k, L.A, rows, nullptr);
+  h->nlaunch += 1;
+  return cudaGetLastError();
+}
+
 // The same with a pending correction (deferred complex64): the rows s of
 // T_true are formed densely first (k_pend_block, in the lane's Xs) and the
 // tensor-core product reads them in place of the stored rows; A's T part is
@@ -1397,6 +1463,11 @@ cudaError_t launch_accept_edges(Handle *h, int f, const int *d_s, const signed c
   if (h->f64tc && layout != PNGF_PREC_C64 && k <= f64tc_max_k()) {
     if ((e = accept_prologue_tc<double2>(h, f, view64(h, f), q.M64, false, q.Einc, d_s, d_d, k)) != cudaSuccess)
       return e;
+    return launch_f64tc_update(h, f, k, q.M64, L.A, L.W);
+  }
+  // larger FP64 accepts: the explicit inverse and one refinement step
+  if (h->f64tc && layout != PNGF_PREC_C64 && L.Xs && L.KD && k <= kMaxTcW && k <= h->acc_cap) {
+    if ((e = accept_prologue_tc_refined(h, f, view64(h, f), q.Einc, d_s, d_d, k)) != cudaSuccess) return e;
     return launch_f64tc_update(h, f, k, q.M64, L.A, L.W);
   }
   // a candidate of the evaluated batch: start from the factorization its kernel left

@@ -103,7 +103,9 @@ struct Lane {
   void *A16 = nullptr, *B16 = nullptr;  // FP64 tensor-core update: bf16 slices, a16_rows x f64tc_op_cols(),
                                         // b16_rows x f64tc_b_cols()
   int *eA = nullptr, *fB = nullptr;     // per-row / per-column power-of-two scales
-  double2 *Xs = nullptr;  // deferred complex64: the rows s of T_true (acc_cap x ldm), input of the tensor-core W
+  double2 *Xs = nullptr;  // rows s of the state as a dense block (acc_cap x ldm): deferred complex64 (T_true), and
+                          //   FP64 accepts of more than 32 edges (the W refinement's residual)
+  double2 *KD = nullptr;  // FP64 accepts of more than 32 edges: K D (acc_cap^2, column-major)
 };
 
 struct Handle {
@@ -393,6 +395,11 @@ cudaError_t launch_f64tc_update(Handle *h, int f, int k, double2 *M, const doubl
 // column-major, X rows s of the state (complex64 when x32, pitch ldx).
 cudaError_t launch_f64tc_wgemm(Handle *h, int f, int k, const double2 *Vneg, const void *X, bool x32, long ldx,
                                const int *d_s, double2 *W);
+// D[0:drows, 0:ncols) -= A B on the tensor cores (FP64-accurate), complex:
+// A drows x k column-major (lda), B k x ncols row-major (ldb), D row-major
+// (pitch ldd complex); the inner dimension in pieces of f64tc_max_k().
+cudaError_t launch_f64tc_small(Handle *h, int f, int k, double2 *D, long drows, long ncols, long ldd,
+                               const double2 *A, long lda, const double2 *B, long ldb);
 // Commits P and the tile map on the device for candidate c of the batch.
 cudaError_t launch_commit(Handle *h, int c);
 // The accept kernels on caller-supplied buffers (no handle): scratch LU (k^2),
