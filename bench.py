@@ -79,6 +79,8 @@ def parse():
                     help="profiling case for the candidate kernel: N passes of every tile at every frequency on a "
                          "state-only handle (G not kept), one JSON line; nothing else runs")
     ap.add_argument("--eval-form", type=int, default=1, help="--eval-probe: candidate-kernel form")
+    ap.add_argument("--converge-seeds", type=int, default=5,
+                    help="seeds of the 21x21 proposal + complex64 against plain FP64 comparison")
     ap.add_argument("--no-c5", action="store_true",
                     help="skip the reduced 41x41 x 4-frequency proposal comparison of the default run")
     ap.add_argument("--c5", action="store_true",
@@ -651,7 +653,7 @@ def gpu_arm(a, world, rank, local):
                 reduce_form(r32, None)[2] / reduce_form(r32, None)[1] else 0
         load = lambda h: [h.load_G(f, G, rows) for f, G in enumerate(Gs)]  # noqa: E731
         runs = []
-        for sd in (a.seed, a.seed + 1, a.seed + 2):  # the network of each run trains on two other seeds
+        for sd in range(a.seed, a.seed + max(1, a.converge_seeds)):  # each run's network trains on two other seeds
             runs.append(converge_compare(a.tiles, FREQS, load, sd, local, train_seeds=(sd + 10, sd + 20),
                                          batch=a.batch, device_loop=bool(a.device_loop), defer_rank=defer))
         conv = runs[0]
@@ -660,9 +662,15 @@ def gpu_arm(a, world, rank, local):
         keys = ("speedup_wall_to_objective", "speedup_both_to_target", "speedup_wall_to_objective_incl_training",
                 "speedup_both_to_target_incl_training")
         conv["seeds"] = [dict({"seed": a.seed + i, "reached_target": r["proposal_c64"]["reached_target"],
-                               "F_plain": r["plain_fp64"]["F_final"], "F_proposal": r["proposal_c64"]["F_final"]},
+                               "F_plain": r["plain_fp64"]["F_final"], "F_proposal": r["proposal_c64"]["F_final"],
+                               "F_gap_rel": (r["proposal_c64"]["F_final"] - r["plain_fp64"]["F_final"]) /
+                                            abs(r["plain_fp64"]["F_final"]),
+                               "plain_wall_s": r["plain_fp64"]["wall_s"],
+                               "proposal_wall_s": r["proposal_c64"]["wall_s"]},
                               **{k: r.get(k) for k in keys}) for i, r in enumerate(runs)]
         conv["reached_fraction"] = sum(x["reached_target"] for x in conv["seeds"]) / len(runs)
+        reached = sorted(x["speedup_wall_to_objective"] for x in conv["seeds"] if x["reached_target"])
+        conv["median_speedup_of_reached"] = reached[len(reached) // 2] if reached else None
     del Gs
     grp = group_bench(a, local) if (not a.no_group and rank == 0) else None
     c5 = c5_compare(a, local) if (not a.no_c5 and not a.no_converge and rank == 0) else None
