@@ -666,7 +666,10 @@ def gpu_arm(a, world, rank, local):
                                "F_gap_rel": (r["proposal_c64"]["F_final"] - r["plain_fp64"]["F_final"]) /
                                             abs(r["plain_fp64"]["F_final"]),
                                "plain_wall_s": r["plain_fp64"]["wall_s"],
-                               "proposal_wall_s": r["proposal_c64"]["wall_s"]},
+                               "proposal_wall_s": r["proposal_c64"]["wall_s"],
+                               "proposal_accepts": r["proposal_c64"]["accepts"],
+                               "proposal_full_passes": r["proposal_c64"]["full_passes"],
+                               "proposal_refreshes": r["proposal_c64"]["refreshes"]},
                               **{k: r.get(k) for k in keys}) for i, r in enumerate(runs)]
         conv["reached_fraction"] = sum(x["reached_target"] for x in conv["seeds"]) / len(runs)
         reached = sorted(x["speedup_wall_to_objective"] for x in conv["seeds"] if x["reached_target"])
