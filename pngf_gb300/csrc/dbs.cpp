@@ -214,7 +214,8 @@ int proposal_step(pngf_dbs *d, int *accepted) {
     return PNGF_OK;
   };
   auto take = [&](const std::vector<int> &list, pngf::EvalOut &o, int best) -> int {
-    int rc = pngf::accept_cand(h, best, o.k[best]);
+    // the tensor-core kernels' status is read at the next batch's collect
+    int rc = pngf::accept_cand_async(h, best, o.k[best], false);
     if (rc) return rc;
     d->F_best = o.F[best];
     ++d->accepts;
