@@ -53,6 +53,9 @@ CASES = [
     # first 120 evaluations.
     dict(name="single_21x21_f5_seed1", tiles=21, freqs=FREQS_WIDE, seed=1, init="random", mode="single",
          max_evals=120),
+    # The same size in the reference's default candidate set (4-fold mirror
+    # hat: flips of 1, 2 or 4 tiles, up to 96 edges): the first 40 evaluations.
+    dict(name="sym_21x21_f5_seed1", tiles=21, freqs=FREQS_WIDE, seed=1, init="random", mode="sym", max_evals=40),
 ]
 
 

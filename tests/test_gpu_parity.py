@@ -70,6 +70,22 @@ def test_dbs_matches_reference_at_benchmark_size(cases, built_lib):
     h.close()
 
 
+def test_dbs_matches_reference_at_benchmark_size_symmetric(cases, built_lib):
+    """The same size in the reference's default candidate set, the 4-fold
+    mirror hat (flips of 1, 2 or 4 tiles, up to 96 edges: the FP64 accepts of
+    more than 32 edges take the refined tensor-core W and the update in
+    pieces): the first 40 evaluations of the reference's run, flip for flip."""
+    c = cases["sym_21x21_f5_seed1"]
+    assert c["tiles"] == 21 and c["mode"] == "sym" and len(c["freqs"]) == 5
+    Gs, gobj = case_G(c, built_lib)
+    h, d, s = gpu_dbs(c, Gs, gobj, batch=-16)
+    ref = golden_log(c["name"])
+    assert sum(r[2] for r in ref["rows"]) >= 5  # several accepts
+    compare_log(d, h, ref, s)
+    d.close()
+    h.close()
+
+
 @pytest.mark.parametrize("batch", [1, 5, -2, -16])
 def test_dbs_batch_size_does_not_change_sequence(batch, cases, built_lib):
     """Speculative batches of any size replay the hat to the reference's order
