@@ -896,11 +896,30 @@ static int prepare_impl(Handle *h, bool fp64) {
     PNGF_CUDA(h, launch_init_M(h, f));
     if (c64 && !fp64) PNGF_CUDA(h, launch_split_M(h, f));
     const int chunk = fp64 ? h->init_chunk : kC64BuildChunk;
+    // A complex64 build of a large state on a handle with deferred updates
+    // pairs its chunks: the second chunk of a pair reads the first one's
+    // update through the pending factors (dense rows and columns of T_true)
+    // and one long-K flush of rank up to 2 x chunk applies both -- half the
+    // passes over T. Measured: 16 % faster at N = 30504 (41x41, 4 frequencies),
+    // 5-9 % slower at N = 8064 (21x21, 5 frequencies), where a pass over T
+    // costs little more than the pending blocks.
+    constexpr long kPairMinN = 16384;
+    const bool pair = c64 && !fp64 && h->n >= kPairMinN && h->defer_cap >= 2 * chunk && h->d_iota &&
+                      lane_of(h, f).Xs;
+    int rp = 0;
     for (size_t c0 = 0; c0 < on.size(); c0 += chunk) {
       const int k = (int)std::min<size_t>(chunk, on.size() - c0);
+      if (pair) {
+        h->defer_rp = rp;
+        h->defer_now = true;
+        h->defer_flush = rp + k + chunk > h->defer_cap || c0 + k >= on.size();
+      }
       PNGF_CUDA(h, launch_accept_edges(h, f, h->d_acc_s + c0, h->d_acc_d + c0, k,
                                        fp64 ? PNGF_PREC_FP64 : PNGF_PREC_C64));
+      if (pair) rp = h->defer_flush ? 0 : rp + k;
     }
+    h->defer_rp = 0;
+    h->defer_now = h->defer_flush = false;
     if (c64 && fp64) PNGF_CUDA(h, launch_split_M(h, f));
     return PNGF_OK;
   };
@@ -914,6 +933,8 @@ static int prepare_impl(Handle *h, bool fp64) {
     stage_out(h, f);
   }
   h->building = false;
+  h->defer_rp = 0;  // a build that stopped early may have left a chunk pending
+  h->defer_now = h->defer_flush = false;
   const int rj = lanes_join(h);
   if (rc) return rc;
   if (rj) return rj;

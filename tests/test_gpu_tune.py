@@ -158,3 +158,33 @@ def test_drift_check_per_frequency(cases, built_lib):
     with pytest.raises(lib.PngfError):
         h.drift_check(3, f=len(Gs))
     h.close()
+
+
+def test_c64_paired_build_large_state(built_lib):
+    """A complex64 build of a state large enough to pair its 96-edge chunks
+    (31x31 tiles, N = 17484; handles with deferred updates): the second chunk
+    of each pair reads the first through the pending factors and one flush
+    applies both. Against the FP64 build its objective stays within the
+    complex64 build's bar (5e-5 relative; measured 1.7e-6, the unpaired build
+    4e-7), and its drift stays below the refresh threshold."""
+    from conftest import force_port_tiles
+    from pngf_gb300 import lib
+    a, freqs = 31, [30e9]
+    rng = np.random.default_rng(7)
+    tm = force_port_tiles(rng.integers(0, 2, a * a), a, a)
+    F = {}
+    for name, prec, build, defer in (("fp64", lib.PREC_FP64, 0, 0), ("c64", lib.PREC_C64, lib.BUILD_C64, 0),
+                                     ("paired", lib.PREC_C64, lib.BUILD_C64, 192)):
+        h = lib.Handle(a, a, freqs, precision=prec, max_flips=1, c64_build=build, defer_rank=defer)
+        assert h.n == 17484
+        h.load_G_synth(0, seed=1)
+        h.set_tile_map(tm)
+        h.set_source_port(a // 2, a // 2, 1, 2)
+        h.prepare()
+        F[name] = h.objective()
+        if name == "paired":
+            assert h.drift_check(4) < 1e-4
+        h.close()
+    err_c64 = abs(F["c64"] - F["fp64"]) / abs(F["fp64"])
+    err_paired = abs(F["paired"] - F["fp64"]) / abs(F["fp64"])
+    assert err_c64 <= 5e-5 and err_paired <= 5e-5, (err_c64, err_paired, F)
