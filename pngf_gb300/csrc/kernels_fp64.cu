@@ -1284,15 +1284,14 @@ static cudaError_t accept_prologue(const SV<TM> &v, long n, int E, long ldm, con
   return cudaGetLastError();
 }
 
-// Accept prologue with W on the tensor cores: K's LU and z (those the candidate
-// kernel left, for a candidate of the evaluated batch), Vneg = -D K^-1,
-// W = [D K^-1 T[s, 0:N], z] as Vneg times the rows s of the state with the
-// FP64-accurate tensor-core product, A = [T; R][:, s]. For the FP64 layout and
-// the complex64 one without deferred updates (whose rows are read as stored).
+// The common start of the tensor-core accept prologues: K's LU and z (those
+// the candidate kernel left, for a candidate of the evaluated batch, else
+// factored here through the view), Vneg = -D K^-1 into the lane's V, and W
+// set to [0, z] (its T part is then accumulated by tensor-core products).
 template <typename TM>
-static cudaError_t accept_prologue_tc(Handle *h, int f, const SV<TM> &v, const void *X, bool x32,
-                                      const double2 *Einc, const int *d_s, const signed char *d_d, int k) {
-  const long n = h->n, rows = n + h->E;
+static cudaError_t accept_tc_start(Handle *h, int f, const SV<TM> &v, const double2 *Einc, const int *d_s,
+                                   const signed char *d_d, int k) {
+  const long n = h->n;
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
   cudaError_t e;
@@ -1319,6 +1318,22 @@ static cudaError_t accept_prologue_tc(Handle *h, int f, const SV<TM> &v, const v
   k_acc_inverse<<<(unsigned)((k + INV_COLS - 1) / INV_COLS), 32 * INV_COLS, smi, st>>>(LU, ldlu, piv, d_d, k, L.V);
   k_W_init<<<dim3((unsigned)((h->ldm + 255) / 256), (unsigned)k), 256, 0, st>>>(L.W, h->ldm, n, z, k);
   h->nlaunch += 2;
+  return cudaGetLastError();
+}
+
+// Accept prologue with W on the tensor cores: K's LU and z (those the candidate
+// kernel left, for a candidate of the evaluated batch), Vneg = -D K^-1,
+// W = [D K^-1 T[s, 0:N], z] as Vneg times the rows s of the state with the
+// FP64-accurate tensor-core product, A = [T; R][:, s]. For the FP64 layout and
+// the complex64 one without deferred updates (whose rows are read as stored).
+template <typename TM>
+static cudaError_t accept_prologue_tc(Handle *h, int f, const SV<TM> &v, const void *X, bool x32,
+                                      const double2 *Einc, const int *d_s, const signed char *d_d, int k) {
+  const long n = h->n, rows = n + h->E;
+  Lane &L = lane_of(h, f);
+  cudaStream_t st = lane_stream(h, f);
+  cudaError_t e;
+  if ((e = accept_tc_start<TM>(h, f, v, Einc, d_s, d_d, k)) != cudaSuccess) return e;
   if ((e = launch_f64tc_wgemm(h, f, k, L.V, X, x32, h->ldm, d_s, L.W)) != cudaSuccess) return e;
   k_acc_gather<TM><<<(unsigned)((rows + 255) / 256), 256, 0, st>>>(v, n, rows, d_s, k, L.A, rows, nullptr);
   h->nlaunch += 1;
@@ -1357,30 +1372,9 @@ static cudaError_t accept_prologue_tc_refined(Handle *h, int f, const SV<double2
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
   cudaError_t e;
-  const double2 *LU = L.LU, *z = L.z;
-  const int *piv = L.piv;
-  int ldlu = k;
-  if (h->acc_cand >= 0) {  // a candidate of the evaluated batch: its kernel left K's LU and z
-    const size_t cf = (size_t)h->acc_cand * h->cfg.num_freq + f, km = (size_t)h->kmax;
-    LU = h->d_eval_LU + cf * km * km;
-    piv = h->d_eval_piv + cf * km;
-    z = h->d_eval_z + cf * km;
-    ldlu = h->kmax;
-  } else {
-    const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
-    if ((e = cudaFuncSetAttribute(k_acc_factor<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf)) !=
-        cudaSuccess)
-      return e;
-    k_acc_factor<double2><<<1, 256, smf, st>>>(v, n, Einc, d_s, d_d, k, L.LU, L.piv, L.z, h->d_acc_status, false);
-    h->nlaunch += 1;
-  }
-  const size_t smi = sizeof(double2) * ((size_t)k * k + k + (size_t)INV_COLS * k);
-  if ((e = cudaFuncSetAttribute(k_acc_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smi)) != cudaSuccess)
-    return e;
-  k_acc_inverse<<<(unsigned)((k + INV_COLS - 1) / INV_COLS), 32 * INV_COLS, smi, st>>>(LU, ldlu, piv, d_d, k, L.V);
-  k_W_init<<<dim3((unsigned)((h->ldm + 255) / 256), (unsigned)k), 256, 0, st>>>(L.W, h->ldm, n, z, k);
+  if ((e = accept_tc_start<double2>(h, f, v, Einc, d_s, d_d, k)) != cudaSuccess) return e;
   k_rows_kd<<<dim3((unsigned)((n + 255) / 256), (unsigned)k), 256, 0, st>>>(v, n, d_s, d_d, k, L.Xs, h->ldm, L.KD);
-  h->nlaunch += 3;
+  h->nlaunch += 1;
   if ((e = launch_f64tc_wgemm(h, f, k, L.V, v.T, false, h->ldm, d_s, L.W)) != cudaSuccess) return e;  // W0
   if ((e = launch_f64tc_small(h, f, k, L.Xs, k, n, h->ldm, L.KD, k, L.W, h->ldm)) != cudaSuccess)
     return e;  // Xs = X - K D W0
@@ -1401,31 +1395,10 @@ static cudaError_t accept_prologue_tc_pend(Handle *h, int f, const SV<float2> &v
   Lane &L = lane_of(h, f);
   cudaStream_t st = lane_stream(h, f);
   cudaError_t e;
-  const double2 *LU = L.LU, *z = L.z;
-  const int *piv = L.piv;
-  int ldlu = k;
-  if (h->acc_cand >= 0) {  // a candidate of the evaluated batch: its kernel left K's LU and z
-    const size_t cf = (size_t)h->acc_cand * h->cfg.num_freq + f, km = (size_t)h->kmax;
-    LU = h->d_eval_LU + cf * km * km;
-    piv = h->d_eval_piv + cf * km;
-    z = h->d_eval_z + cf * km;
-    ldlu = h->kmax;
-  } else {
-    const size_t smf = sizeof(double2) * ((size_t)k * k + 2 * k) + sizeof(int) * k + k + 16;
-    if ((e = cudaFuncSetAttribute(k_acc_factor<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf)) !=
-        cudaSuccess)
-      return e;
-    k_acc_factor<float2><<<1, 256, smf, st>>>(v, n, Einc, d_s, d_d, k, L.LU, L.piv, L.z, h->d_acc_status, false);
-    h->nlaunch += 1;
-  }
-  const size_t smi = sizeof(double2) * ((size_t)k * k + k + (size_t)INV_COLS * k);
-  if ((e = cudaFuncSetAttribute(k_acc_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smi)) != cudaSuccess)
-    return e;
-  k_acc_inverse<<<(unsigned)((k + INV_COLS - 1) / INV_COLS), 32 * INV_COLS, smi, st>>>(LU, ldlu, piv, d_d, k, L.V);
-  k_W_init<<<dim3((unsigned)((h->ldm + 255) / 256), (unsigned)k), 256, 0, st>>>(L.W, h->ldm, n, z, k);
+  if ((e = accept_tc_start<float2>(h, f, v, Einc, d_s, d_d, k)) != cudaSuccess) return e;
   const unsigned gb = (unsigned)((n + PB_M - 1) / PB_M);
   k_pend_block<true><<<gb, 256, 0, st>>>(v.T, v.ldt, v.U, v.Vt, v.rcap, v.rp, n, d_s, k, L.Xs, h->ldm);
-  h->nlaunch += 3;
+  h->nlaunch += 1;
   if ((e = launch_f64tc_wgemm(h, f, k, L.V, L.Xs, false, h->ldm, h->d_iota, L.W)) != cudaSuccess) return e;
   k_pend_block<false><<<gb, 256, 0, st>>>(v.T, v.ldt, v.U, v.Vt, v.rcap, v.rp, n, d_s, k, L.A, rows);
   if (rows > n)
